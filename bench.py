@@ -1,0 +1,318 @@
+"""Benchmark of the GB300 volumetric path tracer (plain path, BASELINE configuration 2).
+
+One step = one launch of the plain tracer over the whole 1024x1024 image at STEP_SPP samples
+per pixel on the sparse 512^3 fBm cloud (sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256
+bounces, sun at 20 degrees + Hosek-Wilkie sky). Metric: paths/s = pixels * spp / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2|c1]
+
+`--impl reference` times the reference's per-path CPU algorithm on the host cores. The reference's
+own implementation (OptiX raygen + tiny-cuda-nn) cannot be built on this platform, so the arm runs
+the project's CPU restatement of it (the oracle), with all host threads, on a bounded sample of
+the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+STEP_SPP = 4
+L2_FLUSH_BYTES = 512 << 20   # larger than the 129 MB L2
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _profile_traffic(kernel_key: str, workload: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/*.md
+    (a line `traffic_bytes_per_launch[<kernel>/<workload>]: <bytes>`)."""
+    pat = re.compile(r"traffic_bytes_per_launch\[" + re.escape(kernel_key) + "/" + re.escape(workload) +
+                     r"\]:\s*([0-9.eE+]+)")
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = pat.search(f.read_text())
+        if m:
+            return float(m.group(1)), f.name
+    return None, None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        cmd = ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.uuid:
+            cmd += ["-i", self.uuid]
+        try:
+            self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc:
+            time.sleep(0.25)
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return None
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _cfg(name):
+    from rtc8_gb300.configs import C1, C2
+    return {"c1": C1, "c2": C2}[name]
+
+
+def _workload_name(cfg):
+    v = cfg.volume
+    return (f"{cfg.name}: plain volumetric path tracing, {cfg.width}x{cfg.height}, {STEP_SPP} spp per step, "
+            f"fBm {v.n}^3 ({'sparse, threshold ' + str(v.threshold) if v.threshold > 0 else 'dense'}), "
+            f"sigma_t max {v.sigma_t_max}, albedo {cfg.albedo}, HG g {cfg.phase_param}, <= {cfg.max_bounces} bounces, "
+            f"sun {cfg.sun_elevation_deg} deg + {'Hosek-Wilkie sky' if cfg.sky else 'constant env'}")
+
+
+# ------------------------------------------------------------------------------ CPU legs
+def cpu_sample(cfg, vox: np.ndarray, env_rgb: np.ndarray | None, target_seconds: float = 12.0, threads: int = 0):
+    """Times the oracle (all host threads) on a bounded sample of the workload: whole image rows
+    spread over the frame, 1 sample per pixel, sized to about `target_seconds`."""
+    from oracle import orc
+
+    threads = threads or (os.cpu_count() or 1)
+    sc = orc.scene_from_config(cfg, vox, env_rgb)
+    rng = orc.seed_states(cfg.width, cfg.height, cfg.rng_seed)
+    # probe with a few rows, then size the sample
+    rows = 0
+    elapsed = 0.0
+    row_step = 8
+    y = 0
+    chunk = max(threads, 8)
+    while elapsed < target_seconds and y < cfg.height:
+        ys = list(range(y, min(cfg.height, y + chunk * row_step), row_step))
+        t0 = time.perf_counter()
+        for yy in ys:
+            orc.render_plain(sc, rng, 1, rows=(yy, yy + 1), threads=threads)
+        elapsed += time.perf_counter() - t0
+        rows += len(ys)
+        y += chunk * row_step
+    paths = rows * cfg.width
+    return {"value": paths / elapsed, "unit": "paths/s", "cores": threads, "kind": "port",
+            "sample": f"{rows} rows x {cfg.width} px x 1 spp of {cfg.name} ({paths} paths, {elapsed:.1f} s), "
+                      f"oracle restatement with OpenMP"}
+
+
+def scene_host_inputs(cfg):
+    """Dense volume and environment image of a configuration, generated by the product on the
+    GPU and copied to the host for the CPU legs."""
+    from rtc8_gb300.renderer import Renderer, setup_scene
+
+    r = Renderer(16, 16)
+    setup_scene(r, cfg)
+    vox = r.download_volume()
+    env = None
+    if cfg.sky is not None:
+        env = r.download_environment(cfg.sky.width, cfg.sky.height)
+    elif cfg.env_constant is not None:
+        from rtc8_gb300.renderer import constant_environment
+        env = constant_environment(cfg.env_constant)
+    r.close()
+    return vox, env
+
+
+# ------------------------------------------------------------------------------ main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    warmup = max(args.warmup, 3)
+
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    cfg = _cfg(args.config)
+    workload = _workload_name(cfg)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        torch.cuda.set_device(local)
+        vox, env = scene_host_inputs(cfg)
+        vals = []
+        sample = None
+        for _ in range(args.warmup + args.steps):
+            s = cpu_sample(cfg, vox, env, target_seconds=max(2.0, 60.0 / max(1, args.warmup + args.steps)))
+            vals.append(s["value"])
+            sample = s
+        v = statistics.mean(vals[args.warmup:]) if args.steps else vals[-1]
+        line = {"impl": "reference", "metric": "paths/s (plain volumetric path tracing)", "value": v,
+                "unit": "paths/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 * cfg.width * cfg.height * STEP_SPP / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": workload},
+                "cpu_baseline": {"value": v, "unit": "paths/s", "cores": sample["cores"], "kind": "port",
+                                 "sample": sample["sample"]},
+                "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    from rtc8_gb300.renderer import Renderer, setup_scene
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg)
+    info = r.volume_info()
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    pinned = torch.empty(cfg.height * cfg.width * 3, dtype=torch.float32, pin_memory=True)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+
+    # ---- device-timed steps (inputs resident in HBM)
+    for _ in range(warmup):
+        flush_l2()
+        r.launch_plain(STEP_SPP, sptr)
+    torch.cuda.synchronize()
+    r.reset_counters()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev).uuid)
+        uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+    except Exception:
+        uuid = None
+    with ClockSampler(uuid) as clk:
+        for i in range(args.steps):
+            flush_l2()
+            ev[i][0].record(stream)
+            r.launch_plain(STEP_SPP, sptr)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    cnt = r.counters()
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    paths_per_rank = cfg.width * cfg.height * STEP_SPP * args.steps
+    value = world * paths_per_rank / (total_ms / 1000.0)
+
+    # ---- end to end through the C ABI with host buffers (result image read back every step)
+    lib = r.lib
+    import ctypes as C
+    e2e_ms = []
+    d2h = cfg.height * cfg.width * 3 * 4
+    h2d = C.sizeof(r.params)
+    for i in range(warmup + args.steps):
+        flush_l2()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.set_frame(r.params)                   # per-frame parameters from the host
+        r.launch_plain(STEP_SPP, sptr)
+        lib.vpt_download_mean(r.ctx, C.cast(pinned.data_ptr(), C.POINTER(C.c_float)))
+        t1 = time.perf_counter()
+        if i >= warmup:
+            e2e_ms.append(1000.0 * (t1 - t0))
+    e2e_total = sum(e2e_ms)
+    e2e_value = world * paths_per_rank / (e2e_total / 1000.0)
+
+    # ---- roofline of the tracer kernel (algorithmic bytes per launch / average launch time)
+    lookups_per_launch = cnt["lookups"] / args.steps
+    pixels = cfg.width * cfg.height
+    alg_bytes = 32.0 * lookups_per_launch + 88.0 * pixels
+    achieved = alg_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    peak, peak_kind = _peaks()
+    traffic, prof = _profile_traffic("plain_trace_kernel", args.config)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs", "traffic_source": prof,
+                "algorithmic_bytes_per_launch": alg_bytes, "lookups_per_launch": lookups_per_launch}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        vox, env = scene_host_inputs(cfg)
+        cpu = cpu_sample(cfg, vox, env, target_seconds=12.0)
+
+    if rank == 0:
+        line = {"metric": "paths/s (plain volumetric path tracing)", "value": value, "unit": "paths/s",
+                "n_gpus": world, "steps": args.steps, "warmup": warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded fBm volume generated on the device)",
+                "config": {"workload": workload, "spp_per_step": STEP_SPP, "l2": "flushed between steps "
+                           f"({L2_FLUSH_BYTES >> 20} MB write)", "active_leaves": info["active_leaves"],
+                           "total_leaves": info["total_leaves"], "parallelism": f"replicas x{world}"},
+                "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": args.steps,
+                "roofline": roofline,
+                "cpu_baseline": cpu,
+                "clocks": clk.summary(),
+                "counters": {"lookups": cnt["lookups"], "vertices": cnt["vertices"], "samples": cnt["samples"]},
+                "device_errors": r.device_errors()}
+        print(json.dumps(line), flush=True)
+    r.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * rtc8_vpt.h — C ABI of the GB300 volumetric path tracer (plain and NRC render paths).
+ *
+ * This surface replaces the reference renderer's per-frame launch entry points
+ * (shocker-0x15/rtcamp8):
+ *   - the OptiX ray-generation programs pathTrace / generateTrainingData / pathTraceWithNRC
+ *     (renderer/gpu_kernels/optix_pathtracing_kernels.cu:438-448), launched by
+ *     optixPipeline.launch(stream, plp, w, h, 1) (renderer/renderer_main.cpp:1575-1577,
+ *     1622-1624, 1640-1642);
+ *   - the CUDA kernels prepareNRC, propagateRadianceValues, shuffleTrainingData and
+ *     accumulateInferredRadianceValues (renderer/gpu_kernels/nrc_set_up_kernels.cu:4, 46,
+ *     88, 176), launched with block 32 (renderer/renderer_main.cpp:1564-1592, 1635-1636);
+ *   - the launch-parameter block PipelineLaunchParameters (renderer/renderer_shared.h:113-172),
+ *     which becomes the opaque VptContext plus the POD structs below.
+ *
+ * Conventions: every call returns VPT_OK (0) or a negative VPT_ERR_* code (no exceptions
+ * cross the ABI); `stream` is a cudaStream_t passed as void* (NULL = legacy default stream);
+ * launches are asynchronous on that stream; a context is not thread-safe (the reference
+ * renderer drives its pipeline from one host thread, renderer_main.cpp:1453-1454).
+ */
+#ifndef RTC8_VPT_H
+#define RTC8_VPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VPT_OK 0
+#define VPT_ERR_INVALID_ARGUMENT (-1)
+#define VPT_ERR_CUDA (-2)
+#define VPT_ERR_NOT_READY (-3)
+#define VPT_ERR_OUT_OF_MEMORY (-4)
+#define VPT_ERR_DEVICE_FAULT_FLAG (-5)
+
+/* Device-side error bits reported by vpt_get_device_errors(). */
+#define VPT_DEVERR_STEP_CAP 0x1u      /* a tracking segment hit max_steps_per_segment */
+#define VPT_DEVERR_NONFINITE 0x2u     /* a non-finite sample contribution was dropped */
+#define VPT_DEVERR_TRAIN_FULL 0x4u    /* the training-vertex buffer overflowed */
+
+typedef struct VptContext VptContext;
+
+/* renderer_shared.h:144-167 (PerFramePipelineLaunchParameters) restricted to volumes, plus the
+ * path rules and light model of the GB300 configurations. */
+typedef struct VptFrameParams {
+    /* PerspectiveCamera (common/common_renderer_types.h:1019-1034) */
+    float cam_aspect;
+    float cam_fovy;              /* radians */
+    float cam_position[3];
+    float cam_orientation[4];    /* quaternion x, y, z, w */
+
+    float density_coeff;         /* sigma_t scale: sigma_t(x) = density_coeff * grid(x) */
+    float scattering_albedo;
+    int32_t phase_kind;          /* 0 = Schlick (reference), 1 = Henyey-Greenstein */
+    float phase_param;           /* Schlick k (scatteringForwardness) or HG g */
+    float radiance_scale;        /* NRC target scale (renderer_shared.h:160); <= 0 = off */
+
+    int32_t env_enabled;
+    float env_power;             /* powerCoeff */
+    float env_rotation;          /* radians */
+
+    int32_t sun_enabled;
+    float sun_direction[3];      /* unit vector towards the sun */
+    float sun_irradiance[3];
+    float sun_select_prob;
+
+    int32_t max_bounces;         /* 0 = no cap (reference) */
+    int32_t rr_start_vertex;     /* Russian roulette from this path length (reference: 1) */
+    int32_t majorant_mode;       /* 0 = global majorant (reference), 1 = 8^3 majorant grid DDA */
+    int32_t max_steps_per_segment;  /* safety cap on lookups per segment (0 = none) */
+} VptFrameParams;
+
+/* ---- context ------------------------------------------------------------------------ */
+int vpt_create(int32_t image_width, int32_t image_height, VptContext** out);
+int vpt_destroy(VptContext* ctx);
+const char* vpt_last_error(void);
+
+/* Per-pixel PCG32 states from one std::mt19937_64(seed) stream in row-major order
+ * (renderer_main.cpp:86-93 uses seed 591842031321323413). Resets the accumulation. */
+int vpt_seed_rng(VptContext* ctx, uint64_t seed);
+int vpt_set_rng_states(VptContext* ctx, const uint64_t* host_states);
+int vpt_get_rng_states(VptContext* ctx, uint64_t* host_states);
+
+/* ---- scene data --------------------------------------------------------------------- */
+/* Density grid from a dense voxel array (x-major: index = (x*ny + y)*nz + z) given as a HOST
+ * pointer (vpt_set_volume_dense) or a DEVICE pointer (vpt_set_volume_dense_device). The grid
+ * is stored on the device as NanoVDB-style 8^3 leaves (values ordered x<<6|y<<3|z) reached
+ * through a dense leaf table; all-zero leaves are not stored. World position of voxel index
+ * (i,j,k) is origin + (i,j,k) * voxel_size; the clip box is [origin, origin + n * voxel_size].
+ * Replaces Scene::allocateVolumeGrid (renderer/renderer_scene.cpp:491-537), including its
+ * global majorant scan over [min, max) of the index box (:498-509). */
+int vpt_set_volume_dense(VptContext* ctx, const float* host_voxels, int32_t nx, int32_t ny,
+                         int32_t nz, float voxel_size, const float origin[3]);
+int vpt_set_volume_dense_device(VptContext* ctx, const float* dev_voxels, int32_t nx, int32_t ny,
+                                int32_t nz, float voxel_size, const float origin[3]);
+/* Seeded fBm value-noise volume generated on the device (octaves, lacunarity, gain, base
+ * frequency in lattice cells across the grid). Values are remapped so min..max -> [0,1];
+ * with threshold > 0 they become max(0, (r - threshold) / (1 - threshold)). */
+int vpt_generate_fbm_volume(VptContext* ctx, int32_t n, uint32_t seed, int32_t octaves,
+                            float lacunarity, float gain, float base_frequency, float threshold,
+                            float voxel_size, const float origin[3]);
+/* Copies the dense voxel values of the last generated/uploaded volume to the host (n^3 floats);
+ * only valid until the next volume call. */
+int vpt_download_volume_dense(VptContext* ctx, float* host_voxels);
+/* Grid statistics: active leaves, total leaves, global majorant, device bytes of the grid. */
+int vpt_get_volume_info(VptContext* ctx, int64_t* active_leaves, int64_t* total_leaves,
+                        float* global_majorant, int64_t* grid_bytes);
+/* Per-cell majorants (one per 8^3 leaf cell, max over the cell's voxels plus a one-voxel
+ * apron on every side) as a host copy of cx*cy*cz floats. */
+int vpt_download_cell_majorants(VptContext* ctx, float* host_cells);
+
+/* Image-based environment from an RGB float image (row-major, rows = polar angle from +y).
+ * Builds the hierarchical importance map on the device (compute_light_probs.cu:161-211). */
+int vpt_set_environment_rgb(VptContext* ctx, const float* host_rgb, int32_t width, int32_t height);
+/* Reads the importance mip chain back (size returned by vpt_get_importance_map_info). */
+int vpt_get_importance_map_info(VptContext* ctx, int32_t* map_w, int32_t* map_h, int32_t* num_mips,
+                                int64_t* total_texels, float* integral);
+int vpt_download_importance_map(VptContext* ctx, float* host_mips);
+
+/* Hosek-Wilkie sky texture (renderer/gpu_kernels/analytic_sky_kernels.cu:220-276) from
+ * per-band model states computed on the host (16 bands). `states` holds, per band:
+ * configs[11][9], radiances[11], emission_correction_factor_sky[11], solar_radius (122 floats);
+ * `solar` holds per band the direct solar radiance at the sun's elevation before limb darkening
+ * followed by 6 limb-darkening coefficients (7 floats). `cmf` holds xs[16], ys[16], zs[16],
+ * center wavelengths[16] and the CMF integral (65 floats). include_solar_disc = 0 leaves the
+ * disc out (the configurations model the sun as a separate delta light). */
+int vpt_generate_sky(VptContext* ctx, int32_t width, int32_t height, const float* states,
+                     const float* solar, const float* cmf, const float sun_direction[3],
+                     int32_t include_solar_disc);
+int vpt_download_environment(VptContext* ctx, float* host_rgb);
+
+/* ---- per-frame parameters ----------------------------------------------------------- */
+int vpt_set_frame_params(VptContext* ctx, const VptFrameParams* params);
+
+/* ---- plain path tracing (pathTrace raygen, optix_pathtracing_kernels.cu:438-440) -------- */
+/* Traces `spp` samples per pixel, continuing each pixel's PCG32 stream, and accumulates
+ * into the FP64 sum buffer and the reference's FP32 running mean (numAccumFrames counts
+ * previous samples). Persistent kernel, one CTA set per SM, pixels handed out dynamically. */
+int vpt_launch_plain(VptContext* ctx, void* stream, uint32_t spp);
+/* Same as vpt_launch_plain, additionally writing a per-sample decision record (4 x u32:
+ * path vertices, primary lookups, shadow lookups, end code) to a device buffer of
+ * width*height*spp*4 u32, sample s of pixel p at (p*spp + s). */
+int vpt_launch_plain_logged(VptContext* ctx, void* stream, uint32_t spp, uint32_t* dev_log);
+int vpt_reset_accumulation(VptContext* ctx);
+
+/* Reads back the accumulation: FP64 per-pixel RGB sums and sample count, FP32 running mean. */
+int vpt_download_sum(VptContext* ctx, double* host_rgb, uint32_t* num_samples);
+int vpt_download_mean(VptContext* ctx, float* host_rgb);
+/* Device pointers of the accumulation buffers (FP64 sum, FP32 mean; 3 values per pixel). */
+int vpt_get_accum_device_ptrs(VptContext* ctx, double** dev_sum, float** dev_mean);
+
+/* Work counters of the last launches since the last reset: density lookups, path vertices,
+ * samples. Enabled by default; read back with a synchronisation. */
+int vpt_get_counters(VptContext* ctx, uint64_t* lookups, uint64_t* vertices, uint64_t* samples);
+int vpt_reset_counters(VptContext* ctx);
+uint32_t vpt_get_device_errors(VptContext* ctx);
+int vpt_synchronize(VptContext* ctx, void* stream);
+
+/* Launch shape of the persistent tracker (CTAs per SM, threads per CTA); 0 = defaults. */
+int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTC8_VPT_H */

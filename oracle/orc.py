@@ -1,0 +1,219 @@
+"""ctypes binding of the oracle library (test infrastructure only; see oracle/vpt_oracle.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+
+
+class OrcScene(C.Structure):
+    _fields_ = [
+        ("voxels", f32p), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("inv_voxel_size", C.c_float), ("origin", C.c_float * 3),
+        ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
+        ("global_majorant", C.c_float), ("cell_majorant", f32p),
+        ("cx", C.c_int32), ("cy", C.c_int32), ("cz", C.c_int32),
+        ("density_coeff", C.c_float), ("albedo", C.c_float),
+        ("phase_kind", C.c_int32), ("phase_param", C.c_float),
+        ("env_enabled", C.c_int32), ("env_rgb", f32p), ("env_w", C.c_int32), ("env_h", C.c_int32),
+        ("env_power", C.c_float), ("env_rotation", C.c_float),
+        ("imp_mips", f32p), ("imp_offsets", i64p), ("map_w", C.c_int32), ("map_h", C.c_int32),
+        ("num_mips", C.c_int32), ("imp_integral", C.c_float),
+        ("sun_enabled", C.c_int32), ("sun_dir", C.c_float * 3), ("sun_irradiance", C.c_float * 3),
+        ("sun_prob", C.c_float),
+        ("world_radius", C.c_float), ("world_min", C.c_float * 3), ("world_max", C.c_float * 3),
+        ("cam_aspect", C.c_float), ("cam_fovy", C.c_float), ("cam_pos", C.c_float * 3), ("cam_quat", C.c_float * 4),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("max_bounces", C.c_int32), ("rr_start", C.c_int32), ("majorant_mode", C.c_int32), ("max_steps", C.c_int32),
+    ]
+
+
+_FUNCS = {
+    "orc_version": (C.c_int, []),
+    "orc_seed_states": (None, [C.c_int32, C.c_int32, C.c_uint64, u64p]),
+    "orc_pcg_floats": (None, [C.c_uint64, C.c_int32, f32p, u64p]),
+    "orc_imp_map_size": (C.c_int64, [C.c_int32, C.c_int32, i32p, i32p, i32p, i64p]),
+    "orc_build_imp_map": (C.c_float, [f32p, C.c_int32, C.c_int32, f32p]),
+    "orc_majorants": (C.c_float, [f32p, C.c_int32, C.c_int32, C.c_int32, f32p]),
+    "orc_sample_density": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p]),
+    "orc_clip_rays": (None, [C.POINTER(OrcScene), f32p, f32p, C.c_int32, f32p, f32p, i32p]),
+    "orc_env_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p, f32p]),
+    "orc_env_evaluate": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p]),
+    "orc_phase_sample": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p, f32p]),
+    "orc_phase_eval": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p]),
+    "orc_polar_yup": (None, [f32p, C.c_int32, f32p]),
+    "orc_coordinate_system": (None, [f32p, C.c_int32, f32p]),
+    "orc_quat_to_matrix": (None, [f32p, f32p]),
+    "orc_render_plain": (C.c_int64, [C.POINTER(OrcScene), u64p, C.c_int32, C.c_int32, f64p, f32p, u32p, C.c_int32,
+                                     C.c_int32, C.c_int32]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        for name, (res, args) in _FUNCS.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def seed_states(width: int, height: int, seed: int) -> np.ndarray:
+    out = np.empty(width * height, dtype=np.uint64)
+    lib().orc_seed_states(width, height, C.c_uint64(seed), p(out, C.c_uint64))
+    return out
+
+
+def pcg_floats(state: int, n: int) -> tuple[np.ndarray, int]:
+    out = np.empty(n, dtype=np.float32)
+    st = C.c_uint64()
+    lib().orc_pcg_floats(C.c_uint64(state), n, p(out, C.c_float), C.byref(st))
+    return out, st.value
+
+
+def importance_map(env_rgb: np.ndarray) -> tuple[np.ndarray, np.ndarray, dict]:
+    img = np.ascontiguousarray(env_rgb, dtype=np.float32)
+    h, w, _ = img.shape
+    mw, mh, nm = C.c_int32(), C.c_int32(), C.c_int32()
+    offs = np.zeros(32, dtype=np.int64)
+    total = lib().orc_imp_map_size(w, h, C.byref(mw), C.byref(mh), C.byref(nm), p(offs, C.c_int64))
+    mips = np.zeros(total, dtype=np.float32)
+    integral = lib().orc_build_imp_map(p(img, C.c_float), w, h, p(mips, C.c_float))
+    return mips, offs, {"map_w": mw.value, "map_h": mh.value, "num_mips": nm.value, "integral": float(integral)}
+
+
+def majorants(vox: np.ndarray) -> tuple[np.ndarray, float]:
+    v = np.ascontiguousarray(vox, dtype=np.float32)
+    nx, ny, nz = v.shape
+    cells = np.zeros(((nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8), dtype=np.float32)
+    g = lib().orc_majorants(p(v, C.c_float), nx, ny, nz, p(cells, C.c_float))
+    return cells, float(g)
+
+
+@dataclass
+class OracleScene:
+    """Keeps the arrays referenced by an OrcScene alive."""
+    scene: OrcScene
+    keep: list
+
+    @property
+    def ref(self):
+        return C.byref(self.scene)
+
+
+def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: float, albedo: float,
+               phase_kind: int, phase_param: float, env_rgb: np.ndarray | None, width: int, height: int,
+               cam_aspect: float, cam_fovy: float, cam_pos, cam_quat, sun_dir=None, sun_irradiance=0.0,
+               sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, env_power=1.0,
+               env_rotation=0.0, cells: np.ndarray | None = None, global_majorant: float | None = None) -> OracleScene:
+    s = OrcScene()
+    v = np.ascontiguousarray(voxels, dtype=np.float32)
+    keep = [v]
+    s.voxels = p(v, C.c_float)
+    s.nx, s.ny, s.nz = v.shape
+    s.inv_voxel_size = float(np.float32(1.0 / float(voxel_size)))
+    o = np.asarray(origin, dtype=np.float32)
+    n = np.array(v.shape, dtype=np.float64)
+    bmax = (o.astype(np.float64) + n * float(np.float32(voxel_size))).astype(np.float32)
+    for a in range(3):
+        s.origin[a] = float(o[a])
+        s.bbox_min[a] = float(o[a])
+        s.bbox_max[a] = float(bmax[a])
+        s.world_min[a] = float(o[a])
+        s.world_max[a] = float(bmax[a])
+    center = (o + bmax) * np.float32(0.5)
+    d = (bmax - center).astype(np.float32)
+    s.world_radius = float(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])))
+    if cells is None or global_majorant is None:
+        cells, global_majorant = majorants(v)
+    cells = np.ascontiguousarray(cells, dtype=np.float32)
+    keep.append(cells)
+    s.global_majorant = global_majorant
+    s.cell_majorant = p(cells, C.c_float)
+    s.cx, s.cy, s.cz = cells.shape
+    s.density_coeff = density_coeff
+    s.albedo = albedo
+    s.phase_kind = phase_kind
+    s.phase_param = phase_param
+    if env_rgb is not None:
+        img = np.ascontiguousarray(env_rgb, dtype=np.float32)
+        mips, offs, info = importance_map(img)
+        keep += [img, mips, offs]
+        s.env_enabled = 1
+        s.env_rgb = p(img, C.c_float)
+        s.env_h, s.env_w = img.shape[:2]
+        s.env_power = env_power
+        s.env_rotation = env_rotation
+        s.imp_mips = p(mips, C.c_float)
+        s.imp_offsets = p(offs, C.c_int64)
+        s.map_w, s.map_h, s.num_mips = info["map_w"], info["map_h"], info["num_mips"]
+        s.imp_integral = info["integral"]
+    if sun_dir is not None:
+        s.sun_enabled = 1
+        for a in range(3):
+            s.sun_dir[a] = float(sun_dir[a])
+            s.sun_irradiance[a] = float(sun_irradiance)
+        s.sun_prob = sun_prob if env_rgb is not None else 1.0
+    s.cam_aspect = cam_aspect
+    s.cam_fovy = cam_fovy
+    for a in range(3):
+        s.cam_pos[a] = float(cam_pos[a])
+    for a in range(4):
+        s.cam_quat[a] = float(cam_quat[a])
+    s.width, s.height = width, height
+    s.max_bounces, s.rr_start, s.majorant_mode, s.max_steps = max_bounces, rr_start, majorant_mode, max_steps
+    return OracleScene(s, keep)
+
+
+def scene_from_config(cfg, voxels: np.ndarray, env_rgb: np.ndarray | None, **over) -> OracleScene:
+    """OrcScene for a rtc8_gb300.configs.SceneConfig (same camera, lights and path rules)."""
+    from rtc8_gb300.configs import camera_for, sun_direction, volume_box
+    vs, origin = volume_box(cfg.volume)
+    cam = camera_for(cfg)
+    sun = None if cfg.sun_elevation_deg is None else sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg)
+    kw = dict(voxels=voxels, voxel_size=vs, origin=origin, density_coeff=cfg.volume.sigma_t_max, albedo=cfg.albedo,
+              phase_kind=cfg.phase_kind, phase_param=cfg.phase_param, env_rgb=env_rgb, width=cfg.width,
+              height=cfg.height, cam_aspect=cam.aspect, cam_fovy=cam.fovy,
+              cam_pos=np.asarray(cam.position, dtype=np.float32), cam_quat=np.asarray(cam.orientation, np.float32),
+              sun_dir=None if sun is None else sun.astype(np.float32), sun_irradiance=cfg.sun_irradiance,
+              sun_prob=cfg.sun_select_prob, max_bounces=cfg.max_bounces, rr_start=cfg.rr_start_vertex,
+              majorant_mode=cfg.majorant_mode, max_steps=cfg.max_steps_per_segment)
+    kw.update(over)
+    return make_scene(**kw)
+
+
+def render_plain(sc: OracleScene, rng: np.ndarray, spp: int, accum_base: int = 0, rows=None, threads: int = 0,
+                 sum_rgb=None, mean_rgb=None, log: bool = False):
+    s = sc.scene
+    r0, r1 = (0, s.height) if rows is None else rows
+    if sum_rgb is None:
+        sum_rgb = np.zeros((s.height, s.width, 3), dtype=np.float64)
+    if mean_rgb is None:
+        mean_rgb = np.zeros((s.height, s.width, 3), dtype=np.float32)
+    dlog = np.zeros((s.height * s.width, spp, 4), dtype=np.uint32) if log else None
+    n = lib().orc_render_plain(sc.ref, p(rng, C.c_uint64), accum_base, spp, p(sum_rgb, C.c_double),
+                               p(mean_rgb, C.c_float), p(dlog, C.c_uint32) if log else None, r0, r1, threads)
+    return {"sum": sum_rgb, "mean": mean_rgb, "log": dlog, "lookups": int(n)}

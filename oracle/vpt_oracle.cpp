@@ -1,0 +1,858 @@
+/*
+ * ORACLE (test infrastructure only) — CPU restatement of the reference's plain volumetric
+ * path tracer. See vpt_oracle.h for the parity status. Citations are file:line within the
+ * reference project (shocker-0x15/rtcamp8).
+ *
+ * Built with -ffp-contract=off so x86-64 and aarch64 hosts produce identical bits.
+ * Random-draw order where the reference leaves it unspecified (two rng draws as arguments
+ * of one call: optix_pathtracing_kernels.cu:341, renderer_kernel_common.h:321-324) is pinned
+ * left to right: the first draw feeds the first parameter.
+ */
+#include "vpt_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr float kPi = 3.14159265358979323846f;
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+inline V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float length(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+// basic_types.h:850-853 and :817-820: v /= length() is a multiply by 1 / length.
+inline V3 normalize(V3 a) {
+    float r = 1.0f / length(a);
+    return a * r;
+}
+
+struct RGB {
+    float r, g, b;
+};
+inline RGB rgb(float r, float g, float b) { return RGB{r, g, b}; }
+inline RGB operator+(RGB a, RGB b) { return rgb(a.r + b.r, a.g + b.g, a.b + b.b); }
+inline RGB operator*(RGB a, RGB b) { return rgb(a.r * b.r, a.g * b.g, a.b * b.b); }
+inline RGB operator*(RGB a, float s) { return rgb(a.r * s, a.g * s, a.b * s); }
+inline RGB operator*(float s, RGB a) { return rgb(s * a.r, s * a.g, s * a.b); }
+// basic_types.h:2939-2942: RGB / s multiplies by 1 / s.
+inline RGB div(RGB a, float s) {
+    float r = 1.0f / s;
+    return a * r;
+}
+// basic_types.h:2981-2986.
+inline float luminance(RGB c) { return 0.2126729f * c.r + 0.7151522f * c.g + 0.0721750f * c.b; }
+inline bool all_nonneg_finite(RGB c) {
+    return std::isfinite(c.r) && std::isfinite(c.g) && std::isfinite(c.b) && c.r >= 0 && c.g >= 0 &&
+           c.b >= 0;
+}
+
+// common_renderer_types.h:101-125 (PCG32, XSH-RR output, 23-bit float trick).
+struct Pcg32 {
+    uint64_t state;
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + 1ULL;
+        uint32_t xorshifted = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = static_cast<uint32_t>(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((-static_cast<int32_t>(rot)) & 31));
+    }
+    float uniform() {
+        uint32_t bits = (next() >> 9) | 0x3f800000u;
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f - 1.0f;
+    }
+};
+
+// common_renderer_types.h:1379-1405 with basic_types.h:857-864 (Duff et al. basis).
+struct Frame {
+    V3 t, b, n;
+};
+inline Frame make_frame(V3 n) {
+    float sign = n.z >= 0 ? 1.0f : -1.0f;
+    float a = -1 / (sign + n.z);
+    float b = n.x * n.y * a;
+    Frame f;
+    f.t = v3(1 + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    f.b = v3(b, sign + n.y * n.y * a, -n.y);
+    f.n = n;
+    return f;
+}
+inline V3 to_local(const Frame& f, V3 v) { return v3(dot(f.t, v), dot(f.b, v), dot(f.n, v)); }
+inline V3 from_local(const Frame& f, V3 v) {
+    return v3(dot(v3(f.t.x, f.b.x, f.n.x), v), dot(v3(f.t.y, f.b.y, f.n.y), v),
+              dot(v3(f.t.z, f.b.z, f.n.z), v));
+}
+
+// basic_types.h:870-874 (theta from +y, phi = atan2(-x, z) wrapped to [0, 2pi)).
+inline void to_polar_yup(V3 v, float* theta, float* phi) {
+    *theta = std::acos(std::min(std::max(v.y, -1.0f), 1.0f));
+    *phi = std::fmod(std::atan2(-v.x, v.z) + 2 * kPi, 2 * kPi);
+}
+// basic_types.h:900-907.
+inline V3 from_polar_yup(float phi, float theta) {
+    float sp = std::sin(phi), cp = std::cos(phi);
+    float st = std::sin(theta), ct = std::cos(theta);
+    return v3(-sp * st, ct, cp * st);
+}
+
+// basic_types.h:1620-1628; matrix columns c0, c1, c2; M * v = (row_i . v) (:2131-2134).
+struct M3 {
+    V3 c0, c1, c2;
+};
+inline M3 quat_to_m3(const float q[4]) {
+    float x = q[0], y = q[1], z = q[2], w = q[3];
+    float xx = x * x, yy = y * y, zz = z * z;
+    float xy = x * y, yz = y * z, zx = z * x;
+    float xw = x * w, yw = y * w, zw = z * w;
+    M3 m;
+    m.c0 = v3(1 - 2 * (yy + zz), 2 * (xy + zw), 2 * (zx - yw));
+    m.c1 = v3(2 * (xy - zw), 1 - 2 * (xx + zz), 2 * (yz + xw));
+    m.c2 = v3(2 * (zx + yw), 2 * (yz - xw), 1 - 2 * (xx + yy));
+    return m;
+}
+inline V3 mul(const M3& m, V3 v) {
+    return v3(dot(v3(m.c0.x, m.c1.x, m.c2.x), v), dot(v3(m.c0.y, m.c1.y, m.c2.y), v),
+              dot(v3(m.c0.z, m.c1.z, m.c2.z), v));
+}
+
+// ---------------------------------------------------------------- density grid
+inline float voxel(const OrcScene& s, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || x >= s.nx || y >= s.ny || z >= s.nz) return 0.0f;
+    return s.voxels[(static_cast<int64_t>(x) * s.ny + y) * s.nz + z];
+}
+// NanoVDB.h:1409-1414 + :2029-2032 (applyInverseMapF for a scale/translate map).
+inline V3 world_to_index(const OrcScene& s, V3 p) {
+    return v3((p.x - s.origin[0]) * s.inv_voxel_size, (p.y - s.origin[1]) * s.inv_voxel_size,
+              (p.z - s.origin[2]) * s.inv_voxel_size);
+}
+// util/SampleFromVoxels.h:419-459 (first-order sampler, z then y then x lerps) and the
+// float Floor at :56-65.
+inline float sample_trilinear(const OrcScene& s, V3 xyz) {
+    float fi = std::floor(xyz.x), fj = std::floor(xyz.y), fk = std::floor(xyz.z);
+    float wx = xyz.x - fi, wy = xyz.y - fj, wz = xyz.z - fk;
+    int i = static_cast<int>(fi), j = static_cast<int>(fj), k = static_cast<int>(fk);
+    auto lerp = [](float a, float b, float w) { return a + w * (b - a); };
+    float vz = voxel(s, i, j, k);
+    float vz1 = voxel(s, i, j, k + 1);
+    float vy = lerp(vz, vz1, wz);
+    vz1 = voxel(s, i, j + 1, k + 1);
+    vz = voxel(s, i, j + 1, k);
+    float vy1 = lerp(vz, vz1, wz);
+    float vx = lerp(vy, vy1, wy);
+    vz = voxel(s, i + 1, j + 1, k);
+    vz1 = voxel(s, i + 1, j + 1, k + 1);
+    vy1 = lerp(vz, vz1, wz);
+    vz1 = voxel(s, i + 1, j, k + 1);
+    vz = voxel(s, i + 1, j, k);
+    vy = lerp(vz, vz1, wz);
+    float vx1 = lerp(vy, vy1, wy);
+    return lerp(vx, vx1, wx);
+}
+
+// util/Ray.h:343-363 (slab test clipped to the ray's time span) and :512-520 (clip).
+inline bool clip_ray(const float bmin[3], const float bmax[3], V3 eye, V3 dir, float tmin, float tmax,
+                     float* t0o, float* t1o) {
+    float inv[3] = {1 / dir.x, 1 / dir.y, 1 / dir.z};
+    float e[3] = {eye.x, eye.y, eye.z};
+    int sg[3] = {inv[0] < 0, inv[1] < 0, inv[2] < 0};
+    auto bb = [&](int side, int axis) { return side ? bmax[axis] : bmin[axis]; };
+    float t0 = (bb(sg[0], 0) - e[0]) * inv[0];
+    float t2 = (bb(1 - sg[1], 1) - e[1]) * inv[1];
+    if (t0 > t2) return false;
+    float t1 = (bb(1 - sg[0], 0) - e[0]) * inv[0];
+    float t3 = (bb(sg[1], 1) - e[1]) * inv[1];
+    if (t3 > t1) return false;
+    if (t3 > t0) t0 = t3;
+    if (t2 < t1) t1 = t2;
+    t3 = (bb(sg[2], 2) - e[2]) * inv[2];
+    if (t3 > t1) return false;
+    t2 = (bb(1 - sg[2], 2) - e[2]) * inv[2];
+    if (t0 > t2) return false;
+    if (t3 > t0) t0 = t3;
+    if (tmax < t0) return false;
+    if (t2 < t1) t1 = t2;
+    if (tmin > t1) return false;
+    if (tmin > t0) t0 = tmin;
+    if (tmax < t1) t1 = tmax;
+    *t0o = t0;
+    *t1o = t1;
+    return true;
+}
+
+// ---------------------------------------------------------------- phase functions
+// common_renderer_types.h:2063-2097 (Schlick); Henyey-Greenstein uses the same local
+// convention (dirLocal.z = -cos(theta), theta measured from the propagation direction).
+inline float phase_pdf(int kind, float g, V3 local) {
+    float cos_theta = -local.z;
+    if (kind == 0) {
+        float d = 1 - g * cos_theta;
+        return (1 - g * g) / (4 * kPi * (d * d));
+    }
+    float d = 1 + g * g - 2 * g * cos_theta;
+    return (1 - g * g) / (4 * kPi * (d * std::sqrt(d)));
+}
+inline float phase_sample(int kind, float g, float u0, float u1, V3* local) {
+    float cos_theta;
+    if (kind == 0) {
+        cos_theta = (2 * u1 + g - 1) / (2 * g * u1 - g + 1);
+    } else if (std::fabs(g) < 1e-3f) {
+        cos_theta = 1 - 2 * u1;
+    } else {
+        float sq = (1 - g * g) / (1 - g + 2 * g * u1);
+        cos_theta = (1 + g * g - sq * sq) / (2 * g);
+    }
+    cos_theta = std::min(std::max(cos_theta, -1.0f), 1.0f);
+    float phi = 2 * kPi * u0;
+    float value;
+    if (kind == 0) {
+        float d = 1 - g * cos_theta;
+        value = (1 - g * g) / (4 * kPi * (d * d));
+    } else {
+        float d = 1 + g * g - 2 * g * cos_theta;
+        value = (1 - g * g) / (4 * kPi * (d * std::sqrt(d)));
+    }
+    float sin_theta = std::sqrt(1 - cos_theta * cos_theta);
+    *local = v3(std::cos(phi) * sin_theta, std::sin(phi) * sin_theta, -cos_theta);
+    return value;
+}
+
+// ---------------------------------------------------------------- environment
+inline int env_texel_x(const OrcScene& s, float u) {
+    int x = static_cast<int>(u * s.env_w);
+    return std::min(std::max(x, 0), s.env_w - 1);
+}
+inline int env_texel_y(const OrcScene& s, float v) {
+    int y = static_cast<int>(v * s.env_h);
+    return std::min(std::max(y, 0), s.env_h - 1);
+}
+inline RGB env_texel(const OrcScene& s, int x, int y) {
+    const float* p = s.env_rgb + 3 * (static_cast<int64_t>(y) * s.env_w + x);
+    return rgb(p[0], p[1], p[2]);
+}
+inline float mip_texel(const OrcScene& s, int level, int x, int y) {
+    int w = std::max(s.map_w >> level, 1);
+    return s.imp_mips[s.imp_offsets[level] + static_cast<int64_t>(y) * w + x];
+}
+
+// common_renderer_types.h:479-548 (hierarchical mip walk from the 2x2 (or 2x1) level down).
+inline void imp_sample(const OrcScene& s, float u0, float u1, int* px, int* py, float* ru0,
+                       float* ru1, float* prob) {
+    int ix = 0, iy = 0;
+    *prob = 1;
+    int cur_w = 2, cur_h = s.map_w > s.map_h ? 1 : 2;
+    for (int level = s.num_mips - 2; level >= 0; --level) {
+        ix *= 2;
+        iy *= 2;
+        // Bounds tests as in the reference: texel centre + offset compared with the level's dims.
+        bool has_lower = (iy + 1.5f) < cur_h;
+        bool has_right = (ix + 1.5f) < cur_w;
+        float vul = mip_texel(s, level, ix, iy);
+        float vur = has_right ? mip_texel(s, level, ix + 1, iy) : 0.0f;
+        float vll = has_lower ? mip_texel(s, level, ix, iy + 1) : 0.0f;
+        float vlr = (has_right && has_lower) ? mip_texel(s, level, ix + 1, iy + 1) : 0.0f;
+        float left = vll + vul;
+        float right = vlr + vur;
+        u0 *= (left + right);
+        *prob *= 1.0f / (left + right);
+        float upper, lower;
+        if (u0 < left) {
+            u0 = (u0 - 0) / left;
+            upper = vul;
+            lower = vll;
+        } else {
+            ix += 1;
+            u0 = (u0 - left) / right;
+            upper = vur;
+            lower = vlr;
+        }
+        u1 *= (upper + lower);
+        if (u1 < upper) {
+            *prob *= upper;
+            u1 = (u1 - 0) / upper;
+        } else {
+            iy += 1;
+            *prob *= lower;
+            u1 = (u1 - upper) / lower;
+        }
+        cur_w *= 2;
+        cur_h *= 2;
+    }
+    *px = ix;
+    *py = iy;
+    *ru0 = u0;
+    *ru1 = u1;
+}
+
+// common_renderer_types.h:2419-2440 + :987-1000 (sample then rotate, power coefficient).
+inline RGB env_sample(const OrcScene& s, float u0, float u1, V3* dir, float* dir_pdf) {
+    float prob;
+    int px, py;
+    imp_sample(s, u0, u1, &px, &py, &u0, &u1, &prob);
+    float u = (px + u0) / s.env_w;
+    float v = (py + u1) / s.env_h;
+    float uv_pdf = static_cast<float>(static_cast<uint32_t>(s.env_w) * static_cast<uint32_t>(s.env_h)) * prob;
+    float phi = 2 * kPi * u;
+    float theta = kPi * v;
+    *dir_pdf = uv_pdf / (2 * (kPi * kPi) * std::sin(theta));
+    RGB radiance;
+    if (!std::isfinite(*dir_pdf)) {
+        *dir_pdf = 0.0f;
+        radiance = rgb(0, 0, 0);
+    } else {
+        radiance = env_texel(s, env_texel_x(s, u), env_texel_y(s, v));
+    }
+    radiance = s.env_power * radiance;
+    float pos_phi = phi - s.env_rotation;
+    pos_phi = pos_phi - std::floor(pos_phi / (2 * kPi)) * 2 * kPi;
+    *dir = from_polar_yup(pos_phi, theta);
+    return radiance;
+}
+
+// common_renderer_types.h:2442-2458 + :1002-1013.
+inline RGB env_evaluate(const OrcScene& s, V3 dir, float* hyp_pdf) {
+    float theta, pos_phi;
+    to_polar_yup(dir, &theta, &pos_phi);
+    float phi = pos_phi + s.env_rotation;
+    phi = phi - std::floor(phi / (2 * kPi)) * 2 * kPi;
+    float u = phi / (2 * kPi), v = theta / kPi;
+    int tx = env_texel_x(s, u), ty = env_texel_y(s, v);
+    RGB radiance = env_texel(s, tx, ty);
+    float prob = mip_texel(s, 0, tx, ty) / s.imp_integral;
+    float uv_pdf = static_cast<float>(static_cast<uint32_t>(s.env_w) * static_cast<uint32_t>(s.env_h)) * prob;
+    *hyp_pdf = uv_pdf / (2 * (kPi * kPi) * std::sin(theta));
+    if (!std::isfinite(*hyp_pdf)) {
+        *hyp_pdf = 0.0f;
+        radiance = rgb(0, 0, 0);
+    }
+    return s.env_power * radiance;
+}
+
+// ---------------------------------------------------------------- tracking
+// Result of tracking one segment.
+enum SegEnd { SEG_EXIT = 0, SEG_COLLIDE = 1, SEG_CAP = 2 };
+
+struct Counters {
+    int64_t lookups = 0;
+    uint32_t primary = 0, shadow = 0;
+};
+
+inline float density_at(const OrcScene& s, V3 eye, V3 dir, float t) {
+    V3 p = eye + dir * t;
+    return s.density_coeff * sample_trilinear(s, world_to_index(s, p));
+}
+
+// Majorant-grid DDA in index space (8^3-voxel cells). Shared definition with the device
+// tracker: overshooting a cell boundary restarts sampling at the boundary (memoryless).
+struct Dda {
+    int cell[3];
+    int step[3];
+    float tnext[3], tdelta[3];
+};
+inline void dda_init(const OrcScene& s, V3 eye, V3 dir, float t, Dda* d) {
+    float o[3] = {(eye.x - s.origin[0]) * s.inv_voxel_size, (eye.y - s.origin[1]) * s.inv_voxel_size,
+                  (eye.z - s.origin[2]) * s.inv_voxel_size};
+    float dd[3] = {dir.x * s.inv_voxel_size, dir.y * s.inv_voxel_size, dir.z * s.inv_voxel_size};
+    int cdim[3] = {s.cx, s.cy, s.cz};
+    for (int a = 0; a < 3; ++a) {
+        float p = o[a] + dd[a] * t;
+        int c = static_cast<int>(std::floor(p * 0.125f));
+        c = std::min(std::max(c, 0), cdim[a] - 1);
+        d->cell[a] = c;
+        if (dd[a] > 0) {
+            d->step[a] = 1;
+            d->tnext[a] = ((c + 1) * 8.0f - o[a]) / dd[a];
+            d->tdelta[a] = 8.0f / dd[a];
+        } else if (dd[a] < 0) {
+            d->step[a] = -1;
+            d->tnext[a] = (c * 8.0f - o[a]) / dd[a];
+            d->tdelta[a] = -8.0f / dd[a];
+        } else {
+            d->step[a] = 0;
+            d->tnext[a] = INFINITY;
+            d->tdelta[a] = INFINITY;
+        }
+    }
+}
+
+// Tracks [t, t1] along (eye, dir). Delta tracking (shadow = false) returns SEG_COLLIDE with
+// *t at the collision; ratio tracking (shadow = true) multiplies *vis.
+inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, float t1, bool shadow,
+                    float* vis, uint32_t* steps, int64_t* lookups) {
+    float t = *tio;
+    uint32_t seg_steps = 0;
+    if (s.majorant_mode == 0) {
+        // optix_pathtracing_kernels.cu:111-124 and renderer_kernel_common.h:372-381.
+        const float maj = s.density_coeff * s.global_majorant;
+        while (true) {
+            t += -std::log(1.0f - rng.uniform()) / maj;
+            if (t > t1) break;
+            float density = density_at(s, eye, dir, t);
+            ++*steps;
+            ++*lookups;
+            ++seg_steps;
+            if (shadow) {
+                *vis *= (1 - density / maj);
+            } else if (rng.uniform() < density / maj) {
+                *tio = t;
+                return SEG_COLLIDE;
+            }
+            if (s.max_steps > 0 && seg_steps >= static_cast<uint32_t>(s.max_steps)) return SEG_CAP;
+        }
+        *tio = t;
+        return SEG_EXIT;
+    }
+    Dda d;
+    dda_init(s, eye, dir, t, &d);
+    while (true) {
+        float texit = std::min(std::min(d.tnext[0], d.tnext[1]), std::min(d.tnext[2], t1));
+        int64_t ci = (static_cast<int64_t>(d.cell[0]) * s.cy + d.cell[1]) * s.cz + d.cell[2];
+        float maj = s.density_coeff * s.cell_majorant[ci];
+        if (maj > 0) {
+            while (true) {
+                float tt = t + -std::log(1.0f - rng.uniform()) / maj;
+                if (tt >= texit) break;
+                t = tt;
+                float density = density_at(s, eye, dir, t);
+                ++*steps;
+                ++*lookups;
+                ++seg_steps;
+                if (shadow) {
+                    *vis *= (1 - density / maj);
+                } else if (rng.uniform() < density / maj) {
+                    *tio = t;
+                    return SEG_COLLIDE;
+                }
+                if (s.max_steps > 0 && seg_steps >= static_cast<uint32_t>(s.max_steps)) return SEG_CAP;
+            }
+        }
+        t = texit;
+        if (texit >= t1) break;
+        int a = (d.tnext[0] <= d.tnext[1] && d.tnext[0] <= d.tnext[2]) ? 0 : (d.tnext[1] <= d.tnext[2] ? 1 : 2);
+        d.cell[a] += d.step[a];
+        int cdim[3] = {s.cx, s.cy, s.cz};
+        if (d.cell[a] < 0 || d.cell[a] >= cdim[a]) break;
+        d.tnext[a] += d.tdelta[a];
+    }
+    *tio = t1;
+    return SEG_EXIT;
+}
+
+// renderer_kernel_common.h:297-403 restricted to the environment light, plus the
+// directional sun of the config mode (picked with probability sun_prob, no MIS: delta light).
+inline RGB next_event(const OrcScene& s, Pcg32& rng, V3 pos, const Frame& fr, float* shadow_vis_out,
+                      uint32_t* shadow_steps, int64_t* lookups, bool* capped) {
+    float u_light = rng.uniform();
+    float u0 = rng.uniform();
+    float u1 = rng.uniform();
+    bool pick_sun = false;
+    float light_prob = 1.0f;
+    if (s.sun_enabled && s.env_enabled) {
+        if (u_light < s.sun_prob) {
+            pick_sun = true;
+            light_prob = s.sun_prob;
+        } else {
+            light_prob = 1.0f - s.sun_prob;
+        }
+    } else if (s.sun_enabled) {
+        pick_sun = true;
+    } else if (!s.env_enabled) {
+        return rgb(0, 0, 0);
+    }
+
+    V3 light_dir;
+    RGB emittance;
+    float area_pdf;
+    if (pick_sun) {
+        light_dir = v3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]);
+        emittance = rgb(s.sun_irradiance[0], s.sun_irradiance[1], s.sun_irradiance[2]);
+        area_pdf = light_prob;
+    } else {
+        float dir_pdf;
+        RGB radiance = env_sample(s, u0, u1, &light_dir, &dir_pdf);
+        emittance = kPi * radiance;
+        area_pdf = dir_pdf;
+        if (area_pdf == 0.0f) return rgb(0, 0, 0);
+        area_pdf *= light_prob;
+    }
+    V3 shadow_dir = -light_dir;
+    V3 light_normal = -light_dir;
+    float lp_cos = dot(shadow_dir, light_normal);
+    if (lp_cos <= 0.0f) return rgb(0, 0, 0);
+    float trace_len = 2 * s.world_radius;
+    V3 light_point = pos + trace_len * -shadow_dir;
+
+    float vis = 1.0f;
+    float t0, t1;
+    if (clip_ray(s.bbox_min, s.bbox_max, light_point, shadow_dir, 0.0f, trace_len, &t0, &t1)) {
+        float t = std::fmax(0.0f, t0);
+        if (track(s, rng, light_point, shadow_dir, &t, t1, true, &vis, shadow_steps, lookups) == SEG_CAP) {
+            *capped = true;
+            return rgb(0, 0, 0);
+        }
+    }
+    *shadow_vis_out = vis;
+    RGB ret = rgb(0, 0, 0);
+    if (vis > 0.0f) {
+        V3 v_in_local = to_local(fr, -shadow_dir);
+        float pf = phase_pdf(s.phase_kind, s.phase_param, v_in_local);
+        RGB fs = rgb(s.albedo, s.albedo, s.albedo) * pf;
+        if (pick_sun) {
+            ret = fs * emittance * (vis / area_pdf);
+        } else {
+            float bsdf_pdf = pf * lp_cos / 1.0f;
+            if (!std::isfinite(bsdf_pdf)) bsdf_pdf = 0.0f;
+            float light_pdf = area_pdf;
+            float mis = (light_pdf * light_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+            RGB le = div(emittance, kPi);
+            float g = lp_cos * 1.0f / 1.0f;
+            ret = fs * le * (vis * mis * g / area_pdf);
+        }
+    }
+    return ret;
+}
+
+// optix_pathtracing_kernels.cu:31-434 with withNRC = generateTrainingData = false.
+RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], int64_t* lookups) {
+    V3 origin, dir;
+    float dir_pdf;
+    {
+        float ux = rng.uniform();
+        float fx = (px + ux) / s.width;
+        float uy = rng.uniform();
+        float fy = (py + uy) / s.height;
+        float vh = 2 * std::tan(s.cam_fovy * 0.5f);
+        float vw = s.cam_aspect * vh;
+        float sensor_area = vw * vh;
+        origin = v3(s.cam_pos[0], s.cam_pos[1], s.cam_pos[2]);
+        V3 local = normalize(v3(vw * (-0.5f + fx), vh * (0.5f - fy), -1));
+        dir = normalize(mul(quat_to_m3(s.cam_quat), local));
+        float az = std::fabs(local.z);
+        dir_pdf = 1 / (az * az * az * sensor_area);
+    }
+    RGB contribution = rgb(0, 0, 0);
+    float inv = 1.0f / dir_pdf;
+    RGB throughput = rgb(1, 1, 1) * inv;
+    const float init_importance = luminance(throughput);
+    uint32_t path_length = 0;
+    uint32_t end_code = 0;
+    while (true) {
+        ++path_length;
+        bool collided = false;
+        float hit_dist = 1e10f;
+        float t0, t1;
+        if (clip_ray(s.bbox_min, s.bbox_max, origin, dir, 0.0f, hit_dist, &t0, &t1)) {
+            float t = std::fmax(0.0f, t0);
+            float unused = 1.0f;
+            SegEnd e = track(s, rng, origin, dir, &t, t1, false, &unused, &rec[1], lookups);
+            if (e == SEG_CAP) {
+                end_code = ORC_END_STEP_CAP;
+                break;
+            }
+            if (e == SEG_COLLIDE) {
+                collided = true;
+                hit_dist = t;
+            }
+        }
+        if (!collided) {
+            // optix_pathtracing_kernels.cu:130-174 (environment hit with MIS).
+            if (s.env_enabled) {
+                float hyp_pdf;
+                RGB radiance = env_evaluate(s, dir, &hyp_pdf);
+                float mis = 1.0f;
+                if (path_length > 1) {
+                    float light_pdf = (s.sun_enabled ? (1.0f - s.sun_prob) : 1.0f) * hyp_pdf;
+                    float bsdf_pdf = dir_pdf;
+                    mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+                }
+                contribution = contribution + throughput * (radiance * mis);
+            }
+            end_code = ORC_END_ESCAPE;
+            break;
+        }
+        V3 pos = origin + hit_dist * dir;
+        Frame fr = make_frame(-dir);
+
+        // Russian roulette (:254-268).
+        float continue_prob = 1.0f;
+        if (static_cast<int32_t>(path_length) >= s.rr_start) {
+            continue_prob = std::fmin(luminance(throughput) / init_importance, 1.0f);
+            if (rng.uniform() >= continue_prob) {
+                end_code = ORC_END_RR;
+                break;
+            }
+        }
+        throughput = div(throughput, continue_prob);
+
+        float vis;
+        bool capped = false;
+        RGB nee = next_event(s, rng, pos, fr, &vis, &rec[2], lookups, &capped);
+        if (capped) {
+            end_code = ORC_END_STEP_CAP;
+            break;
+        }
+        contribution = contribution + throughput * nee;
+
+        if (s.max_bounces > 0 && static_cast<int32_t>(path_length) >= s.max_bounces) {
+            end_code = ORC_END_MAX_BOUNCES;
+            break;
+        }
+        float u0 = rng.uniform();
+        float u1 = rng.uniform();
+        V3 local;
+        float pdf = phase_sample(s.phase_kind, s.phase_param, u0, u1, &local);
+        if (pdf == 0.0f) {
+            end_code = ORC_END_PDF_ZERO;
+            break;
+        }
+        RGB fs = rgb(s.albedo, s.albedo, s.albedo) * pdf;
+        dir = from_local(fr, local);
+        RGB local_tp = fs * (std::fabs(1.0f) / pdf);
+        throughput = throughput * local_tp;
+        origin = pos;
+        dir_pdf = pdf;
+    }
+    rec[0] = path_length;
+    rec[3] = end_code;
+    return contribution;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_version(void) { return 1; }
+
+// renderer_main.cpp:86-93: one std::mt19937_64 stream, row-major pixel order.
+void orc_seed_states(int32_t width, int32_t height, uint64_t seed, uint64_t* out) {
+    std::mt19937_64 gen(seed);
+    for (int64_t i = 0; i < static_cast<int64_t>(width) * height; ++i) out[i] = gen();
+}
+
+void orc_pcg_floats(uint64_t state, int32_t n, float* out, uint64_t* state_out) {
+    Pcg32 r{state};
+    for (int i = 0; i < n; ++i) out[i] = r.uniform();
+    if (state_out) *state_out = r.state;
+}
+
+// renderer_scene.h:1185-1198: map dims are next powers of two with height >= width / 2.
+int64_t orc_imp_map_size(int32_t env_w, int32_t env_h, int32_t* map_w, int32_t* map_h, int32_t* num_mips,
+                         int64_t* offsets) {
+    auto next_pow2 = [](uint32_t v) {
+        uint32_t p = 1;
+        while (p < v) p <<= 1;
+        return p;
+    };
+    uint32_t dx = next_pow2(env_w);
+    uint32_t dy = std::max(next_pow2(env_h), dx >> 1);
+    int levels = 1;
+    while ((1u << (levels - 1)) < dx) ++levels;
+    *map_w = dx;
+    *map_h = dy;
+    *num_mips = levels;
+    int64_t off = 0;
+    for (int l = 0; l < levels; ++l) {
+        if (offsets) offsets[l] = off;
+        int64_t w = std::max<int64_t>(dx >> l, 1), h = std::max<int64_t>(dy >> l, 1);
+        off += w * h;
+    }
+    return off;
+}
+
+// compute_light_probs.cu:161-211. Returns the integral written by the last level.
+float orc_build_imp_map(const float* env_rgb, int32_t env_w, int32_t env_h, float* mips) {
+    int32_t mw, mh, nm;
+    int64_t offs[32];
+    orc_imp_map_size(env_w, env_h, &mw, &mh, &nm, offs);
+    for (int y = 0; y < mh; ++y) {
+        for (int x = 0; x < mw; ++x) {
+            float importance = 0.0f;
+            if (x < env_w && y < env_h) {
+                const float* p = env_rgb + 3 * (static_cast<int64_t>(y) * env_w + x);
+                RGB c = rgb(p[0], p[1], p[2]);
+                float correction = kPi / 2 * std::sin(kPi * (y + 0.5f) / env_h);
+                importance = luminance(c) * correction;
+            }
+            mips[offs[0] + static_cast<int64_t>(y) * mw + x] = importance;
+        }
+    }
+    float integral = 0.0f;
+    for (int l = 1; l < nm; ++l) {
+        int sw = mw >> (l - 1), sh = mh >> (l - 1);
+        int dw = std::max(mw >> l, 1), dh = std::max(mh >> l, 1);
+        for (int y = 0; y < dh; ++y) {
+            for (int x = 0; x < dw; ++x) {
+                float sum = 0.0f;
+                int xs[4] = {2 * x, 2 * x + 1, 2 * x, 2 * x + 1};
+                int ys[4] = {2 * y, 2 * y, 2 * y + 1, 2 * y + 1};
+                for (int q = 0; q < 4; ++q) {
+                    if (xs[q] < sw && ys[q] < sh)
+                        sum += mips[offs[l - 1] + static_cast<int64_t>(ys[q]) * std::max(sw, 1) + xs[q]];
+                }
+                sum *= 0.25f;
+                mips[offs[l] + static_cast<int64_t>(y) * dw + x] = sum;
+                if (l == nm - 1) integral = sum * static_cast<float>(1u << (2 * (nm - 1)));
+            }
+        }
+    }
+    return integral;
+}
+
+// Majorant cells of the config mode: max over voxels [8c-1, 8c+9] of each 8^3 cell and the
+// reference's global majorant over index coordinates [0, n-1) (renderer_scene.cpp:498-509).
+float orc_majorants(const float* v, int32_t nx, int32_t ny, int32_t nz, float* cells) {
+    int lx = (nx + 7) / 8, ly = (ny + 7) / 8, lz = (nz + 7) / 8;
+    auto at = [&](int x, int y, int z) -> float {
+        if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.0f;
+        return v[(static_cast<int64_t>(x) * ny + y) * nz + z];
+    };
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int cx = 0; cx < lx; ++cx)
+        for (int cy = 0; cy < ly; ++cy)
+            for (int cz = 0; cz < lz; ++cz) {
+                float m = 0.0f;
+                for (int x = 8 * cx - 1; x <= 8 * cx + 9; ++x)
+                    for (int y = 8 * cy - 1; y <= 8 * cy + 9; ++y)
+                        for (int z = 8 * cz - 1; z <= 8 * cz + 9; ++z) m = std::max(m, at(x, y, z));
+                cells[(static_cast<int64_t>(cx) * ly + cy) * lz + cz] = m;
+            }
+    float g = -INFINITY;
+    for (int x = 0; x < nx - 1; ++x)
+        for (int y = 0; y < ny - 1; ++y)
+            for (int z = 0; z < nz - 1; ++z) g = std::max(g, at(x, y, z));
+    return g;
+}
+
+void orc_sample_density(const OrcScene* sc, const float* idx, int32_t n, float* out) {
+    for (int i = 0; i < n; ++i) out[i] = sample_trilinear(*sc, v3(idx[3 * i], idx[3 * i + 1], idx[3 * i + 2]));
+}
+
+void orc_clip_rays(const OrcScene* sc, const float* org, const float* dir, int32_t n, float* t0, float* t1,
+                   int32_t* hit) {
+    for (int i = 0; i < n; ++i) {
+        float a = 0, b = 0;
+        hit[i] = clip_ray(sc->bbox_min, sc->bbox_max, v3(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
+                          v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), 0.0f, 1e10f, &a, &b);
+        t0[i] = a;
+        t1[i] = b;
+    }
+}
+
+void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, float* pdf, float* out) {
+    for (int i = 0; i < n; ++i) {
+        V3 d;
+        float p;
+        RGB c = env_sample(*sc, u[2 * i], u[2 * i + 1], &d, &p);
+        dir[3 * i] = d.x;
+        dir[3 * i + 1] = d.y;
+        dir[3 * i + 2] = d.z;
+        pdf[i] = p;
+        out[3 * i] = c.r;
+        out[3 * i + 1] = c.g;
+        out[3 * i + 2] = c.b;
+    }
+}
+
+void orc_env_evaluate(const OrcScene* sc, const float* dir, int32_t n, float* pdf, float* out) {
+    for (int i = 0; i < n; ++i) {
+        float p;
+        RGB c = env_evaluate(*sc, v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), &p);
+        pdf[i] = p;
+        out[3 * i] = c.r;
+        out[3 * i + 1] = c.g;
+        out[3 * i + 2] = c.b;
+    }
+}
+
+void orc_phase_sample(int32_t kind, float param, const float* u, int32_t n, float* dl, float* pdf) {
+    for (int i = 0; i < n; ++i) {
+        V3 l;
+        pdf[i] = phase_sample(kind, param, u[2 * i], u[2 * i + 1], &l);
+        dl[3 * i] = l.x;
+        dl[3 * i + 1] = l.y;
+        dl[3 * i + 2] = l.z;
+    }
+}
+
+void orc_phase_eval(int32_t kind, float param, const float* dl, int32_t n, float* pdf) {
+    for (int i = 0; i < n; ++i) pdf[i] = phase_pdf(kind, param, v3(dl[3 * i], dl[3 * i + 1], dl[3 * i + 2]));
+}
+
+void orc_polar_yup(const float* v, int32_t n, float* tp) {
+    for (int i = 0; i < n; ++i) to_polar_yup(v3(v[3 * i], v[3 * i + 1], v[3 * i + 2]), &tp[2 * i], &tp[2 * i + 1]);
+}
+
+void orc_coordinate_system(const float* nrm, int32_t n, float* tb) {
+    for (int i = 0; i < n; ++i) {
+        Frame f = make_frame(v3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]));
+        float vals[6] = {f.t.x, f.t.y, f.t.z, f.b.x, f.b.y, f.b.z};
+        std::memcpy(tb + 6 * i, vals, sizeof(vals));
+    }
+}
+
+void orc_quat_to_matrix(const float* q, float* m9) {
+    M3 m = quat_to_m3(q);
+    float vals[9] = {m.c0.x, m.c0.y, m.c0.z, m.c1.x, m.c1.y, m.c1.z, m.c2.x, m.c2.y, m.c2.z};
+    std::memcpy(m9, vals, sizeof(vals));
+}
+
+int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum_base, int32_t spp,
+                         double* sum_rgb, float* mean_rgb, uint32_t* dlog, int32_t row0, int32_t row1,
+                         int32_t nthreads) {
+    const OrcScene& s = *sc;
+    int64_t total = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+#endif
+    for (int y = row0; y < row1; ++y) {
+        for (int x = 0; x < s.width; ++x) {
+            int64_t pix = static_cast<int64_t>(y) * s.width + x;
+            Pcg32 rng{rng_states[pix]};
+            for (int i = 0; i < spp; ++i) {
+                uint32_t rec[4] = {0, 0, 0, 0};
+                int64_t lk = 0;
+                RGB c = trace_path(s, rng, x, y, rec, &lk);
+                total += lk;
+                if (dlog) std::memcpy(dlog + 4 * (pix * spp + i), rec, sizeof(rec));
+                // optix_pathtracing_kernels.cu:415-432: drop non-finite / negative samples.
+                if (!all_nonneg_finite(c)) continue;
+                if (sum_rgb) {
+                    sum_rgb[3 * pix] += c.r;
+                    sum_rgb[3 * pix + 1] += c.g;
+                    sum_rgb[3 * pix + 2] += c.b;
+                }
+                if (mean_rgb) {
+                    uint32_t n = static_cast<uint32_t>(accum_base + i);
+                    RGB prev = rgb(0, 0, 0);
+                    if (n > 0) prev = rgb(mean_rgb[3 * pix], mean_rgb[3 * pix + 1], mean_rgb[3 * pix + 2]);
+                    float w = 1.0f / (n + 1);
+                    RGB r = (1 - w) * prev + w * c;
+                    mean_rgb[3 * pix] = r.r;
+                    mean_rgb[3 * pix + 1] = r.g;
+                    mean_rgb[3 * pix + 2] = r.b;
+                }
+            }
+            rng_states[pix] = rng.state;
+        }
+    }
+    return total;
+}
+
+}  // extern "C"

@@ -1,0 +1,118 @@
+/*
+ * ORACLE (test infrastructure only) — CPU restatement of the reference path tracer's
+ * volume-only hot path (shocker-0x15/rtcamp8). Only tests/, the smoke check and the
+ * CPU-baseline / reference legs of bench.py load this library; the product library never
+ * links, calls or ships it.
+ *
+ * Parity status: the reference's own hot path (an OptiX ray-generation program plus
+ * tiny-cuda-nn) cannot be built in this environment, and the reference has no tests or
+ * golden vectors. The oracle is therefore pinned component by component against programs
+ * compiled from the reference's own sources (NanoVDB sampler / ray clip, basic_types.h
+ * math, Hosek-Wilkie sky model) through the committed recipe in oracle/build_ref.sh and
+ * the golden vectors in tests/golden/; the end-to-end estimator is pinned by analytic
+ * tests (furnace, constant-density transmittance) only.
+ *
+ * All structs are plain C so Python (ctypes) can fill them.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct OrcScene {
+    /* Dense voxel array, x-major (index = (x * ny + y) * nz + z), values outside are 0. */
+    const float* voxels;
+    int32_t nx, ny, nz;
+    float inv_voxel_size;      /* world -> index scale (float copy of 1/voxel size) */
+    float origin[3];           /* world position of index (0,0,0) */
+    float bbox_min[3], bbox_max[3];   /* world-space clip box of the grid */
+    float global_majorant;     /* max voxel value (reference loop over [min,max)) */
+    const float* cell_majorant;       /* per 8^3-voxel cell, 9^3 apron max; may be null */
+    int32_t cx, cy, cz;
+    float density_coeff;
+    float albedo;
+    int32_t phase_kind;        /* 0 = Schlick(k), 1 = Henyey-Greenstein(g) */
+    float phase_param;
+
+    /* Image-based environment (point-sampled RGB, row-major, y = polar angle). */
+    int32_t env_enabled;
+    const float* env_rgb;      /* env_w * env_h * 3 */
+    int32_t env_w, env_h;
+    float env_power, env_rotation;
+    const float* imp_mips;     /* importance mip chain, level L at imp_offsets[L] */
+    const int64_t* imp_offsets;
+    int32_t map_w, map_h, num_mips;
+    float imp_integral;
+
+    /* Directional sun (config mode only). */
+    int32_t sun_enabled;
+    float sun_dir[3];          /* unit vector towards the sun */
+    float sun_irradiance[3];
+    float sun_prob;            /* probability of picking the sun in NEE */
+
+    float world_radius;
+    float world_min[3], world_max[3];
+
+    float cam_aspect, cam_fovy;
+    float cam_pos[3];
+    float cam_quat[4];         /* x, y, z, w */
+    int32_t width, height;
+
+    int32_t max_bounces;       /* 0 = unlimited */
+    int32_t rr_start;          /* RR draws when pathLength >= rr_start */
+    int32_t majorant_mode;     /* 0 = single global majorant, 1 = per-cell majorant DDA */
+    int32_t max_steps;         /* safety cap on density lookups per segment, 0 = none */
+} OrcScene;
+
+/* Per-sample decision record: vertices, primary lookups, shadow lookups, end code. */
+enum {
+    ORC_END_ESCAPE = 1,
+    ORC_END_RR = 2,
+    ORC_END_PDF_ZERO = 3,
+    ORC_END_MAX_BOUNCES = 4,
+    ORC_END_STEP_CAP = 5,
+};
+
+int orc_version(void);
+
+/* PCG32 / seeding helpers. */
+void orc_seed_states(int32_t width, int32_t height, uint64_t seed, uint64_t* out);
+void orc_pcg_floats(uint64_t state, int32_t n, float* out, uint64_t* state_out);
+
+/* Importance map build for an RGB environment image (restates computeFirstMip... +
+ * computeMipOfImportanceMap). Writes the chain into mips_out (size from orc_imp_map_size). */
+int64_t orc_imp_map_size(int32_t env_w, int32_t env_h, int32_t* map_w, int32_t* map_h,
+                         int32_t* num_mips, int64_t* offsets);
+float orc_build_imp_map(const float* env_rgb, int32_t env_w, int32_t env_h, float* mips_out);
+
+/* Majorant cells (per 8^3 cell, max over voxels [8c-1, 8c+9]) and the return value is the
+ * reference's global majorant (max over index coordinates [0, n-1) per axis). */
+float orc_majorants(const float* voxels, int32_t nx, int32_t ny, int32_t nz, float* cells);
+
+/* Component batch entry points used by the known-answer tests. */
+void orc_sample_density(const OrcScene* sc, const float* idx_xyz, int32_t n, float* out);
+void orc_clip_rays(const OrcScene* sc, const float* org, const float* dir, int32_t n,
+                   float* t0, float* t1, int32_t* hit);
+void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, float* pdf,
+                    float* rgb);
+void orc_env_evaluate(const OrcScene* sc, const float* dir, int32_t n, float* pdf, float* rgb);
+void orc_phase_sample(int32_t kind, float param, const float* u, int32_t n, float* dir_local,
+                      float* pdf);
+void orc_phase_eval(int32_t kind, float param, const float* dir_local, int32_t n, float* pdf);
+void orc_polar_yup(const float* v, int32_t n, float* theta_phi);
+void orc_coordinate_system(const float* nrm, int32_t n, float* tb);
+void orc_quat_to_matrix(const float* q, float* m9);
+
+/* Plain path tracer: spp samples per pixel over rows [row0, row1), continuing each
+ * pixel's PCG32 stream. sum_rgb (double, += per sample), mean_rgb (reference running
+ * mean with numAccumFrames = accum_base + i) and dlog (4 x u32 per pixel-sample,
+ * index (pixel * spp + i)) may be null. Returns the number of density lookups. */
+int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng, int32_t accum_base, int32_t spp,
+                         double* sum_rgb, float* mean_rgb, uint32_t* dlog, int32_t row0,
+                         int32_t row1, int32_t nthreads);
+
+#ifdef __cplusplus
+}
+#endif

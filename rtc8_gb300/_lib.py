@@ -1,0 +1,121 @@
+"""ctypes binding of ``librtc8_gb300.so`` (the C ABI in include/rtc8_vpt.h and rtc8_nrc.h).
+
+The library is built in-tree by :func:`rtc8_gb300.build.build`. Loading fails loudly when it
+is missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "librtc8_gb300.so"
+
+c_float_p = C.POINTER(C.c_float)
+c_double_p = C.POINTER(C.c_double)
+c_u32_p = C.POINTER(C.c_uint32)
+c_u64_p = C.POINTER(C.c_uint64)
+c_i32_p = C.POINTER(C.c_int32)
+c_i64_p = C.POINTER(C.c_int64)
+
+
+class VptFrameParams(C.Structure):
+    """Mirror of ``VptFrameParams`` (include/rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("cam_aspect", C.c_float),
+        ("cam_fovy", C.c_float),
+        ("cam_position", C.c_float * 3),
+        ("cam_orientation", C.c_float * 4),
+        ("density_coeff", C.c_float),
+        ("scattering_albedo", C.c_float),
+        ("phase_kind", C.c_int32),
+        ("phase_param", C.c_float),
+        ("radiance_scale", C.c_float),
+        ("env_enabled", C.c_int32),
+        ("env_power", C.c_float),
+        ("env_rotation", C.c_float),
+        ("sun_enabled", C.c_int32),
+        ("sun_direction", C.c_float * 3),
+        ("sun_irradiance", C.c_float * 3),
+        ("sun_select_prob", C.c_float),
+        ("max_bounces", C.c_int32),
+        ("rr_start_vertex", C.c_int32),
+        ("majorant_mode", C.c_int32),
+        ("max_steps_per_segment", C.c_int32),
+    ]
+
+
+# name -> (restype, argtypes)
+_VPT = {
+    "vpt_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "vpt_destroy": (C.c_int, [C.c_void_p]),
+    "vpt_last_error": (C.c_char_p, []),
+    "vpt_seed_rng": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vpt_set_rng_states": (C.c_int, [C.c_void_p, c_u64_p]),
+    "vpt_get_rng_states": (C.c_int, [C.c_void_p, c_u64_p]),
+    "vpt_set_volume_dense": (C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, c_float_p]),
+    "vpt_set_volume_dense_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                              c_float_p]),
+    "vpt_generate_fbm_volume": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_int32, C.c_float, C.c_float, C.c_float,
+                                          C.c_float, C.c_float, c_float_p]),
+    "vpt_download_volume_dense": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_get_volume_info": (C.c_int, [C.c_void_p, c_i64_p, c_i64_p, c_float_p, c_i64_p]),
+    "vpt_download_cell_majorants": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_set_environment_rgb": (C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32]),
+    "vpt_get_importance_map_info": (C.c_int, [C.c_void_p, c_i32_p, c_i32_p, c_i32_p, c_i64_p, c_float_p]),
+    "vpt_download_importance_map": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_generate_sky": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, c_float_p, c_float_p, c_float_p, c_float_p,
+                                   C.c_int32]),
+    "vpt_download_environment": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_set_frame_params": (C.c_int, [C.c_void_p, C.POINTER(VptFrameParams)]),
+    "vpt_launch_plain": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_launch_plain_logged": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vpt_reset_accumulation": (C.c_int, [C.c_void_p]),
+    "vpt_download_sum": (C.c_int, [C.c_void_p, c_double_p, c_u32_p]),
+    "vpt_download_mean": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_get_accum_device_ptrs": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "vpt_get_counters": (C.c_int, [C.c_void_p, c_u64_p, c_u64_p, c_u64_p]),
+    "vpt_reset_counters": (C.c_int, [C.c_void_p]),
+    "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
+    "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+}
+
+EXPORTS: dict[str, tuple] = dict(_VPT)
+
+_lib: C.CDLL | None = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Loads the product library and declares every exported entry point."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(rtc8_gb300 has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class VptError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        msg = load().vpt_last_error()
+        raise VptError(f"{what} failed with code {rc}: {msg.decode() if msg else ''}")
+
+
+def ptr(arr, ctype):
+    """Pointer to a contiguous numpy array."""
+    return arr.ctypes.data_as(C.POINTER(ctype))

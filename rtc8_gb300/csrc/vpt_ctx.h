@@ -1,0 +1,67 @@
+// Host-side state of a VptContext (device buffers and scene metadata).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/rtc8_vpt.h"
+
+namespace vpt {
+
+struct TraceParams;
+struct NrcBuffers;
+
+struct VptContextImpl {
+    int32_t width = 0, height = 0;
+    int device = 0, num_sms = 0;
+    int32_t ctas_per_sm = 0, threads = 0;
+
+    // per pixel (renderer_main.cpp:80-129)
+    uint64_t* d_rng = nullptr;
+    double* d_sum = nullptr;
+    float* d_mean = nullptr;
+    uint32_t accum_samples = 0;
+
+    unsigned int* d_work = nullptr;
+    unsigned long long* d_counters = nullptr;
+    unsigned int* d_err = nullptr;
+    unsigned int* d_scratch_u32 = nullptr;
+    float* d_integral = nullptr;
+
+    // density grid
+    bool has_volume = false;
+    float* d_dense = nullptr;
+    int32_t* d_leaf_table = nullptr;
+    float* d_leaf_values = nullptr;
+    float* d_cell_maj = nullptr;
+    int32_t nx = 0, ny = 0, nz = 0, lx = 0, ly = 0, lz = 0;
+    int64_t active_leaves = 0, total_leaves = 0;
+    float global_majorant = 0, voxel_size = 1, inv_voxel_size = 1;
+    float origin[3] = {0, 0, 0}, bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
+    float world_radius = 1;
+
+    // environment
+    float4* d_env = nullptr;
+    float* d_mips = nullptr;
+    int32_t env_w = 0, env_h = 0, map_w = 0, map_h = 0, num_mips = 0;
+    int64_t mip_offset[16] = {};
+    int64_t mip_total = 0;
+    float imp_integral = 0;
+
+    VptFrameParams frame{};
+    bool has_frame = false;
+
+    // neural-radiance-cache render/training buffers (allocated on first use)
+    NrcBuffers* nrc = nullptr;
+    void release_nrc();
+};
+
+int ctx_set_error(int code, const char* msg);
+int fill_trace_params(VptContextImpl* c, TraceParams* tp);
+int persistent_grid(VptContextImpl* c, int threads, const void* kernel);
+int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
+                         const float sun_dir[3], int include_disc);
+const void* plain_kernel_ptr(bool grid_majorant, bool logged);
+
+}  // namespace vpt

@@ -1,0 +1,470 @@
+// Persistent megakernel for the plain volumetric path tracer (the reference's pathTrace
+// ray-generation program, renderer/gpu_kernels/optix_pathtracing_kernels.cu:31-434 with
+// withNRC = generateTrainingData = false, for volume-only scenes).
+//
+// GB300 layout: one resident set of CTAs per SM; each lane owns one pixel at a time,
+// traces all of that launch's samples of the pixel (so the pixel's PCG32 stream advances
+// exactly as in the reference, one sample after the other) and fetches the next pixel
+// from a global counter when done (path regeneration, no idle lanes at the tail of a
+// long path). Each loop iteration first lets every lane run its cheap, divergent event
+// logic (camera ray, vertex, Russian roulette, NEE set-up, phase sampling, accumulation)
+// until it needs a density value, then all lanes perform their grid lookups together,
+// so the dominant gathers of delta tracking and ratio tracking run converged.
+#include "vpt_ctx.h"
+#include "vpt_tracer.cuh"
+
+namespace vpt {
+namespace {
+
+enum : uint32_t {
+    ST_FETCH = 0,    // get the next pixel
+    ST_CAMERA,       // start a sample: camera ray
+    ST_SEGMENT,      // start a primary segment: ++pathLength, clip
+    ST_STEP,         // advance the current segment to its next lookup
+    ST_VERTEX,       // primary collision: RR, NEE set-up
+    ST_NEE_DONE,     // shadow segment finished: NEE contribution, phase sampling
+    ST_ESCAPE,       // primary segment left the grid
+    ST_END_SAMPLE,   // accumulate, next sample or next pixel
+    ST_DONE,
+};
+
+enum : uint32_t { END_ESCAPE = 1, END_RR = 2, END_PDF_ZERO = 3, END_MAX_BOUNCES = 4, END_STEP_CAP = 5 };
+
+struct DdaState {
+    int cell[3];
+    int step[3];
+    float tnext[3], tdelta[3];
+};
+
+__device__ __forceinline__ void dda_init(const Grid& g, V3 eye, V3 dir, float t, DdaState* d) {
+    float o[3] = {(eye.x - g.origin[0]) * g.inv_voxel_size, (eye.y - g.origin[1]) * g.inv_voxel_size,
+                  (eye.z - g.origin[2]) * g.inv_voxel_size};
+    float dd[3] = {dir.x * g.inv_voxel_size, dir.y * g.inv_voxel_size, dir.z * g.inv_voxel_size};
+    int cdim[3] = {g.lx, g.ly, g.lz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float p = o[a] + dd[a] * t;
+        int c = static_cast<int>(floorf(p * 0.125f));
+        c = min(max(c, 0), cdim[a] - 1);
+        d->cell[a] = c;
+        if (dd[a] > 0) {
+            d->step[a] = 1;
+            d->tnext[a] = ((c + 1) * 8.0f - o[a]) / dd[a];
+            d->tdelta[a] = 8.0f / dd[a];
+        } else if (dd[a] < 0) {
+            d->step[a] = -1;
+            d->tnext[a] = (c * 8.0f - o[a]) / dd[a];
+            d->tdelta[a] = -8.0f / dd[a];
+        } else {
+            d->step[a] = 0;
+            d->tnext[a] = INFINITY;
+            d->tdelta[a] = INFINITY;
+        }
+    }
+}
+
+template <bool kGridMajorant, bool kLog>
+__global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
+    const Grid& g = P.grid;
+    const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
+    const float global_maj = P.density_coeff * g.global_majorant;
+
+    uint32_t st = ST_FETCH;
+    uint32_t pixel = 0, sample = 0;
+    Pcg32 rng{0};
+    double sum_r = 0, sum_g = 0, sum_b = 0;
+    RGB mean = rgb(0, 0, 0);
+
+    // per-sample state
+    V3 origin = v3(0, 0, 0), dir = v3(0, 0, 1);
+    float dir_pdf = 1.0f, init_importance = 1.0f;
+    RGB throughput = rgb(0, 0, 0), contribution = rgb(0, 0, 0);
+    uint32_t path_length = 0, end_code = 0;
+    uint32_t rec_primary = 0, rec_shadow = 0;
+
+    // current segment
+    bool shadow = false;
+    V3 seg_eye = v3(0, 0, 0), seg_dir = v3(0, 0, 1);
+    float t = 0, t1 = 0, maj = global_maj, texit = 0;
+    uint32_t seg_steps = 0;
+    DdaState dda;
+
+    // NEE in flight
+    V3 light_dir = v3(0, 1, 0);
+    RGB emittance = rgb(0, 0, 0);
+    float area_pdf = 1.0f, vis = 1.0f;
+    bool pick_sun = false;
+
+    unsigned long long n_lookups = 0, n_vertices = 0, n_samples = 0;
+    unsigned int err = 0;
+
+    while (true) {
+        // ---------------------------------------------------------------- divergent part
+        bool need_lookup = false;
+        V3 lookup_pos = v3(0, 0, 0);
+        while (!need_lookup && st != ST_DONE) {
+            switch (st) {
+            case ST_FETCH: {
+                pixel = atomicAdd(P.work_counter, 1u);
+                if (pixel >= num_pixels) {
+                    st = ST_DONE;
+                    break;
+                }
+                rng.state = P.rng[pixel];
+                sum_r = sum_g = sum_b = 0;
+                if (P.accum_base > 0) {
+                    mean = rgb(P.mean_rgb[3 * pixel], P.mean_rgb[3 * pixel + 1], P.mean_rgb[3 * pixel + 2]);
+                } else {
+                    mean = rgb(0, 0, 0);
+                }
+                sample = 0;
+                st = ST_CAMERA;
+                break;
+            }
+            case ST_CAMERA: {
+                // optix_pathtracing_kernels.cu:43-55, 76-81.
+                uint32_t px = pixel % static_cast<uint32_t>(P.width);
+                uint32_t py = pixel / static_cast<uint32_t>(P.width);
+                float ux = rng.uniform();
+                float fx = (px + ux) / P.width;
+                float uy = rng.uniform();
+                float fy = (py + uy) / P.height;
+                float vh = 2 * tanf(P.cam_fovy * 0.5f);
+                float vw = P.cam_aspect * vh;
+                float sensor_area = vw * vh;
+                origin = v3(P.cam_pos[0], P.cam_pos[1], P.cam_pos[2]);
+                V3 local = normalize(v3(vw * (-0.5f + fx), vh * (0.5f - fy), -1));
+                dir = normalize(mul(quat_to_m3(P.cam_quat[0], P.cam_quat[1], P.cam_quat[2], P.cam_quat[3]), local));
+                float az = fabsf(local.z);
+                dir_pdf = 1 / (az * az * az * sensor_area);
+                float inv = 1.0f / dir_pdf;
+                throughput = rgb(1, 1, 1) * inv;
+                init_importance = luminance(throughput);
+                contribution = rgb(0, 0, 0);
+                path_length = 0;
+                end_code = 0;
+                rec_primary = rec_shadow = 0;
+                st = ST_SEGMENT;
+                break;
+            }
+            case ST_SEGMENT: {
+                ++path_length;
+                ++n_vertices;
+                float a, b;
+                if (clip_ray(g.bbox_min, g.bbox_max, origin, dir, 0.0f, 1e10f, &a, &b)) {
+                    shadow = false;
+                    seg_eye = origin;
+                    seg_dir = dir;
+                    t = fmaxf(0.0f, a);
+                    t1 = b;
+                    seg_steps = 0;
+                    if constexpr (kGridMajorant) {
+                        dda_init(g, seg_eye, seg_dir, t, &dda);
+                        texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+                        maj = P.density_coeff *
+                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                    }
+                    st = ST_STEP;
+                } else {
+                    st = ST_ESCAPE;
+                }
+                break;
+            }
+            case ST_STEP: {
+                if constexpr (!kGridMajorant) {
+                    // optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378.
+                    t += -logf(1.0f - rng.uniform()) / maj;
+                    if (t > t1) {
+                        st = shadow ? ST_NEE_DONE : ST_ESCAPE;
+                    } else {
+                        lookup_pos = seg_eye + seg_dir * t;
+                        need_lookup = true;
+                    }
+                } else {
+                    // Majorant-grid DDA: sample within the current cell; overshooting its exit
+                    // restarts at the exit (memoryless), empty cells are skipped without draws.
+                    bool seg_end = false;
+                    while (true) {
+                        if (maj > 0) {
+                            float tt = t + -logf(1.0f - rng.uniform()) / maj;
+                            if (tt < texit) {
+                                t = tt;
+                                lookup_pos = seg_eye + seg_dir * t;
+                                need_lookup = true;
+                                break;
+                            }
+                        }
+                        t = texit;
+                        if (texit >= t1) {
+                            seg_end = true;
+                            break;
+                        }
+                        int ax = (dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2]) ? 0
+                                 : (dda.tnext[1] <= dda.tnext[2] ? 1 : 2);
+                        dda.cell[ax] += dda.step[ax];
+                        int lim = ax == 0 ? g.lx : (ax == 1 ? g.ly : g.lz);
+                        if (dda.cell[ax] < 0 || dda.cell[ax] >= lim) {
+                            t = t1;
+                            seg_end = true;
+                            break;
+                        }
+                        dda.tnext[ax] += dda.tdelta[ax];
+                        texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+                        maj = P.density_coeff *
+                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                    }
+                    if (seg_end) st = shadow ? ST_NEE_DONE : ST_ESCAPE;
+                }
+                break;
+            }
+            case ST_ESCAPE: {
+                // optix_pathtracing_kernels.cu:130-174.
+                if (P.env_enabled) {
+                    float hyp_pdf;
+                    RGB radiance = env_evaluate(P.env, dir, &hyp_pdf);
+                    float mis = 1.0f;
+                    if (path_length > 1) {
+                        float light_pdf = (P.sun.enabled ? (1.0f - P.sun.select_prob) : 1.0f) * hyp_pdf;
+                        float bsdf_pdf = dir_pdf;
+                        mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+                    }
+                    contribution = contribution + throughput * (radiance * mis);
+                }
+                end_code = END_ESCAPE;
+                st = ST_END_SAMPLE;
+                break;
+            }
+            case ST_VERTEX: {
+                // In-medium vertex (:176-182), Russian roulette (:254-268, 332), NEE set-up
+                // (renderer_kernel_common.h:297-358).
+                origin = origin + t * dir;
+                float continue_prob = 1.0f;
+                if (static_cast<int32_t>(path_length) >= P.rr_start) {
+                    continue_prob = fminf(luminance(throughput) / init_importance, 1.0f);
+                    if (rng.uniform() >= continue_prob) {
+                        end_code = END_RR;
+                        st = ST_END_SAMPLE;
+                        break;
+                    }
+                }
+                throughput = rdiv(throughput, continue_prob);
+
+                float u_light = rng.uniform();
+                float u0 = rng.uniform();
+                float u1 = rng.uniform();
+                pick_sun = false;
+                float light_prob = 1.0f;
+                bool have_light = true;
+                if (P.sun.enabled && P.env_enabled) {
+                    if (u_light < P.sun.select_prob) {
+                        pick_sun = true;
+                        light_prob = P.sun.select_prob;
+                    } else {
+                        light_prob = 1.0f - P.sun.select_prob;
+                    }
+                } else if (P.sun.enabled) {
+                    pick_sun = true;
+                } else if (!P.env_enabled) {
+                    have_light = false;
+                }
+                vis = 0.0f;
+                if (have_light) {
+                    if (pick_sun) {
+                        light_dir = v3(P.sun.dir[0], P.sun.dir[1], P.sun.dir[2]);
+                        emittance = rgb(P.sun.irradiance[0], P.sun.irradiance[1], P.sun.irradiance[2]);
+                        area_pdf = light_prob;
+                    } else {
+                        float pdf;
+                        RGB radiance = env_sample(P.env, u0, u1, &light_dir, &pdf);
+                        emittance = kPi * radiance;
+                        area_pdf = pdf;
+                        if (area_pdf == 0.0f) have_light = false;
+                        area_pdf *= light_prob;
+                    }
+                }
+                if (have_light) {
+                    V3 sdir = -light_dir;
+                    float lp_cos = dot(sdir, -light_dir);
+                    if (lp_cos <= 0.0f) have_light = false;
+                }
+                if (!have_light) {
+                    st = ST_NEE_DONE;  // vis = 0: no contribution
+                    break;
+                }
+                vis = 1.0f;
+                float trace_len = 2 * P.world_radius;
+                seg_dir = -light_dir;
+                seg_eye = origin + trace_len * -seg_dir;
+                float a, b;
+                if (clip_ray(g.bbox_min, g.bbox_max, seg_eye, seg_dir, 0.0f, trace_len, &a, &b)) {
+                    shadow = true;
+                    t = fmaxf(0.0f, a);
+                    t1 = b;
+                    seg_steps = 0;
+                    if constexpr (kGridMajorant) {
+                        dda_init(g, seg_eye, seg_dir, t, &dda);
+                        texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+                        maj = P.density_coeff *
+                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                    } else {
+                        maj = global_maj;
+                    }
+                    st = ST_STEP;
+                } else {
+                    st = ST_NEE_DONE;
+                }
+                break;
+            }
+            case ST_NEE_DONE: {
+                // renderer_kernel_common.h:385-402, then phase sampling (:341-356).
+                if (vis > 0.0f) {
+                    V3 sdir = -light_dir;
+                    Frame fr = make_frame(-dir);
+                    V3 v_in_local = to_local(fr, -sdir);
+                    float pf = phase_pdf(P.phase_kind, P.phase_param, v_in_local);
+                    RGB fs = rgb(P.albedo, P.albedo, P.albedo) * pf;
+                    RGB nee;
+                    if (pick_sun) {
+                        nee = fs * emittance * (vis / area_pdf);
+                    } else {
+                        float lp_cos = dot(sdir, -light_dir);
+                        float bsdf_pdf = pf * lp_cos / 1.0f;
+                        if (!isfinite(bsdf_pdf)) bsdf_pdf = 0.0f;
+                        float light_pdf = area_pdf;
+                        float mis = (light_pdf * light_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+                        RGB le = rdiv(emittance, kPi);
+                        float gterm = lp_cos * 1.0f / 1.0f;
+                        nee = fs * le * (vis * mis * gterm / area_pdf);
+                    }
+                    contribution = contribution + throughput * nee;
+                }
+                if (P.max_bounces > 0 && static_cast<int32_t>(path_length) >= P.max_bounces) {
+                    end_code = END_MAX_BOUNCES;
+                    st = ST_END_SAMPLE;
+                    break;
+                }
+                Frame fr = make_frame(-dir);
+                float u0 = rng.uniform();
+                float u1 = rng.uniform();
+                V3 local;
+                float pdf = phase_sample(P.phase_kind, P.phase_param, u0, u1, &local);
+                if (pdf == 0.0f) {
+                    end_code = END_PDF_ZERO;
+                    st = ST_END_SAMPLE;
+                    break;
+                }
+                RGB fs = rgb(P.albedo, P.albedo, P.albedo) * pdf;
+                dir = from_local(fr, local);
+                RGB local_tp = fs * (fabsf(1.0f) / pdf);
+                throughput = throughput * local_tp;
+                dir_pdf = pdf;
+                st = ST_SEGMENT;
+                break;
+            }
+            case ST_END_SAMPLE: {
+                // optix_pathtracing_kernels.cu:413-432 (non-finite samples are dropped).
+                ++n_samples;
+                if constexpr (kLog) {
+                    uint4 rec = make_uint4(path_length, rec_primary, rec_shadow, end_code);
+                    reinterpret_cast<uint4*>(P.dlog)[static_cast<uint64_t>(pixel) * P.spp + sample] = rec;
+                }
+                if (all_nonneg_finite(contribution)) {
+                    sum_r += contribution.r;
+                    sum_g += contribution.g;
+                    sum_b += contribution.b;
+                    uint32_t n = P.accum_base + sample;
+                    RGB prev = n > 0 ? mean : rgb(0, 0, 0);
+                    float w = 1.0f / (n + 1);
+                    mean = (1 - w) * prev + w * contribution;
+                } else {
+                    err |= VPT_DEVERR_NONFINITE;
+                }
+                ++sample;
+                if (sample < P.spp) {
+                    st = ST_CAMERA;
+                } else {
+                    P.rng[pixel] = rng.state;
+                    P.sum_rgb[3 * pixel] += sum_r;
+                    P.sum_rgb[3 * pixel + 1] += sum_g;
+                    P.sum_rgb[3 * pixel + 2] += sum_b;
+                    P.mean_rgb[3 * pixel] = mean.r;
+                    P.mean_rgb[3 * pixel + 1] = mean.g;
+                    P.mean_rgb[3 * pixel + 2] = mean.b;
+                    st = ST_FETCH;
+                }
+                break;
+            }
+            default:
+                st = ST_DONE;
+                break;
+            }
+        }
+
+        if (!__any_sync(0xffffffffu, need_lookup)) {
+            if (__all_sync(0xffffffffu, st == ST_DONE)) break;
+            continue;
+        }
+
+        // ---------------------------------------------------------------- converged lookups
+        float density = 0.0f;
+        if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos));
+
+        if (need_lookup) {
+            ++n_lookups;
+            ++seg_steps;
+            if (shadow) {
+                ++rec_shadow;
+                vis *= (1 - density / maj);
+            } else {
+                ++rec_primary;
+                if (rng.uniform() < density / maj) st = ST_VERTEX;
+            }
+            if (st == ST_STEP && P.max_steps > 0 && seg_steps >= static_cast<uint32_t>(P.max_steps)) {
+                err |= VPT_DEVERR_STEP_CAP;
+                end_code = END_STEP_CAP;
+                st = ST_END_SAMPLE;
+            }
+        }
+    }
+
+    // warp-reduce the work counters
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_lookups += __shfl_down_sync(0xffffffffu, n_lookups, o);
+        n_vertices += __shfl_down_sync(0xffffffffu, n_vertices, o);
+        n_samples += __shfl_down_sync(0xffffffffu, n_samples, o);
+    }
+    err = __reduce_or_sync(0xffffffffu, err);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(P.counters + 0, n_lookups);
+        atomicAdd(P.counters + 1, n_vertices);
+        atomicAdd(P.counters + 2, n_samples);
+        if (err) atomicOr(P.error_flags, err);
+    }
+}
+
+}  // namespace
+
+const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
+    if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true>)
+                                     : reinterpret_cast<const void*>(plain_trace_kernel<false, true>);
+    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false>)
+                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false>);
+}
+
+void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, cudaStream_t s) {
+    dim3 grid(grid_ctas), block(threads);
+    if (p.dlog) {
+        if (grid_majorant)
+            plain_trace_kernel<true, true><<<grid, block, 0, s>>>(p);
+        else
+            plain_trace_kernel<false, true><<<grid, block, 0, s>>>(p);
+    } else {
+        if (grid_majorant)
+            plain_trace_kernel<true, false><<<grid, block, 0, s>>>(p);
+        else
+            plain_trace_kernel<false, false><<<grid, block, 0, s>>>(p);
+    }
+}
+
+}  // namespace vpt

@@ -1,0 +1,49 @@
+// Launch parameters and kernel declarations of the persistent volumetric tracker.
+#pragma once
+
+#include "vpt_device.cuh"
+#include "../../include/rtc8_vpt.h"
+
+namespace vpt {
+
+struct Sun {
+    float dir[3];
+    float irradiance[3];
+    float select_prob;
+    int32_t enabled;
+};
+
+// One launch of the tracker. Plain kernel parameter (lives in the constant bank).
+struct TraceParams {
+    Grid grid;
+    Env env;
+    Sun sun;
+    int32_t env_enabled;
+
+    float cam_aspect, cam_fovy;
+    float cam_pos[3];
+    float cam_quat[4];
+    int32_t width, height;
+
+    float density_coeff, albedo;
+    int32_t phase_kind;
+    float phase_param;
+    float world_radius;
+
+    int32_t max_bounces, rr_start, max_steps;
+
+    uint32_t spp;             // samples per pixel in this launch
+    uint32_t accum_base;      // samples already accumulated (numAccumFrames of the first one)
+
+    uint64_t* rng;            // per pixel
+    double* sum_rgb;          // 3 per pixel
+    float* mean_rgb;          // 3 per pixel
+    uint32_t* dlog;           // optional, 4 per pixel-sample
+    unsigned int* work_counter;
+    unsigned long long* counters;  // lookups, vertices, samples
+    unsigned int* error_flags;
+};
+
+void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, cudaStream_t s);
+
+}  // namespace vpt

@@ -1,0 +1,221 @@
+"""Host-side driver of the GB300 volumetric path tracer over the C ABI.
+
+:class:`Renderer` owns one ``VptContext`` and mirrors the reference's headless frame loop
+(renderer/renderer_main.cpp:1444-1667): scene set-up (volume, environment, camera, medium
+parameters) followed by per-frame launches of the path-tracing entry points.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import VptFrameParams, check, ptr
+from .configs import SceneConfig, camera_for, sun_direction, volume_box
+
+
+class Renderer:
+    def __init__(self, width: int, height: int):
+        self.lib = _lib.load()
+        self.width, self.height = width, height
+        h = C.c_void_p()
+        check(self.lib.vpt_create(width, height, C.byref(h)), "vpt_create")
+        self.ctx = h
+        self.params = VptFrameParams()
+
+    # ------------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        if self.ctx:
+            self.lib.vpt_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ scene
+    def seed_rng(self, seed: int) -> None:
+        check(self.lib.vpt_seed_rng(self.ctx, C.c_uint64(seed)), "vpt_seed_rng")
+
+    def rng_states(self) -> np.ndarray:
+        out = np.empty(self.width * self.height, dtype=np.uint64)
+        check(self.lib.vpt_get_rng_states(self.ctx, ptr(out, C.c_uint64)), "vpt_get_rng_states")
+        return out
+
+    def set_volume_dense(self, voxels: np.ndarray, voxel_size: float, origin) -> None:
+        v = np.ascontiguousarray(voxels, dtype=np.float32)
+        o = np.ascontiguousarray(origin, dtype=np.float32)
+        nx, ny, nz = v.shape
+        check(self.lib.vpt_set_volume_dense(self.ctx, ptr(v, C.c_float), nx, ny, nz, voxel_size, ptr(o, C.c_float)),
+              "vpt_set_volume_dense")
+
+    def generate_fbm_volume(self, spec, voxel_size: float, origin) -> None:
+        o = np.ascontiguousarray(origin, dtype=np.float32)
+        check(self.lib.vpt_generate_fbm_volume(self.ctx, spec.n, spec.seed, spec.octaves, spec.lacunarity, spec.gain,
+                                               spec.base_frequency, spec.threshold, voxel_size, ptr(o, C.c_float)),
+              "vpt_generate_fbm_volume")
+
+    def download_volume(self) -> np.ndarray:
+        info = self.volume_info()
+        n = info["dims"]
+        out = np.empty(n, dtype=np.float32)
+        check(self.lib.vpt_download_volume_dense(self.ctx, ptr(out, C.c_float)), "vpt_download_volume_dense")
+        return out
+
+    def volume_info(self) -> dict:
+        a, t, b = C.c_int64(), C.c_int64(), C.c_int64()
+        m = C.c_float()
+        check(self.lib.vpt_get_volume_info(self.ctx, C.byref(a), C.byref(t), C.byref(m), C.byref(b)),
+              "vpt_get_volume_info")
+        tot = t.value
+        return {"active_leaves": a.value, "total_leaves": tot, "global_majorant": m.value, "grid_bytes": b.value,
+                "dims": self._dims}
+
+    def cell_majorants(self) -> np.ndarray:
+        info = self.volume_info()
+        out = np.empty(info["total_leaves"], dtype=np.float32)
+        check(self.lib.vpt_download_cell_majorants(self.ctx, ptr(out, C.c_float)), "vpt_download_cell_majorants")
+        return out
+
+    def set_environment_rgb(self, rgb: np.ndarray) -> None:
+        img = np.ascontiguousarray(rgb, dtype=np.float32)
+        h, w, _ = img.shape
+        check(self.lib.vpt_set_environment_rgb(self.ctx, ptr(img, C.c_float), w, h), "vpt_set_environment_rgb")
+
+    def generate_sky(self, width: int, height: int, states: np.ndarray, solar: np.ndarray, cmf: np.ndarray,
+                     sun_dir, include_solar_disc: bool) -> None:
+        s = np.ascontiguousarray(states, dtype=np.float32)
+        so = np.ascontiguousarray(solar, dtype=np.float32)
+        cm = np.ascontiguousarray(cmf, dtype=np.float32)
+        d = np.ascontiguousarray(sun_dir, dtype=np.float32)
+        check(self.lib.vpt_generate_sky(self.ctx, width, height, ptr(s, C.c_float), ptr(so, C.c_float),
+                                        ptr(cm, C.c_float), ptr(d, C.c_float), int(include_solar_disc)),
+              "vpt_generate_sky")
+
+    def importance_map(self) -> tuple[np.ndarray, dict]:
+        mw, mh, nm = C.c_int32(), C.c_int32(), C.c_int32()
+        tot, integ = C.c_int64(), C.c_float()
+        check(self.lib.vpt_get_importance_map_info(self.ctx, C.byref(mw), C.byref(mh), C.byref(nm), C.byref(tot),
+                                                   C.byref(integ)), "vpt_get_importance_map_info")
+        out = np.empty(tot.value, dtype=np.float32)
+        check(self.lib.vpt_download_importance_map(self.ctx, ptr(out, C.c_float)), "vpt_download_importance_map")
+        return out, {"map_w": mw.value, "map_h": mh.value, "num_mips": nm.value, "integral": integ.value}
+
+    def download_environment(self, width: int, height: int) -> np.ndarray:
+        out = np.empty((height, width, 3), dtype=np.float32)
+        check(self.lib.vpt_download_environment(self.ctx, ptr(out, C.c_float)), "vpt_download_environment")
+        return out
+
+    # ------------------------------------------------------------------ frame
+    def set_frame(self, p: VptFrameParams) -> None:
+        self.params = p
+        check(self.lib.vpt_set_frame_params(self.ctx, C.byref(p)), "vpt_set_frame_params")
+
+    def set_launch_shape(self, ctas_per_sm: int = 0, threads: int = 0) -> None:
+        check(self.lib.vpt_set_launch_shape(self.ctx, ctas_per_sm, threads), "vpt_set_launch_shape")
+
+    def launch_plain(self, spp: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_launch_plain(self.ctx, C.c_void_p(stream or 0), spp), "vpt_launch_plain")
+
+    def launch_plain_logged(self, spp: int, dev_log_ptr: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_launch_plain_logged(self.ctx, C.c_void_p(stream or 0), spp, C.c_void_p(dev_log_ptr)),
+              "vpt_launch_plain_logged")
+
+    def synchronize(self, stream: int | None = None) -> None:
+        check(self.lib.vpt_synchronize(self.ctx, C.c_void_p(stream or 0)), "vpt_synchronize")
+
+    def reset_accumulation(self) -> None:
+        check(self.lib.vpt_reset_accumulation(self.ctx), "vpt_reset_accumulation")
+
+    def download_sum(self) -> tuple[np.ndarray, int]:
+        out = np.empty((self.height, self.width, 3), dtype=np.float64)
+        n = C.c_uint32()
+        check(self.lib.vpt_download_sum(self.ctx, ptr(out, C.c_double), C.byref(n)), "vpt_download_sum")
+        return out, n.value
+
+    def download_mean(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        check(self.lib.vpt_download_mean(self.ctx, ptr(out, C.c_float)), "vpt_download_mean")
+        return out
+
+    def image(self) -> np.ndarray:
+        s, n = self.download_sum()
+        return s / max(n, 1)
+
+    def counters(self) -> dict:
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(self.lib.vpt_get_counters(self.ctx, C.byref(a), C.byref(b), C.byref(c)), "vpt_get_counters")
+        return {"lookups": a.value, "vertices": b.value, "samples": c.value}
+
+    def reset_counters(self) -> None:
+        check(self.lib.vpt_reset_counters(self.ctx), "vpt_reset_counters")
+
+    def device_errors(self) -> int:
+        return int(self.lib.vpt_get_device_errors(self.ctx))
+
+    _dims = (0, 0, 0)
+
+
+def frame_params(cfg: SceneConfig, env_enabled: bool = True) -> VptFrameParams:
+    """Per-frame launch parameters of a configuration (renderer_main.cpp:1466-1469 defaults
+    are reproduced by SceneConfig's reference-mode values)."""
+    cam = camera_for(cfg)
+    p = VptFrameParams()
+    p.cam_aspect = cam.aspect
+    p.cam_fovy = cam.fovy
+    p.cam_position[:] = [float(x) for x in cam.position]
+    p.cam_orientation[:] = [float(x) for x in cam.orientation]
+    p.density_coeff = cfg.volume.sigma_t_max
+    p.scattering_albedo = cfg.albedo
+    p.phase_kind = cfg.phase_kind
+    p.phase_param = cfg.phase_param
+    p.radiance_scale = 0.0
+    p.env_enabled = int(env_enabled and (cfg.env_constant is not None or cfg.sky is not None))
+    p.env_power = 1.0
+    p.env_rotation = 0.0
+    if cfg.sun_elevation_deg is not None:
+        p.sun_enabled = 1
+        p.sun_direction[:] = [float(x) for x in sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg)]
+        p.sun_irradiance[:] = [cfg.sun_irradiance] * 3
+        p.sun_select_prob = cfg.sun_select_prob if p.env_enabled else 1.0
+    p.max_bounces = cfg.max_bounces
+    p.rr_start_vertex = cfg.rr_start_vertex
+    p.majorant_mode = cfg.majorant_mode
+    p.max_steps_per_segment = cfg.max_steps_per_segment
+    return p
+
+
+def constant_environment(value: float, width: int = 64, height: int = 32) -> np.ndarray:
+    return np.full((height, width, 3), value, dtype=np.float32)
+
+
+def setup_scene(r: Renderer, cfg: SceneConfig, volume: np.ndarray | None = None) -> None:
+    """Builds the configuration's scene on the device: volume (generated on the device unless
+    `volume` is given), environment, frame parameters, RNG seeds."""
+    vs, origin = volume_box(cfg.volume)
+    if volume is None:
+        r.generate_fbm_volume(cfg.volume, vs, origin)
+        r._dims = (cfg.volume.n,) * 3
+    else:
+        r.set_volume_dense(volume, vs, origin)
+        r._dims = tuple(volume.shape)
+    if cfg.sky is not None:
+        from . import sky as _sky
+        st = _sky.load_sky_state(cfg.sky, cfg.sun_elevation_deg)
+        d = sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg)
+        r.generate_sky(cfg.sky.width, cfg.sky.height, st["states"], st["solar"], st["cmf"], d,
+                       cfg.sky.include_solar_disc)
+    elif cfg.env_constant is not None:
+        r.set_environment_rgb(constant_environment(cfg.env_constant))
+    r.set_frame(frame_params(cfg))
+    r.seed_rng(cfg.rng_seed)

@@ -1,0 +1,61 @@
+"""Regenerates the golden fixtures from programs built against the reference's own sources.
+
+Run in a checkout that has the reference next to it (REF, default /root/reference):
+
+    python tests/golden/make_golden.py
+
+It builds oracle/_ref/ with oracle/build_ref.sh and writes
+  tests/golden/ref_basic_types.json   common/basic_types.{h,cpp} outputs (polar maps, frames,
+                                      quaternion matrices, 16-band CIE CMF integrals)
+  tests/golden/ref_nanovdb.json       NanoVDB 32.3 GridBuilder / SampleFromVoxels<1> / Ray::clip
+  tests/golden/ref_hosek_kat.json     Hosek-Wilkie radiance at fixed angles (first sky entry)
+  rtc8_gb300/data/hosek_sky.json      per-band sky states used by the sky configurations
+The fixtures are committed; the GPU host never reads the reference.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[2]
+REF_BIN = ROOT / "oracle" / "_ref"
+GOLDEN = ROOT / "tests" / "golden"
+DATA = ROOT / "rtc8_gb300" / "data"
+
+# (solar elevation deg, turbidity, ground albedo; negative = the renderer's per-band ramp)
+SKY_REQUESTS = [(20.0, 3.0, 0.3), (30.0, 4.0, -1.0), (20.0, 4.0, -1.0)]
+
+
+def run(name: str, *args: str) -> dict:
+    out = subprocess.run([str(REF_BIN / name), *args], check=True, capture_output=True, text=True).stdout
+    return json.loads(out)
+
+
+def main() -> int:
+    env = dict(os.environ)
+    subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh")], check=True, env=env)
+    basic = run("ref_kat_basic")
+    (GOLDEN / "ref_basic_types.json").write_text(json.dumps(basic))
+    nvdb = run("ref_kat_nanovdb")
+    (GOLDEN / "ref_nanovdb.json").write_text(json.dumps(nvdb))
+    args = [str(x) for req in SKY_REQUESTS for x in req]
+    sky = run("ref_hosek_dump", *args)
+    kat = sky["entries"][0].pop("radiance_kat")
+    first = sky["entries"][0]
+    (GOLDEN / "ref_hosek_kat.json").write_text(json.dumps({
+        "elevation_deg": first["elevation_deg"], "turbidity": first["turbidity"], "albedo": first["albedo"],
+        "band_theta_gamma_radiance": kat}))
+    DATA.mkdir(exist_ok=True)
+    sky["cmf"] = basic["cmf_xs_ys_zs_centers_integral"]
+    sky["source"] = ("Hosek-Wilkie 2013 v1.4a model states (arhosekskymodelstate_alloc_init) per renderer band, "
+                     "and the renderer's 16-band CIE 1931 CMF integrals, generated by tests/golden/make_golden.py")
+    (DATA / "hosek_sky.json").write_text(json.dumps(sky))
+    print("wrote fixtures")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
