@@ -70,6 +70,13 @@ typedef struct VptFrameParams {
     int32_t rr_start_vertex;     /* Russian roulette from this path length (reference: 1) */
     int32_t majorant_mode;       /* 0 = global majorant (reference), 1 = 8^3 majorant grid DDA */
     int32_t max_steps_per_segment;  /* safety cap on lookups per segment (0 = none) */
+    /* 0 = reference streams: one PCG32 stream per pixel, samples drawn one after the other
+     *     (renderer_main.cpp:86-93, optix_pathtracing_kernels.cu:38, 413); a launch traces a
+     *     pixel's samples in order, so the per-pixel chain bounds the launch time.
+     * 1 = sample-parallel streams: sample s of a pixel starts from the pixel's seed state advanced
+     *     by s * 2^40 draws (PCG jump-ahead), so every (pixel, sample) is an independent work item;
+     *     the per-pixel seed states are not modified by a launch. */
+    int32_t rng_stream_mode;
 } VptFrameParams;
 
 /* ---- context ------------------------------------------------------------------------ */

@@ -36,6 +36,7 @@ class OrcScene(C.Structure):
         ("cam_aspect", C.c_float), ("cam_fovy", C.c_float), ("cam_pos", C.c_float * 3), ("cam_quat", C.c_float * 4),
         ("width", C.c_int32), ("height", C.c_int32),
         ("max_bounces", C.c_int32), ("rr_start", C.c_int32), ("majorant_mode", C.c_int32), ("max_steps", C.c_int32),
+        ("stream_mode", C.c_int32),
     ]
 
 
@@ -127,7 +128,7 @@ class OracleScene:
 def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: float, albedo: float,
                phase_kind: int, phase_param: float, env_rgb: np.ndarray | None, width: int, height: int,
                cam_aspect: float, cam_fovy: float, cam_pos, cam_quat, sun_dir=None, sun_irradiance=0.0,
-               sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, env_power=1.0,
+               sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, stream_mode=0, env_power=1.0,
                env_rotation=0.0, cells: np.ndarray | None = None, global_majorant: float | None = None) -> OracleScene:
     s = OrcScene()
     v = np.ascontiguousarray(voxels, dtype=np.float32)
@@ -185,6 +186,7 @@ def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: 
         s.cam_quat[a] = float(cam_quat[a])
     s.width, s.height = width, height
     s.max_bounces, s.rr_start, s.majorant_mode, s.max_steps = max_bounces, rr_start, majorant_mode, max_steps
+    s.stream_mode = stream_mode
     return OracleScene(s, keep)
 
 
@@ -200,7 +202,8 @@ def scene_from_config(cfg, voxels: np.ndarray, env_rgb: np.ndarray | None, **ove
               cam_pos=np.asarray(cam.position, dtype=np.float32), cam_quat=np.asarray(cam.orientation, np.float32),
               sun_dir=None if sun is None else sun.astype(np.float32), sun_irradiance=cfg.sun_irradiance,
               sun_prob=cfg.sun_select_prob, max_bounces=cfg.max_bounces, rr_start=cfg.rr_start_vertex,
-              majorant_mode=cfg.majorant_mode, max_steps=cfg.max_steps_per_segment)
+              majorant_mode=cfg.majorant_mode, max_steps=cfg.max_steps_per_segment,
+              stream_mode=cfg.rng_stream_mode)
     kw.update(over)
     return make_scene(**kw)
 

@@ -78,6 +78,25 @@ struct Pcg32 {
     }
 };
 
+// Jump-ahead of the PCG32 state by `delta` draws (O(log delta) LCG advance, Brown 1994 as
+// used by the PCG family's pcg_advance).
+inline uint64_t pcg_advance(uint64_t state, uint64_t delta) {
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL;
+    uint64_t acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    return acc_mult * state + acc_plus;
+}
+// Sample-parallel streams: sample s of a pixel starts 2^40 * s draws into the pixel's stream.
+constexpr int kSampleStreamShift = 40;
+
 // common_renderer_types.h:1379-1405 with basic_types.h:857-864 (Duff et al. basis).
 struct Frame {
     V3 t, b, n;
@@ -289,6 +308,8 @@ inline void imp_sample(const OrcScene& s, float u0, float u1, int* px, int* py, 
             *prob *= lower;
             u1 = (u1 - upper) / lower;
         }
+        ix = std::min(ix, cur_w - 1);
+        iy = std::min(iy, cur_h - 1);
         cur_w *= 2;
         cur_h *= 2;
     }
@@ -343,6 +364,12 @@ inline RGB env_evaluate(const OrcScene& s, V3 dir, float* hyp_pdf) {
 }
 
 // ---------------------------------------------------------------- tracking
+// Limits applied when the configurable caps are disabled (same values as the device tracker).
+constexpr uint32_t kHardStepCap = 1u << 24;
+constexpr uint32_t kHardVertexCap = 1u << 16;
+inline uint32_t step_cap(const OrcScene& s) {
+    return s.max_steps > 0 ? static_cast<uint32_t>(s.max_steps) : kHardStepCap;
+}
 // Result of tracking one segment.
 enum SegEnd { SEG_EXIT = 0, SEG_COLLIDE = 1, SEG_CAP = 2 };
 
@@ -400,7 +427,7 @@ inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, f
         const float maj = s.density_coeff * s.global_majorant;
         while (true) {
             t += -std::log(1.0f - rng.uniform()) / maj;
-            if (t > t1) break;
+            if (!(t <= t1)) break;  // also ends the segment on a NaN distance
             float density = density_at(s, eye, dir, t);
             ++*steps;
             ++*lookups;
@@ -411,7 +438,7 @@ inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, f
                 *tio = t;
                 return SEG_COLLIDE;
             }
-            if (s.max_steps > 0 && seg_steps >= static_cast<uint32_t>(s.max_steps)) return SEG_CAP;
+            if (seg_steps >= step_cap(s)) return SEG_CAP;
         }
         *tio = t;
         return SEG_EXIT;
@@ -437,7 +464,7 @@ inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, f
                     *tio = t;
                     return SEG_COLLIDE;
                 }
-                if (s.max_steps > 0 && seg_steps >= static_cast<uint32_t>(s.max_steps)) return SEG_CAP;
+                if (seg_steps >= step_cap(s)) return SEG_CAP;
             }
         }
         t = texit;
@@ -552,6 +579,10 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
     uint32_t end_code = 0;
     while (true) {
         ++path_length;
+        if (path_length > kHardVertexCap) {
+            end_code = ORC_END_MAX_BOUNCES;
+            break;
+        }
         bool collided = false;
         float hit_dist = 1e10f;
         float t0, t1;
@@ -826,6 +857,8 @@ int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum
             int64_t pix = static_cast<int64_t>(y) * s.width + x;
             Pcg32 rng{rng_states[pix]};
             for (int i = 0; i < spp; ++i) {
+                if (s.stream_mode == 1)
+                    rng.state = pcg_advance(rng_states[pix], static_cast<uint64_t>(accum_base + i) << kSampleStreamShift);
                 uint32_t rec[4] = {0, 0, 0, 0};
                 int64_t lk = 0;
                 RGB c = trace_path(s, rng, x, y, rec, &lk);
@@ -838,7 +871,7 @@ int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum
                     sum_rgb[3 * pix + 1] += c.g;
                     sum_rgb[3 * pix + 2] += c.b;
                 }
-                if (mean_rgb) {
+                if (mean_rgb && s.stream_mode == 0) {
                     uint32_t n = static_cast<uint32_t>(accum_base + i);
                     RGB prev = rgb(0, 0, 0);
                     if (n > 0) prev = rgb(mean_rgb[3 * pix], mean_rgb[3 * pix + 1], mean_rgb[3 * pix + 2]);
@@ -849,7 +882,7 @@ int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum
                     mean_rgb[3 * pix + 2] = r.b;
                 }
             }
-            rng_states[pix] = rng.state;
+            if (s.stream_mode == 0) rng_states[pix] = rng.state;
         }
     }
     return total;

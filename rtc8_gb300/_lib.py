@@ -42,6 +42,7 @@ class VptFrameParams(C.Structure):
         ("rr_start_vertex", C.c_int32),
         ("majorant_mode", C.c_int32),
         ("max_steps_per_segment", C.c_int32),
+        ("rng_stream_mode", C.c_int32),
     ]
 
 

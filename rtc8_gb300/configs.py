@@ -59,6 +59,7 @@ class SceneConfig:
     rr_start_vertex: int = 9     # "Russian roulette after 8" bounces
     majorant_mode: int = 1       # 1 = 8^3 majorant grid with DDA
     max_steps_per_segment: int = 1 << 20
+    rng_stream_mode: int = 1       # 0 = reference per-pixel sequential streams, 1 = sample-parallel
     fov_deg: float = 40.0
     cam_distance_diagonals: float = 2.5
     cam_direction: tuple = (0.55, 0.3, 1.0)   # from the grid centre towards the camera
@@ -81,7 +82,7 @@ C1 = SceneConfig(name="c1_dense64_256px", width=256, height=256, spp=16,
 # The same scene rendered with the reference's own path rules: single global majorant,
 # Schlick phase function, no bounce cap, Russian roulette at every vertex, environment only.
 C1_REFERENCE_MODE = C1.replace(name="c1_reference_mode", phase_kind=0, phase_param=0.0, sun_elevation_deg=None,
-                               max_bounces=0, rr_start_vertex=1, majorant_mode=0)
+                               max_bounces=0, rr_start_vertex=1, majorant_mode=0, rng_stream_mode=0)
 
 # BASELINE configuration 2: 1024^2 x 64 spp, sparse 512^3 fBm (6 octaves, threshold 0.55),
 # sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256 bounces, sun at 20 degrees + Hosek sky.

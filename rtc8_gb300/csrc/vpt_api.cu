@@ -358,7 +358,8 @@ int vpt_generate_sky(VptContext* c, int32_t w, int32_t h, const float* states, c
 int vpt_set_frame_params(VptContext* c, const VptFrameParams* p) {
     if (!c || !p) return set_error(VPT_ERR_INVALID_ARGUMENT, "null argument");
     if (!(p->density_coeff >= 0) || p->phase_kind < 0 || p->phase_kind > 1 || p->majorant_mode < 0 || p->majorant_mode > 1 ||
-        p->max_bounces < 0 || !(p->sun_select_prob >= 0 && p->sun_select_prob <= 1))
+        p->max_bounces < 0 || !(p->sun_select_prob >= 0 && p->sun_select_prob <= 1) || p->rng_stream_mode < 0 ||
+        p->rng_stream_mode > 1)
         return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_set_frame_params: bad values");
     c->frame = *p;
     c->has_frame = true;
@@ -460,14 +461,19 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     tp.spp = spp;
     tp.accum_base = c->accum_samples;
     tp.dlog = dlog;
+    tp.stream_mode = c->frame.rng_stream_mode;
+    uint64_t npix = static_cast<uint64_t>(c->width) * c->height;
+    if (npix * spp >= (1ull << 31)) return set_error(VPT_ERR_INVALID_ARGUMENT, "too many samples in one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     int threads = c->threads > 0 ? c->threads : 128;
     bool grid_maj = c->frame.majorant_mode == 1;
     int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr));
     vpt::launch_plain(tp, grid_maj, ctas, threads, s);
-    VPT_CUDA(cudaGetLastError());
     c->accum_samples += spp;
+    if (tp.stream_mode == 1)
+        vpt::launch_finalize_mean(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->accum_samples, s);
+    VPT_CUDA(cudaGetLastError());
     return VPT_OK;
 }
 

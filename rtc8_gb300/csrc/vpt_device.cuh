@@ -68,6 +68,24 @@ struct Pcg32 {
     }
 };
 
+// Jump-ahead of a PCG32 state by `delta` draws (O(log delta) LCG advance, Brown 1994).
+__device__ __forceinline__ uint64_t pcg_advance(uint64_t state, uint64_t delta) {
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL;
+    uint64_t acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    return acc_mult * state + acc_plus;
+}
+// Sample-parallel streams: sample s of a pixel starts 2^40 * s draws into the pixel's stream.
+constexpr int kSampleStreamShift = 40;
+
 // ------------------------------------------------------------------------------ frames
 // common_renderer_types.h:1379-1405 with basic_types.h:857-864.
 struct Frame {
@@ -152,10 +170,17 @@ __device__ __forceinline__ V3 world_to_index(const Grid& g, V3 p) {
               (p.z - g.origin[2]) * g.inv_voxel_size);
 }
 
+// The last leaf a lane looked up: successive tracking steps along a ray mostly stay in the
+// same 8^3 leaf, so the table read (a dependent load before the voxel loads) is skipped.
+struct LeafCache {
+    int32_t key = -1;
+    int32_t slot = -1;
+};
+
 // util/SampleFromVoxels.h:419-459: first-order sampler, lerps along z, then y, then x.
 // When the 2x2x2 stencil lies inside one leaf (about 2/3 of the lookups) it reads one
-// table entry and eight values of that leaf.
-__device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz) {
+// table entry (or the lane's cached one) and eight values of that leaf.
+__device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz, LeafCache& cache) {
     float fi = floorf(xyz.x), fj = floorf(xyz.y), fk = floorf(xyz.z);
     float wx = xyz.x - fi, wy = xyz.y - fj, wz = xyz.z - fk;
     int i = static_cast<int>(fi), j = static_cast<int>(fj), k = static_cast<int>(fk);
@@ -164,7 +189,15 @@ __device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz) {
                   static_cast<uint32_t>(j) < static_cast<uint32_t>(g.ny - 1) &&
                   static_cast<uint32_t>(k) < static_cast<uint32_t>(g.nz - 1);
     if (inside && (i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7) {
-        int32_t slot = leaf_slot(g, i >> 3, j >> 3, k >> 3);
+        int32_t key = ((i >> 3) * g.ly + (j >> 3)) * g.lz + (k >> 3);
+        int32_t slot;
+        if (key == cache.key) {
+            slot = cache.slot;
+        } else {
+            slot = __ldg(g.leaf_table + key);
+            cache.key = key;
+            cache.slot = slot;
+        }
         if (slot < 0) return 0.0f;
         const float* p = g.leaf_values + static_cast<int64_t>(slot) * 512 + (((i & 7) << 6) | ((j & 7) << 3) | (k & 7));
         v000 = __ldg(p);
@@ -196,21 +229,21 @@ __device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz) {
 }
 
 // util/Ray.h:343-363 + :512-520 (slab test, clipped to the ray's [tmin, tmax]).
-__device__ __forceinline__ bool clip_ray(const float bmin[3], const float bmax[3], V3 eye, V3 dir, float tmin,
-                                         float tmax, float* t0o, float* t1o) {
+__device__ __forceinline__ bool clip_ray(V3 bmin, V3 bmax, V3 eye, V3 dir, float tmin, float tmax, float* t0o,
+                                         float* t1o) {
     float ix = 1 / dir.x, iy = 1 / dir.y, iz = 1 / dir.z;
     bool sx = ix < 0, sy = iy < 0, sz = iz < 0;
-    float t0 = ((sx ? bmax[0] : bmin[0]) - eye.x) * ix;
-    float t2 = ((sy ? bmin[1] : bmax[1]) - eye.y) * iy;
+    float t0 = ((sx ? bmax.x : bmin.x) - eye.x) * ix;
+    float t2 = ((sy ? bmin.y : bmax.y) - eye.y) * iy;
     if (t0 > t2) return false;
-    float t1 = ((sx ? bmin[0] : bmax[0]) - eye.x) * ix;
-    float t3 = ((sy ? bmax[1] : bmin[1]) - eye.y) * iy;
+    float t1 = ((sx ? bmin.x : bmax.x) - eye.x) * ix;
+    float t3 = ((sy ? bmax.y : bmin.y) - eye.y) * iy;
     if (t3 > t1) return false;
     if (t3 > t0) t0 = t3;
     if (t2 < t1) t1 = t2;
-    t3 = ((sz ? bmax[2] : bmin[2]) - eye.z) * iz;
+    t3 = ((sz ? bmax.z : bmin.z) - eye.z) * iz;
     if (t3 > t1) return false;
-    t2 = ((sz ? bmin[2] : bmax[2]) - eye.z) * iz;
+    t2 = ((sz ? bmin.z : bmax.z) - eye.z) * iz;
     if (t0 > t2) return false;
     if (t3 > t0) t0 = t3;
     if (tmax < t0) return false;
@@ -314,6 +347,9 @@ __device__ __forceinline__ void imp_sample(const Env& e, float u0, float u1, int
             p *= lower;
             u1 = (u1 - upper) / lower;
         }
+        // Only an all-zero map can step outside the level (0 / 0 picks the right column).
+        ix = min(ix, cur_w - 1);
+        iy = min(iy, cur_h - 1);
         cur_w *= 2;
         cur_h *= 2;
     }

@@ -30,6 +30,11 @@ enum : uint32_t {
 
 enum : uint32_t { END_ESCAPE = 1, END_RR = 2, END_PDF_ZERO = 3, END_MAX_BOUNCES = 4, END_STEP_CAP = 5 };
 
+// Limits that apply even when the caller disables the configurable caps, so that no input
+// (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
+constexpr uint32_t kHardStepCap = 1u << 24;
+constexpr uint32_t kHardVertexCap = 1u << 16;
+
 struct DdaState {
     int cell[3];
     int step[3];
@@ -68,6 +73,9 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
     const Grid& g = P.grid;
     const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
     const float global_maj = P.density_coeff * g.global_majorant;
+    const uint32_t step_cap = P.max_steps > 0 ? static_cast<uint32_t>(P.max_steps) : kHardStepCap;
+    const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
+    const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
 
     uint32_t st = ST_FETCH;
     uint32_t pixel = 0, sample = 0;
@@ -97,6 +105,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
 
     unsigned long long n_lookups = 0, n_vertices = 0, n_samples = 0;
     unsigned int err = 0;
+    LeafCache leaf_cache;
 
     while (true) {
         // ---------------------------------------------------------------- divergent part
@@ -105,6 +114,20 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
         while (!need_lookup && st != ST_DONE) {
             switch (st) {
             case ST_FETCH: {
+                if (P.stream_mode == 1) {
+                    // One (pixel, sample) per work item, samples of all pixels interleaved.
+                    uint32_t item = atomicAdd(P.work_counter, 1u);
+                    if (item >= num_pixels * P.spp) {
+                        st = ST_DONE;
+                        break;
+                    }
+                    pixel = item % num_pixels;
+                    sample = item / num_pixels;
+                    rng.state = pcg_advance(P.rng[pixel], static_cast<uint64_t>(P.accum_base + sample)
+                                                              << kSampleStreamShift);
+                    st = ST_CAMERA;
+                    break;
+                }
                 pixel = atomicAdd(P.work_counter, 1u);
                 if (pixel >= num_pixels) {
                     st = ST_DONE;
@@ -150,8 +173,13 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
             case ST_SEGMENT: {
                 ++path_length;
                 ++n_vertices;
+                if (path_length > kHardVertexCap) {
+                    end_code = END_MAX_BOUNCES;
+                    st = ST_END_SAMPLE;
+                    break;
+                }
                 float a, b;
-                if (clip_ray(g.bbox_min, g.bbox_max, origin, dir, 0.0f, 1e10f, &a, &b)) {
+                if (clip_ray(bmin, bmax, origin, dir, 0.0f, 1e10f, &a, &b)) {
                     shadow = false;
                     seg_eye = origin;
                     seg_dir = dir;
@@ -174,7 +202,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                 if constexpr (!kGridMajorant) {
                     // optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378.
                     t += -logf(1.0f - rng.uniform()) / maj;
-                    if (t > t1) {
+                    if (!(t <= t1)) {  // also ends the segment on a NaN distance
                         st = shadow ? ST_NEE_DONE : ST_ESCAPE;
                     } else {
                         lookup_pos = seg_eye + seg_dir * t;
@@ -199,16 +227,23 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                             seg_end = true;
                             break;
                         }
-                        int ax = (dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2]) ? 0
-                                 : (dda.tnext[1] <= dda.tnext[2] ? 1 : 2);
-                        dda.cell[ax] += dda.step[ax];
-                        int lim = ax == 0 ? g.lx : (ax == 1 ? g.ly : g.lz);
-                        if (dda.cell[ax] < 0 || dda.cell[ax] >= lim) {
+                        // Advance along the axis whose boundary comes first (x, then y, then z on
+                        // ties); written with selects so the DDA state stays in registers.
+                        bool ax0 = dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2];
+                        bool ax1 = !ax0 && dda.tnext[1] <= dda.tnext[2];
+                        bool ax2 = !ax0 && !ax1;
+                        if (ax0) dda.cell[0] += dda.step[0];
+                        if (ax1) dda.cell[1] += dda.step[1];
+                        if (ax2) dda.cell[2] += dda.step[2];
+                        if (dda.cell[0] < 0 || dda.cell[0] >= g.lx || dda.cell[1] < 0 || dda.cell[1] >= g.ly ||
+                            dda.cell[2] < 0 || dda.cell[2] >= g.lz) {
                             t = t1;
                             seg_end = true;
                             break;
                         }
-                        dda.tnext[ax] += dda.tdelta[ax];
+                        if (ax0) dda.tnext[0] += dda.tdelta[0];
+                        if (ax1) dda.tnext[1] += dda.tdelta[1];
+                        if (ax2) dda.tnext[2] += dda.tdelta[2];
                         texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
                         maj = P.density_coeff *
                               __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
@@ -296,7 +331,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                 seg_dir = -light_dir;
                 seg_eye = origin + trace_len * -seg_dir;
                 float a, b;
-                if (clip_ray(g.bbox_min, g.bbox_max, seg_eye, seg_dir, 0.0f, trace_len, &a, &b)) {
+                if (clip_ray(bmin, bmax, seg_eye, seg_dir, 0.0f, trace_len, &a, &b)) {
                     shadow = true;
                     t = fmaxf(0.0f, a);
                     t1 = b;
@@ -368,6 +403,17 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                     uint4 rec = make_uint4(path_length, rec_primary, rec_shadow, end_code);
                     reinterpret_cast<uint4*>(P.dlog)[static_cast<uint64_t>(pixel) * P.spp + sample] = rec;
                 }
+                if (P.stream_mode == 1) {
+                    if (all_nonneg_finite(contribution)) {
+                        atomicAdd(P.sum_rgb + 3 * pixel, static_cast<double>(contribution.r));
+                        atomicAdd(P.sum_rgb + 3 * pixel + 1, static_cast<double>(contribution.g));
+                        atomicAdd(P.sum_rgb + 3 * pixel + 2, static_cast<double>(contribution.b));
+                    } else {
+                        err |= VPT_DEVERR_NONFINITE;
+                    }
+                    st = ST_FETCH;
+                    break;
+                }
                 if (all_nonneg_finite(contribution)) {
                     sum_r += contribution.r;
                     sum_g += contribution.g;
@@ -407,7 +453,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
 
         // ---------------------------------------------------------------- converged lookups
         float density = 0.0f;
-        if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos));
+        if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos), leaf_cache);
 
         if (need_lookup) {
             ++n_lookups;
@@ -419,7 +465,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                 ++rec_primary;
                 if (rng.uniform() < density / maj) st = ST_VERTEX;
             }
-            if (st == ST_STEP && P.max_steps > 0 && seg_steps >= static_cast<uint32_t>(P.max_steps)) {
+            if (st == ST_STEP && seg_steps >= step_cap) {
                 err |= VPT_DEVERR_STEP_CAP;
                 end_code = END_STEP_CAP;
                 st = ST_END_SAMPLE;
@@ -443,7 +489,18 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
     }
 }
 
+// Mean image of the sample-parallel mode: FP64 sums over the samples accumulated so far.
+__global__ void finalize_mean_kernel(const double* __restrict__ sum, float* __restrict__ mean, uint32_t n,
+                                     double inv_samples) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mean[i] = static_cast<float>(sum[i] * inv_samples);
+}
+
 }  // namespace
+
+void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s) {
+    finalize_mean_kernel<<<(n_values + 255) / 256, 256, 0, s>>>(sum, mean, n_values, 1.0 / samples);
+}
 
 const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
     if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true>)

@@ -34,6 +34,7 @@ struct TraceParams {
 
     uint32_t spp;             // samples per pixel in this launch
     uint32_t accum_base;      // samples already accumulated (numAccumFrames of the first one)
+    int32_t stream_mode;      // 0 = per-pixel sequential streams, 1 = sample-parallel streams
 
     uint64_t* rng;            // per pixel
     double* sum_rgb;          // 3 per pixel
@@ -45,5 +46,6 @@ struct TraceParams {
 };
 
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, cudaStream_t s);
+void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
 
 }  // namespace vpt

@@ -192,6 +192,7 @@ def frame_params(cfg: SceneConfig, env_enabled: bool = True) -> VptFrameParams:
     p.rr_start_vertex = cfg.rr_start_vertex
     p.majorant_mode = cfg.majorant_mode
     p.max_steps_per_segment = cfg.max_steps_per_segment
+    p.rng_stream_mode = cfg.rng_stream_mode
     return p
 
 
