@@ -77,6 +77,9 @@ typedef struct VptFrameParams {
      *     by s * 2^40 draws (PCG jump-ahead), so every (pixel, sample) is an independent work item;
      *     the per-pixel seed states are not modified by a launch. */
     int32_t rng_stream_mode;
+    /* log2 of the majorant-grid cell size in voxels (>= 3; 3 = one cell per 8^3 leaf). Larger
+     * cells mean fewer DDA steps per ray and looser majorants. */
+    int32_t majorant_cell_log2;
 } VptFrameParams;
 
 /* ---- context ------------------------------------------------------------------------ */
@@ -158,9 +161,10 @@ int vpt_download_mean(VptContext* ctx, float* host_rgb);
 /* Device pointers of the accumulation buffers (FP64 sum, FP32 mean; 3 values per pixel). */
 int vpt_get_accum_device_ptrs(VptContext* ctx, double** dev_sum, float** dev_mean);
 
-/* Work counters of the last launches since the last reset: density lookups, path vertices,
- * samples. Enabled by default; read back with a synchronisation. */
-int vpt_get_counters(VptContext* ctx, uint64_t* lookups, uint64_t* vertices, uint64_t* samples);
+/* Work counters of the launches since the last reset: density lookups, path vertices,
+ * samples, majorant-grid cell steps. Read back with a synchronisation. */
+int vpt_get_counters(VptContext* ctx, uint64_t* lookups, uint64_t* vertices, uint64_t* samples,
+                     uint64_t* cell_steps);
 int vpt_reset_counters(VptContext* ctx);
 uint32_t vpt_get_device_errors(VptContext* ctx);
 int vpt_synchronize(VptContext* ctx, void* stream);

@@ -36,7 +36,7 @@ class OrcScene(C.Structure):
         ("cam_aspect", C.c_float), ("cam_fovy", C.c_float), ("cam_pos", C.c_float * 3), ("cam_quat", C.c_float * 4),
         ("width", C.c_int32), ("height", C.c_int32),
         ("max_bounces", C.c_int32), ("rr_start", C.c_int32), ("majorant_mode", C.c_int32), ("max_steps", C.c_int32),
-        ("stream_mode", C.c_int32),
+        ("stream_mode", C.c_int32), ("maj_shift", C.c_int32),
     ]
 
 
@@ -114,6 +114,15 @@ def majorants(vox: np.ndarray) -> tuple[np.ndarray, float]:
     return cells, float(g)
 
 
+def pool_cells(cells: np.ndarray, factor: int) -> np.ndarray:
+    """Majorant cells of `factor`^3 times the volume (max-pooling, ragged edges included)."""
+    cx, cy, cz = cells.shape
+    mx, my, mz = (-(-cx // factor), -(-cy // factor), -(-cz // factor))
+    pad = np.zeros((mx * factor, my * factor, mz * factor), dtype=np.float32)
+    pad[:cx, :cy, :cz] = cells
+    return pad.reshape(mx, factor, my, factor, mz, factor).max(axis=(1, 3, 5))
+
+
 @dataclass
 class OracleScene:
     """Keeps the arrays referenced by an OrcScene alive."""
@@ -128,7 +137,8 @@ class OracleScene:
 def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: float, albedo: float,
                phase_kind: int, phase_param: float, env_rgb: np.ndarray | None, width: int, height: int,
                cam_aspect: float, cam_fovy: float, cam_pos, cam_quat, sun_dir=None, sun_irradiance=0.0,
-               sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, stream_mode=0, env_power=1.0,
+               sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, stream_mode=0, maj_shift=3,
+               env_power=1.0,
                env_rotation=0.0, cells: np.ndarray | None = None, global_majorant: float | None = None) -> OracleScene:
     s = OrcScene()
     v = np.ascontiguousarray(voxels, dtype=np.float32)
@@ -150,6 +160,9 @@ def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: 
     s.world_radius = float(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])))
     if cells is None or global_majorant is None:
         cells, global_majorant = majorants(v)
+    if maj_shift > 3:
+        cells = pool_cells(cells, 1 << (maj_shift - 3))
+    s.maj_shift = max(maj_shift, 3)
     cells = np.ascontiguousarray(cells, dtype=np.float32)
     keep.append(cells)
     s.global_majorant = global_majorant
@@ -203,7 +216,7 @@ def scene_from_config(cfg, voxels: np.ndarray, env_rgb: np.ndarray | None, **ove
               sun_dir=None if sun is None else sun.astype(np.float32), sun_irradiance=cfg.sun_irradiance,
               sun_prob=cfg.sun_select_prob, max_bounces=cfg.max_bounces, rr_start=cfg.rr_start_vertex,
               majorant_mode=cfg.majorant_mode, max_steps=cfg.max_steps_per_segment,
-              stream_mode=cfg.rng_stream_mode)
+              stream_mode=cfg.rng_stream_mode, maj_shift=cfg.majorant_cell_log2)
     kw.update(over)
     return make_scene(**kw)
 

@@ -395,19 +395,21 @@ inline void dda_init(const OrcScene& s, V3 eye, V3 dir, float t, Dda* d) {
                   (eye.z - s.origin[2]) * s.inv_voxel_size};
     float dd[3] = {dir.x * s.inv_voxel_size, dir.y * s.inv_voxel_size, dir.z * s.inv_voxel_size};
     int cdim[3] = {s.cx, s.cy, s.cz};
+    const float size = static_cast<float>(1 << (s.maj_shift < 3 ? 3 : s.maj_shift));
+    const float inv_size = 1.0f / size;
     for (int a = 0; a < 3; ++a) {
         float p = o[a] + dd[a] * t;
-        int c = static_cast<int>(std::floor(p * 0.125f));
+        int c = static_cast<int>(std::floor(p * inv_size));
         c = std::min(std::max(c, 0), cdim[a] - 1);
         d->cell[a] = c;
         if (dd[a] > 0) {
             d->step[a] = 1;
-            d->tnext[a] = ((c + 1) * 8.0f - o[a]) / dd[a];
-            d->tdelta[a] = 8.0f / dd[a];
+            d->tnext[a] = ((c + 1) * size - o[a]) / dd[a];
+            d->tdelta[a] = size / dd[a];
         } else if (dd[a] < 0) {
             d->step[a] = -1;
-            d->tnext[a] = (c * 8.0f - o[a]) / dd[a];
-            d->tdelta[a] = -8.0f / dd[a];
+            d->tnext[a] = (c * size - o[a]) / dd[a];
+            d->tdelta[a] = -size / dd[a];
         } else {
             d->step[a] = 0;
             d->tnext[a] = INFINITY;

@@ -65,6 +65,7 @@ typedef struct OrcScene {
     int32_t majorant_mode;     /* 0 = single global majorant, 1 = per-cell majorant DDA */
     int32_t max_steps;         /* safety cap on density lookups per segment, 0 = none */
     int32_t stream_mode;       /* 0 = per-pixel sequential streams, 1 = sample s jumped by s * 2^40 */
+    int32_t maj_shift;         /* majorant cells of 2^maj_shift voxels (cell_majorant has cx*cy*cz) */
 } OrcScene;
 
 /* Per-sample decision record: vertices, primary lookups, shadow lookups, end code. */

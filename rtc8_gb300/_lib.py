@@ -43,6 +43,7 @@ class VptFrameParams(C.Structure):
         ("majorant_mode", C.c_int32),
         ("max_steps_per_segment", C.c_int32),
         ("rng_stream_mode", C.c_int32),
+        ("majorant_cell_log2", C.c_int32),
     ]
 
 
@@ -75,7 +76,7 @@ _VPT = {
     "vpt_download_sum": (C.c_int, [C.c_void_p, c_double_p, c_u32_p]),
     "vpt_download_mean": (C.c_int, [C.c_void_p, c_float_p]),
     "vpt_get_accum_device_ptrs": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
-    "vpt_get_counters": (C.c_int, [C.c_void_p, c_u64_p, c_u64_p, c_u64_p]),
+    "vpt_get_counters": (C.c_int, [C.c_void_p, c_u64_p, c_u64_p, c_u64_p, c_u64_p]),
     "vpt_reset_counters": (C.c_int, [C.c_void_p]),
     "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
     "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -60,6 +60,7 @@ class SceneConfig:
     majorant_mode: int = 1       # 1 = 8^3 majorant grid with DDA
     max_steps_per_segment: int = 1 << 20
     rng_stream_mode: int = 1       # 0 = reference per-pixel sequential streams, 1 = sample-parallel
+    majorant_cell_log2: int = 3    # majorant-grid cell = 2^k voxels (3: one cell per 8^3 leaf)
     fov_deg: float = 40.0
     cam_distance_diagonals: float = 2.5
     cam_direction: tuple = (0.55, 0.3, 1.0)   # from the grid centre towards the camera
@@ -89,13 +90,15 @@ C1_REFERENCE_MODE = C1.replace(name="c1_reference_mode", phase_kind=0, phase_par
 C2 = SceneConfig(name="c2_sparse512_1024px", width=1024, height=1024, spp=64,
                  volume=VolumeSpec(n=512, seed=2, octaves=6, threshold=0.55, sigma_t_max=200.0),
                  albedo=0.999, phase_kind=1, phase_param=0.85, sun_elevation_deg=20.0, env_constant=None,
-                 sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=256, rr_start_vertex=9)
+                 sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=256, rr_start_vertex=9,
+                 majorant_cell_log2=5)
 
 # BASELINE configuration 5 (stress): 2048^2, sparse 1024^3, sigma_t max 400, albedo 0.9995, g = 0.9.
 C5 = SceneConfig(name="c5_sparse1024_2048px", width=2048, height=2048, spp=16,
                  volume=VolumeSpec(n=1024, seed=5, octaves=6, threshold=0.6, sigma_t_max=400.0),
                  albedo=0.9995, phase_kind=1, phase_param=0.9, sun_elevation_deg=20.0, env_constant=None,
-                 sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=1024, rr_start_vertex=9)
+                 sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=1024, rr_start_vertex=9,
+                 majorant_cell_log2=6)
 
 CONFIGS = {c.name: c for c in (C1, C1_REFERENCE_MODE, C2, C5)}
 

@@ -110,6 +110,7 @@ int vpt_destroy(VptContext* c) {
     dev_free(&c->d_leaf_table);
     dev_free(&c->d_leaf_values);
     dev_free(&c->d_cell_maj);
+    dev_free(&c->d_maj);
     dev_free(&c->d_dense);
     dev_free(&c->d_env);
     dev_free(&c->d_mips);
@@ -124,6 +125,7 @@ int vpt_seed_rng(VptContext* c, uint64_t seed) {
     std::mt19937_64 gen(seed);
     for (int64_t i = 0; i < npix; ++i) states[i] = gen();
     VPT_CUDA(cudaMemcpy(c->d_rng, states.data(), npix * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    c->stream_samples = 0;
     return vpt_reset_accumulation(c);
 }
 
@@ -197,6 +199,7 @@ static int build_grid_from_dense(VptContext* c, const float* d_dense, int nx, in
     // compute_light_probs.cu:139-157: world AABB = grid box (no meshes), radius = |max - centre|.
     c->world_radius = std::sqrt(r2);
     c->has_volume = true;
+    c->maj_shift = 0;  // the pooled majorant grid is rebuilt at the next launch
     VPT_CUDA(cudaDeviceSynchronize());
     return VPT_OK;
 }
@@ -359,7 +362,7 @@ int vpt_set_frame_params(VptContext* c, const VptFrameParams* p) {
     if (!c || !p) return set_error(VPT_ERR_INVALID_ARGUMENT, "null argument");
     if (!(p->density_coeff >= 0) || p->phase_kind < 0 || p->phase_kind > 1 || p->majorant_mode < 0 || p->majorant_mode > 1 ||
         p->max_bounces < 0 || !(p->sun_select_prob >= 0 && p->sun_select_prob <= 1) || p->rng_stream_mode < 0 ||
-        p->rng_stream_mode > 1)
+        p->rng_stream_mode > 1 || p->majorant_cell_log2 < 0 || p->majorant_cell_log2 > 10)
         return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_set_frame_params: bad values");
     c->frame = *p;
     c->has_frame = true;
@@ -377,14 +380,37 @@ int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads) {
 }  // extern "C"
 
 namespace vpt {
+// Majorant grid of the DDA for the frame's cell size, max-pooled from the 8^3-voxel cells.
+static int ensure_majorant_grid(VptContextImpl* c) {
+    int shift = c->frame.majorant_cell_log2 < 3 ? 3 : c->frame.majorant_cell_log2;
+    if (c->d_maj && c->maj_shift == shift) return VPT_OK;
+    int factor = 1 << (shift - 3);
+    c->mx = (c->lx + factor - 1) / factor;
+    c->my = (c->ly + factor - 1) / factor;
+    c->mz = (c->lz + factor - 1) / factor;
+    int rc;
+    if ((rc = dev_alloc(&c->d_maj, static_cast<size_t>(c->mx) * c->my * c->mz))) return rc;
+    pool_majorants(c->d_cell_maj, c->lx, c->ly, c->lz, c->d_maj, c->mx, c->my, c->mz, factor, 0);
+    VPT_CUDA(cudaDeviceSynchronize());
+    c->maj_shift = shift;
+    return VPT_OK;
+}
+
 int fill_trace_params(VptContextImpl* c, TraceParams* tp) {
     if (!c->has_volume || !c->has_frame) return set_error(VPT_ERR_NOT_READY, "volume or frame parameters missing");
+    int rc = ensure_majorant_grid(c);
+    if (rc) return rc;
     const VptFrameParams& f = c->frame;
     std::memset(tp, 0, sizeof(*tp));
     Grid& g = tp->grid;
     g.leaf_table = c->d_leaf_table;
     g.leaf_values = c->d_leaf_values;
     g.cell_majorant = c->d_cell_maj;
+    g.maj = c->d_maj;
+    g.mx = c->mx;
+    g.my = c->my;
+    g.mz = c->mz;
+    g.maj_shift = c->maj_shift;
     g.nx = c->nx;
     g.ny = c->ny;
     g.nz = c->nz;
@@ -440,11 +466,11 @@ int fill_trace_params(VptContextImpl* c, TraceParams* tp) {
     return VPT_OK;
 }
 
-int persistent_grid(VptContextImpl* c, int threads, const void* kernel) {
+int persistent_grid(VptContextImpl* c, int threads, const void* kernel, size_t smem) {
     int per_sm = c->ctas_per_sm;
     if (per_sm <= 0) {
         int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0) != cudaSuccess || occ <= 0) occ = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ <= 0) occ = 1;
         per_sm = occ;
     }
     return c->num_sms * per_sm;
@@ -462,15 +488,22 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     tp.accum_base = c->accum_samples;
     tp.dlog = dlog;
     tp.stream_mode = c->frame.rng_stream_mode;
+    tp.stream_base = c->stream_samples;
     uint64_t npix = static_cast<uint64_t>(c->width) * c->height;
     if (npix * spp >= (1ull << 31)) return set_error(VPT_ERR_INVALID_ARGUMENT, "too many samples in one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     int threads = c->threads > 0 ? c->threads : 128;
     bool grid_maj = c->frame.majorant_mode == 1;
-    int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr));
-    vpt::launch_plain(tp, grid_maj, ctas, threads, s);
+    size_t smem = 0;
+    if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {
+        tp.maj_in_smem = 1;
+        smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
+    }
+    int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr), smem);
+    vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
     c->accum_samples += spp;
+    c->stream_samples += spp;
     if (tp.stream_mode == 1)
         vpt::launch_finalize_mean(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->accum_samples, s);
     VPT_CUDA(cudaGetLastError());
@@ -508,7 +541,7 @@ int vpt_get_accum_device_ptrs(VptContext* c, double** sum, float** mean) {
     return VPT_OK;
 }
 
-int vpt_get_counters(VptContext* c, uint64_t* lookups, uint64_t* vertices, uint64_t* samples) {
+int vpt_get_counters(VptContext* c, uint64_t* lookups, uint64_t* vertices, uint64_t* samples, uint64_t* cells) {
     if (!c) return set_error(VPT_ERR_INVALID_ARGUMENT, "null context");
     unsigned long long h[8];
     VPT_CUDA(cudaDeviceSynchronize());
@@ -516,6 +549,7 @@ int vpt_get_counters(VptContext* c, uint64_t* lookups, uint64_t* vertices, uint6
     if (lookups) *lookups = h[0];
     if (vertices) *vertices = h[1];
     if (samples) *samples = h[2];
+    if (cells) *cells = h[3];
     return VPT_OK;
 }
 

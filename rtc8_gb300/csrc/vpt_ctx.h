@@ -22,6 +22,7 @@ struct VptContextImpl {
     double* d_sum = nullptr;
     float* d_mean = nullptr;
     uint32_t accum_samples = 0;
+    uint32_t stream_samples = 0;   // samples ever traced since seeding (sample-parallel streams)
 
     unsigned int* d_work = nullptr;
     unsigned long long* d_counters = nullptr;
@@ -35,6 +36,8 @@ struct VptContextImpl {
     int32_t* d_leaf_table = nullptr;
     float* d_leaf_values = nullptr;
     float* d_cell_maj = nullptr;
+    float* d_maj = nullptr;          // majorant grid of the DDA (pooled cells)
+    int32_t mx = 0, my = 0, mz = 0, maj_shift = 0;
     int32_t nx = 0, ny = 0, nz = 0, lx = 0, ly = 0, lz = 0;
     int64_t active_leaves = 0, total_leaves = 0;
     float global_majorant = 0, voxel_size = 1, inv_voxel_size = 1;
@@ -59,7 +62,7 @@ struct VptContextImpl {
 
 int ctx_set_error(int code, const char* msg);
 int fill_trace_params(VptContextImpl* c, TraceParams* tp);
-int persistent_grid(VptContextImpl* c, int threads, const void* kernel);
+int persistent_grid(VptContextImpl* c, int threads, const void* kernel, size_t smem);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);

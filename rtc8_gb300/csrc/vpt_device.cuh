@@ -143,7 +143,11 @@ __device__ __forceinline__ V3 mul(const M3& m, V3 v) {
 struct Grid {
     const int32_t* __restrict__ leaf_table;   // lx*ly*lz, slot or -1
     const float* __restrict__ leaf_values;    // slot * 512 + local
-    const float* __restrict__ cell_majorant;  // lx*ly*lz
+    const float* __restrict__ cell_majorant;  // lx*ly*lz (8^3-voxel cells)
+    // Majorant grid of the DDA: cells of 2^maj_shift voxels (maj_shift >= 3), max-pooled from
+    // the 8^3-voxel cells, mx*my*mz values.
+    const float* __restrict__ maj;
+    int32_t mx, my, mz, maj_shift;
     int32_t nx, ny, nz;
     int32_t lx, ly, lz;
     float inv_voxel_size;

@@ -2,14 +2,15 @@
 // ray-generation program, renderer/gpu_kernels/optix_pathtracing_kernels.cu:31-434 with
 // withNRC = generateTrainingData = false, for volume-only scenes).
 //
-// GB300 layout: one resident set of CTAs per SM; each lane owns one pixel at a time,
-// traces all of that launch's samples of the pixel (so the pixel's PCG32 stream advances
-// exactly as in the reference, one sample after the other) and fetches the next pixel
-// from a global counter when done (path regeneration, no idle lanes at the tail of a
-// long path). Each loop iteration first lets every lane run its cheap, divergent event
-// logic (camera ray, vertex, Russian roulette, NEE set-up, phase sampling, accumulation)
-// until it needs a density value, then all lanes perform their grid lookups together,
-// so the dominant gathers of delta tracking and ratio tracking run converged.
+// GB300 layout: one resident set of CTAs per SM pulls work items from a global counter (path
+// regeneration: a lane that finishes a path starts the next one at once). A work item is a
+// pixel (reference streams: its samples are traced in order so the pixel's PCG32 stream
+// advances exactly as in the reference) or one (pixel, sample) pair (sample-parallel streams).
+// Each loop iteration first lets every lane run its cheap, divergent event logic (camera ray,
+// vertex, Russian roulette, NEE set-up, phase sampling, accumulation, a bounded number of
+// majorant-grid cell steps) until it needs a density value, then all lanes perform their grid
+// lookups together, so the dominant gathers of delta and ratio tracking run converged. The
+// majorant grid is staged in shared memory when it fits.
 #include "vpt_ctx.h"
 #include "vpt_tracer.cuh"
 
@@ -17,14 +18,14 @@ namespace vpt {
 namespace {
 
 enum : uint32_t {
-    ST_FETCH = 0,    // get the next pixel
+    ST_FETCH = 0,    // get the next work item
     ST_CAMERA,       // start a sample: camera ray
     ST_SEGMENT,      // start a primary segment: ++pathLength, clip
     ST_STEP,         // advance the current segment to its next lookup
     ST_VERTEX,       // primary collision: RR, NEE set-up
     ST_NEE_DONE,     // shadow segment finished: NEE contribution, phase sampling
     ST_ESCAPE,       // primary segment left the grid
-    ST_END_SAMPLE,   // accumulate, next sample or next pixel
+    ST_END_SAMPLE,   // accumulate, next sample or next item
     ST_DONE,
 };
 
@@ -34,6 +35,8 @@ enum : uint32_t { END_ESCAPE = 1, END_RR = 2, END_PDF_ZERO = 3, END_MAX_BOUNCES 
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
+// Majorant-grid cells a lane may cross in one divergent pass before yielding to the warp.
+constexpr int kCellStepsPerPass = 4;
 
 struct DdaState {
     int cell[3];
@@ -41,25 +44,29 @@ struct DdaState {
     float tnext[3], tdelta[3];
 };
 
+// Majorant-grid DDA in index space. Cells are 2^maj_shift voxels wide; shared definition with
+// the oracle's restatement (overshooting a cell's exit restarts sampling at the exit).
 __device__ __forceinline__ void dda_init(const Grid& g, V3 eye, V3 dir, float t, DdaState* d) {
     float o[3] = {(eye.x - g.origin[0]) * g.inv_voxel_size, (eye.y - g.origin[1]) * g.inv_voxel_size,
                   (eye.z - g.origin[2]) * g.inv_voxel_size};
     float dd[3] = {dir.x * g.inv_voxel_size, dir.y * g.inv_voxel_size, dir.z * g.inv_voxel_size};
-    int cdim[3] = {g.lx, g.ly, g.lz};
+    int cdim[3] = {g.mx, g.my, g.mz};
+    const float size = static_cast<float>(1 << g.maj_shift);
+    const float inv_size = 1.0f / size;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         float p = o[a] + dd[a] * t;
-        int c = static_cast<int>(floorf(p * 0.125f));
+        int c = static_cast<int>(floorf(p * inv_size));
         c = min(max(c, 0), cdim[a] - 1);
         d->cell[a] = c;
         if (dd[a] > 0) {
             d->step[a] = 1;
-            d->tnext[a] = ((c + 1) * 8.0f - o[a]) / dd[a];
-            d->tdelta[a] = 8.0f / dd[a];
+            d->tnext[a] = ((c + 1) * size - o[a]) / dd[a];
+            d->tdelta[a] = size / dd[a];
         } else if (dd[a] < 0) {
             d->step[a] = -1;
-            d->tnext[a] = (c * 8.0f - o[a]) / dd[a];
-            d->tdelta[a] = -8.0f / dd[a];
+            d->tnext[a] = (c * size - o[a]) / dd[a];
+            d->tdelta[a] = -size / dd[a];
         } else {
             d->step[a] = 0;
             d->tnext[a] = INFINITY;
@@ -68,9 +75,23 @@ __device__ __forceinline__ void dda_init(const Grid& g, V3 eye, V3 dir, float t,
     }
 }
 
+__device__ __forceinline__ float cell_maj(const float* maj, const Grid& g, const DdaState& d) {
+    return maj[(d.cell[0] * g.my + d.cell[1]) * g.mz + d.cell[2]];
+}
+
 template <bool kGridMajorant, bool kLog>
 __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
+    extern __shared__ float s_maj[];
     const Grid& g = P.grid;
+    const float* maj_grid = g.maj;
+    if constexpr (kGridMajorant) {
+        if (P.maj_in_smem) {
+            const int cells = g.mx * g.my * g.mz;
+            for (int i = threadIdx.x; i < cells; i += blockDim.x) s_maj[i] = g.maj[i];
+            __syncthreads();
+            maj_grid = s_maj;
+        }
+    }
     const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
     const float global_maj = P.density_coeff * g.global_majorant;
     const uint32_t step_cap = P.max_steps > 0 ? static_cast<uint32_t>(P.max_steps) : kHardStepCap;
@@ -103,15 +124,15 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
     float area_pdf = 1.0f, vis = 1.0f;
     bool pick_sun = false;
 
-    unsigned long long n_lookups = 0, n_vertices = 0, n_samples = 0;
+    unsigned long long n_lookups = 0, n_vertices = 0, n_samples = 0, n_cells = 0;
     unsigned int err = 0;
     LeafCache leaf_cache;
 
     while (true) {
         // ---------------------------------------------------------------- divergent part
-        bool need_lookup = false;
+        bool need_lookup = false, yield = false;
         V3 lookup_pos = v3(0, 0, 0);
-        while (!need_lookup && st != ST_DONE) {
+        while (!need_lookup && !yield && st != ST_DONE) {
             switch (st) {
             case ST_FETCH: {
                 if (P.stream_mode == 1) {
@@ -123,7 +144,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                     }
                     pixel = item % num_pixels;
                     sample = item / num_pixels;
-                    rng.state = pcg_advance(P.rng[pixel], static_cast<uint64_t>(P.accum_base + sample)
+                    rng.state = pcg_advance(P.rng[pixel], static_cast<uint64_t>(P.stream_base + sample)
                                                               << kSampleStreamShift);
                     st = ST_CAMERA;
                     break;
@@ -189,8 +210,9 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                     if constexpr (kGridMajorant) {
                         dda_init(g, seg_eye, seg_dir, t, &dda);
                         texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
-                        maj = P.density_coeff *
-                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                        maj = P.density_coeff * cell_maj(maj_grid, g, dda);
+                    } else {
+                        maj = global_maj;
                     }
                     st = ST_STEP;
                 } else {
@@ -210,9 +232,9 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                     }
                 } else {
                     // Majorant-grid DDA: sample within the current cell; overshooting its exit
-                    // restarts at the exit (memoryless), empty cells are skipped without draws.
+                    // restarts at the exit (memoryless); empty cells are skipped without draws.
                     bool seg_end = false;
-                    while (true) {
+                    for (int c = 0; c < kCellStepsPerPass; ++c) {
                         if (maj > 0) {
                             float tt = t + -logf(1.0f - rng.uniform()) / maj;
                             if (tt < texit) {
@@ -235,8 +257,9 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                         if (ax0) dda.cell[0] += dda.step[0];
                         if (ax1) dda.cell[1] += dda.step[1];
                         if (ax2) dda.cell[2] += dda.step[2];
-                        if (dda.cell[0] < 0 || dda.cell[0] >= g.lx || dda.cell[1] < 0 || dda.cell[1] >= g.ly ||
-                            dda.cell[2] < 0 || dda.cell[2] >= g.lz) {
+                        ++n_cells;
+                        if (dda.cell[0] < 0 || dda.cell[0] >= g.mx || dda.cell[1] < 0 || dda.cell[1] >= g.my ||
+                            dda.cell[2] < 0 || dda.cell[2] >= g.mz) {
                             t = t1;
                             seg_end = true;
                             break;
@@ -245,10 +268,12 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                         if (ax1) dda.tnext[1] += dda.tdelta[1];
                         if (ax2) dda.tnext[2] += dda.tdelta[2];
                         texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
-                        maj = P.density_coeff *
-                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                        maj = P.density_coeff * cell_maj(maj_grid, g, dda);
                     }
-                    if (seg_end) st = shadow ? ST_NEE_DONE : ST_ESCAPE;
+                    if (seg_end)
+                        st = shadow ? ST_NEE_DONE : ST_ESCAPE;
+                    else if (!need_lookup)
+                        yield = true;  // let the warp's lookups run before crossing more cells
                 }
                 break;
             }
@@ -339,8 +364,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
                     if constexpr (kGridMajorant) {
                         dda_init(g, seg_eye, seg_dir, t, &dda);
                         texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
-                        maj = P.density_coeff *
-                              __ldg(g.cell_majorant + (static_cast<int64_t>(dda.cell[0]) * g.ly + dda.cell[1]) * g.lz + dda.cell[2]);
+                        maj = P.density_coeff * cell_maj(maj_grid, g, dda);
                     } else {
                         maj = global_maj;
                     }
@@ -479,12 +503,14 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
         n_lookups += __shfl_down_sync(0xffffffffu, n_lookups, o);
         n_vertices += __shfl_down_sync(0xffffffffu, n_vertices, o);
         n_samples += __shfl_down_sync(0xffffffffu, n_samples, o);
+        n_cells += __shfl_down_sync(0xffffffffu, n_cells, o);
     }
     err = __reduce_or_sync(0xffffffffu, err);
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(P.counters + 0, n_lookups);
         atomicAdd(P.counters + 1, n_vertices);
         atomicAdd(P.counters + 2, n_samples);
+        atomicAdd(P.counters + 3, n_cells);
         if (err) atomicOr(P.error_flags, err);
     }
 }
@@ -496,10 +522,30 @@ __global__ void finalize_mean_kernel(const double* __restrict__ sum, float* __re
         mean[i] = static_cast<float>(sum[i] * inv_samples);
 }
 
+// Majorant grid of 2^shift-voxel cells from the 8^3-voxel cells (max-pooling by 2^(shift-3)).
+__global__ void pool_majorants_kernel(const float* __restrict__ fine, int lx, int ly, int lz, float* __restrict__ out,
+                                      int mx, int my, int mz, int factor) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= mx * my * mz) return;
+    int cz = i % mz, cy = (i / mz) % my, cx = i / (mz * my);
+    float m = 0.0f;
+    for (int x = cx * factor; x < min((cx + 1) * factor, lx); ++x)
+        for (int y = cy * factor; y < min((cy + 1) * factor, ly); ++y)
+            for (int z = cz * factor; z < min((cz + 1) * factor, lz); ++z)
+                m = fmaxf(m, fine[(static_cast<int64_t>(x) * ly + y) * lz + z]);
+    out[i] = m;
+}
+
 }  // namespace
 
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s) {
     finalize_mean_kernel<<<(n_values + 255) / 256, 256, 0, s>>>(sum, mean, n_values, 1.0 / samples);
+}
+
+void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int mx, int my, int mz, int factor,
+                    cudaStream_t s) {
+    int n = mx * my * mz;
+    pool_majorants_kernel<<<(n + 255) / 256, 256, 0, s>>>(fine, lx, ly, lz, out, mx, my, mz, factor);
 }
 
 const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
@@ -509,16 +555,16 @@ const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
                          : reinterpret_cast<const void*>(plain_trace_kernel<false, false>);
 }
 
-void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, cudaStream_t s) {
+void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s) {
     dim3 grid(grid_ctas), block(threads);
     if (p.dlog) {
         if (grid_majorant)
-            plain_trace_kernel<true, true><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<true, true><<<grid, block, smem, s>>>(p);
         else
             plain_trace_kernel<false, true><<<grid, block, 0, s>>>(p);
     } else {
         if (grid_majorant)
-            plain_trace_kernel<true, false><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<true, false><<<grid, block, smem, s>>>(p);
         else
             plain_trace_kernel<false, false><<<grid, block, 0, s>>>(p);
     }

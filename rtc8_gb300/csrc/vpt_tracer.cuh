@@ -35,6 +35,8 @@ struct TraceParams {
     uint32_t spp;             // samples per pixel in this launch
     uint32_t accum_base;      // samples already accumulated (numAccumFrames of the first one)
     int32_t stream_mode;      // 0 = per-pixel sequential streams, 1 = sample-parallel streams
+    uint32_t stream_base;     // sample-parallel mode: index of the first sample of this launch
+    int32_t maj_in_smem;      // majorant grid staged in dynamic shared memory
 
     uint64_t* rng;            // per pixel
     double* sum_rgb;          // 3 per pixel
@@ -45,7 +47,12 @@ struct TraceParams {
     unsigned int* error_flags;
 };
 
-void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, cudaStream_t s);
+// Majorant grids up to this many cells are staged in shared memory (32 KB).
+constexpr int kMajSmemCells = 8192;
+
+void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
+void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int mx, int my, int mz, int factor,
+                    cudaStream_t s);
 
 }  // namespace vpt

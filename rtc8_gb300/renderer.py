@@ -153,9 +153,9 @@ class Renderer:
         return s / max(n, 1)
 
     def counters(self) -> dict:
-        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        check(self.lib.vpt_get_counters(self.ctx, C.byref(a), C.byref(b), C.byref(c)), "vpt_get_counters")
-        return {"lookups": a.value, "vertices": b.value, "samples": c.value}
+        a, b, c, d = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(self.lib.vpt_get_counters(self.ctx, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "vpt_get_counters")
+        return {"lookups": a.value, "vertices": b.value, "samples": c.value, "cell_steps": d.value}
 
     def reset_counters(self) -> None:
         check(self.lib.vpt_reset_counters(self.ctx), "vpt_reset_counters")
@@ -193,6 +193,7 @@ def frame_params(cfg: SceneConfig, env_enabled: bool = True) -> VptFrameParams:
     p.majorant_mode = cfg.majorant_mode
     p.max_steps_per_segment = cfg.max_steps_per_segment
     p.rng_stream_mode = cfg.rng_stream_mode
+    p.majorant_cell_log2 = cfg.majorant_cell_log2
     return p
 
 

@@ -71,10 +71,12 @@ def test_decision_parity_reference_mode(cuda_device, k):
     assert g["counters"]["samples"] == cfg.width * cfg.height * 4
 
 
-@pytest.mark.parametrize("g_param,mode,streams", [(0.8, 1, 1), (0.8, 0, 1), (-0.3, 1, 1), (0.8, 1, 0)])
-def test_decision_parity_config_mode(cuda_device, g_param, mode, streams):
-    """Both majorant modes and both RNG stream layouts against the oracle."""
-    cfg = small_config_mode(size=48, n=32, g=g_param, majorant_mode=mode).replace(rng_stream_mode=streams)
+@pytest.mark.parametrize("g_param,mode,streams,cell_log2",
+                         [(0.8, 1, 1, 3), (0.8, 0, 1, 3), (-0.3, 1, 1, 3), (0.8, 1, 0, 3), (0.8, 1, 1, 4)])
+def test_decision_parity_config_mode(cuda_device, g_param, mode, streams, cell_log2):
+    """Both majorant modes, both RNG stream layouts and two majorant-cell sizes against the oracle."""
+    cfg = small_config_mode(size=48, n=40, g=g_param, majorant_mode=mode).replace(rng_stream_mode=streams,
+                                                                                   majorant_cell_log2=cell_log2)
     g, o, same = _compare(cfg, spp=4)
     frac = same.mean()
     assert frac >= DECISION_PARITY, f"identical decisions {frac:.5f}"
@@ -113,10 +115,12 @@ def test_global_and_grid_majorants_agree_statistically(cuda_device):
         setup_scene(r, cfg)
         sq = np.zeros((cfg.height, cfg.width, 3))
         s = np.zeros((cfg.height, cfg.width, 3))
+        prev = np.zeros((cfg.height, cfg.width, 3))
         for _ in range(8):
-            r.reset_accumulation()
             r.launch_plain(spp // 8)
-            x = r.download_sum()[0] / (spp // 8)
+            cum = r.download_sum()[0]
+            x = (cum - prev) / (spp // 8)  # mean of this batch of samples
+            prev = cum
             s += x
             sq += x * x
         m = s / 8
