@@ -111,6 +111,7 @@ int vpt_destroy(VptContext* c) {
     dev_free(&c->d_leaf_values);
     dev_free(&c->d_cell_maj);
     dev_free(&c->d_maj);
+    dev_free(&c->d_jumps);
     dev_free(&c->d_dense);
     dev_free(&c->d_env);
     dev_free(&c->d_mips);
@@ -380,6 +381,46 @@ int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads) {
 }  // extern "C"
 
 namespace vpt {
+// LCG jump (multiplier, increment) of `delta` PCG32 draws (O(log delta) advance, Brown 1994).
+static void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus) {
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    *mult = acc_mult;
+    *plus = acc_plus;
+}
+
+// Jump table of a sample-parallel launch: entry i advances a pixel's seed state to the start
+// of sample (first + i), i.e. by (first + i) * 2^40 draws.
+int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaStream_t s) {
+    if (count > (1u << 20)) return set_error(VPT_ERR_INVALID_ARGUMENT, "at most 2^20 samples per pixel and launch");
+    if (c->jump_capacity < count) {
+        int rc = dev_alloc(&c->d_jumps, count);
+        if (rc) return rc;
+        c->jump_capacity = count;
+    }
+    std::vector<ulonglong2> table(count);
+    uint64_t a, b, a1, b1;
+    lcg_jump(static_cast<uint64_t>(first) << kSampleStreamShift, &a, &b);
+    lcg_jump(1ULL << kSampleStreamShift, &a1, &b1);
+    for (uint32_t i = 0; i < count; ++i) {
+        table[i] = make_ulonglong2(a, b);
+        b = a1 * b + b1;  // compose with one more 2^40-draw jump
+        a = a1 * a;
+    }
+    // Ordered on the launch's stream; a copy from pageable memory has consumed the host buffer
+    // when the call returns.
+    VPT_CUDA(cudaMemcpyAsync(c->d_jumps, table.data(), count * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+    return VPT_OK;
+}
+
 // Majorant grid of the DDA for the frame's cell size, max-pooled from the 8^3-voxel cells.
 static int ensure_majorant_grid(VptContextImpl* c) {
     int shift = c->frame.majorant_cell_log2 < 3 ? 3 : c->frame.majorant_cell_log2;
@@ -492,6 +533,11 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     uint64_t npix = static_cast<uint64_t>(c->width) * c->height;
     if (npix * spp >= (1ull << 31)) return set_error(VPT_ERR_INVALID_ARGUMENT, "too many samples in one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (tp.stream_mode == 1) {
+        int rc2 = vpt::upload_sample_jumps(c, c->stream_samples, spp, s);
+        if (rc2) return rc2;
+        tp.sample_jumps = c->d_jumps;
+    }
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     int threads = c->threads > 0 ? c->threads : 128;
     bool grid_maj = c->frame.majorant_mode == 1;

@@ -23,6 +23,8 @@ struct VptContextImpl {
     float* d_mean = nullptr;
     uint32_t accum_samples = 0;
     uint32_t stream_samples = 0;   // samples ever traced since seeding (sample-parallel streams)
+    ulonglong2* d_jumps = nullptr; // per-launch PCG jump table of the sample-parallel streams
+    uint32_t jump_capacity = 0;
 
     unsigned int* d_work = nullptr;
     unsigned long long* d_counters = nullptr;

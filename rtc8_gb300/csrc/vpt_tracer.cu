@@ -135,21 +135,30 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
         while (!need_lookup && !yield && st != ST_DONE) {
             switch (st) {
             case ST_FETCH: {
+                // Warp-aggregated fetch: one atomic for all lanes of the warp that need work now.
+                const uint32_t need = __activemask();
+                const int leader = __ffs(need) - 1;
+                const uint32_t lane = threadIdx.x & 31;
+                uint32_t base = 0;
+                if (static_cast<int>(lane) == leader) base = atomicAdd(P.work_counter, __popc(need));
+                base = __shfl_sync(need, base, leader);
+                const uint32_t item = base + __popc(need & ((1u << lane) - 1u));
                 if (P.stream_mode == 1) {
                     // One (pixel, sample) per work item, samples of all pixels interleaved.
-                    uint32_t item = atomicAdd(P.work_counter, 1u);
                     if (item >= num_pixels * P.spp) {
                         st = ST_DONE;
                         break;
                     }
                     pixel = item % num_pixels;
                     sample = item / num_pixels;
-                    rng.state = pcg_advance(P.rng[pixel], static_cast<uint64_t>(P.stream_base + sample)
-                                                              << kSampleStreamShift);
+                    // Sample (stream_base + sample) starts (stream_base + sample) * 2^40 draws into
+                    // the pixel's stream: state = A * seed + C with the launch's jump table.
+                    const ulonglong2 jump = P.sample_jumps[sample];
+                    rng.state = jump.x * P.rng[pixel] + jump.y;
                     st = ST_CAMERA;
                     break;
                 }
-                pixel = atomicAdd(P.work_counter, 1u);
+                pixel = item;
                 if (pixel >= num_pixels) {
                     st = ST_DONE;
                     break;

@@ -36,6 +36,7 @@ struct TraceParams {
     uint32_t accum_base;      // samples already accumulated (numAccumFrames of the first one)
     int32_t stream_mode;      // 0 = per-pixel sequential streams, 1 = sample-parallel streams
     uint32_t stream_base;     // sample-parallel mode: index of the first sample of this launch
+    const ulonglong2* sample_jumps;  // sample-parallel mode: LCG jump (A, C) of sample stream_base + i
     int32_t maj_in_smem;      // majorant grid staged in dynamic shared memory
 
     uint64_t* rng;            // per pixel
