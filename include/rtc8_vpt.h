@@ -169,8 +169,10 @@ int vpt_reset_counters(VptContext* ctx);
 uint32_t vpt_get_device_errors(VptContext* ctx);
 int vpt_synchronize(VptContext* ctx, void* stream);
 
-/* Launch shape of the persistent tracker (CTAs per SM, threads per CTA); 0 = defaults. */
-int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta);
+/* Launch shape of the persistent tracker (CTAs per SM, threads per CTA) and the number of
+ * parked lanes of a warp that triggers its joint event phase; 0 = defaults. */
+int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,
+                         int32_t park_threshold);
 
 #ifdef __cplusplus
 }

@@ -80,7 +80,7 @@ _VPT = {
     "vpt_reset_counters": (C.c_int, [C.c_void_p]),
     "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
     "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
-    "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
 }
 
 EXPORTS: dict[str, tuple] = dict(_VPT)

@@ -370,11 +370,13 @@ int vpt_set_frame_params(VptContext* c, const VptFrameParams* p) {
     return VPT_OK;
 }
 
-int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads) {
-    if (!c || ctas_per_sm < 0 || threads < 0 || (threads && (threads % 32 || threads > 128)))
+int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads, int32_t park_threshold) {
+    if (!c || ctas_per_sm < 0 || threads < 0 || (threads && (threads % 32 || threads > 128)) || park_threshold < 0 ||
+        park_threshold > 32)
         return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_set_launch_shape: bad arguments");
     c->ctas_per_sm = ctas_per_sm;
     c->threads = threads;
+    c->park_threshold = park_threshold;
     return VPT_OK;
 }
 
@@ -530,6 +532,7 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     tp.dlog = dlog;
     tp.stream_mode = c->frame.rng_stream_mode;
     tp.stream_base = c->stream_samples;
+    tp.park_threshold = c->park_threshold;
     uint64_t npix = static_cast<uint64_t>(c->width) * c->height;
     if (npix * spp >= (1ull << 31)) return set_error(VPT_ERR_INVALID_ARGUMENT, "too many samples in one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -15,7 +15,7 @@ struct NrcBuffers;
 struct VptContextImpl {
     int32_t width = 0, height = 0;
     int device = 0, num_sms = 0;
-    int32_t ctas_per_sm = 0, threads = 0;
+    int32_t ctas_per_sm = 0, threads = 0, park_threshold = 0;
 
     // per pixel (renderer_main.cpp:80-129)
     uint64_t* d_rng = nullptr;

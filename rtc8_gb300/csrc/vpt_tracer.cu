@@ -35,8 +35,10 @@ enum : uint32_t { END_ESCAPE = 1, END_RR = 2, END_PDF_ZERO = 3, END_MAX_BOUNCES 
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
-// Majorant-grid cells a lane may cross in one divergent pass before yielding to the warp.
-constexpr int kCellStepsPerPass = 4;
+// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp.
+constexpr int kCellStepsPerPass = 1;
+// Parked lanes of a warp that trigger a joint event phase.
+constexpr int kParkThreshold = 12;
 
 struct DdaState {
     int cell[3];
@@ -80,7 +82,7 @@ __device__ __forceinline__ float cell_maj(const float* maj, const Grid& g, const
 }
 
 template <bool kGridMajorant, bool kLog>
-__global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
+__global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P) {
     extern __shared__ float s_maj[];
     const Grid& g = P.grid;
     const float* maj_grid = g.maj;
@@ -95,6 +97,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
     const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
     const float global_maj = P.density_coeff * g.global_majorant;
     const uint32_t step_cap = P.max_steps > 0 ? static_cast<uint32_t>(P.max_steps) : kHardStepCap;
+    const int park_threshold = P.park_threshold > 0 ? P.park_threshold : kParkThreshold;
     const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
     const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
 
@@ -129,10 +132,18 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
     LeafCache leaf_cache;
 
     while (true) {
-        // ---------------------------------------------------------------- divergent part
+        // Warp-level event batching: lanes whose path reached an event (segment end, collision,
+        // new sample) park until at least kParkThreshold lanes of the warp are parked, or no lane
+        // is tracking any more; then all parked lanes run their event logic together. In between,
+        // the tracking lanes advance one step per iteration (a density lookup or one DDA cell).
+        const bool tracking = st == ST_STEP;
+        const uint32_t ev_mask = __ballot_sync(0xffffffffu, !tracking && st != ST_DONE);
+        const uint32_t tr_mask = __ballot_sync(0xffffffffu, tracking);
+        if ((ev_mask | tr_mask) == 0) break;
+        const bool event_phase = ev_mask != 0 && (tr_mask == 0 || __popc(ev_mask) >= park_threshold);
         bool need_lookup = false, yield = false;
         V3 lookup_pos = v3(0, 0, 0);
-        while (!need_lookup && !yield && st != ST_DONE) {
+        while (!need_lookup && !yield && st != ST_DONE && (event_phase ? st != ST_STEP : st == ST_STEP)) {
             switch (st) {
             case ST_FETCH: {
                 // Warp-aggregated fetch: one atomic for all lanes of the warp that need work now.
@@ -479,10 +490,7 @@ __global__ void __launch_bounds__(128) plain_trace_kernel(const TraceParams P) {
             }
         }
 
-        if (!__any_sync(0xffffffffu, need_lookup)) {
-            if (__all_sync(0xffffffffu, st == ST_DONE)) break;
-            continue;
-        }
+        if (event_phase || !__any_sync(0xffffffffu, need_lookup)) continue;
 
         // ---------------------------------------------------------------- converged lookups
         float density = 0.0f;

@@ -38,6 +38,7 @@ struct TraceParams {
     uint32_t stream_base;     // sample-parallel mode: index of the first sample of this launch
     const ulonglong2* sample_jumps;  // sample-parallel mode: LCG jump (A, C) of sample stream_base + i
     int32_t maj_in_smem;      // majorant grid staged in dynamic shared memory
+    int32_t park_threshold;   // parked lanes that trigger a warp's event phase (0 = default)
 
     uint64_t* rng;            // per pixel
     double* sum_rgb;          // 3 per pixel

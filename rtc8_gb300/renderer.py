@@ -121,8 +121,8 @@ class Renderer:
         self.params = p
         check(self.lib.vpt_set_frame_params(self.ctx, C.byref(p)), "vpt_set_frame_params")
 
-    def set_launch_shape(self, ctas_per_sm: int = 0, threads: int = 0) -> None:
-        check(self.lib.vpt_set_launch_shape(self.ctx, ctas_per_sm, threads), "vpt_set_launch_shape")
+    def set_launch_shape(self, ctas_per_sm: int = 0, threads: int = 0, park_threshold: int = 0) -> None:
+        check(self.lib.vpt_set_launch_shape(self.ctx, ctas_per_sm, threads, park_threshold), "vpt_set_launch_shape")
 
     def launch_plain(self, spp: int, stream: int | None = None) -> None:
         check(self.lib.vpt_launch_plain(self.ctx, C.c_void_p(stream or 0), spp), "vpt_launch_plain")
