@@ -153,6 +153,44 @@ int vpt_launch_plain(VptContext* ctx, void* stream, uint32_t spp);
  * path vertices, primary lookups, shadow lookups, end code) to a device buffer of
  * width*height*spp*4 u32, sample s of pixel p at (p*spp + s). */
 int vpt_launch_plain_logged(VptContext* ctx, void* stream, uint32_t spp, uint32_t* dev_log);
+
+/* Allocation-free launch of the plain tracer. It has no counterpart in the reference: it is for
+ * callers that cannot call cudaMalloc (a host renderer whose device memory belongs to its own
+ * pool allocator, or code running where allocating is not allowed), so it needs no VptContext.
+ * The caller passes every input (grid, majorant grid, environment, importance mip chain, per
+ * pixel PCG32 seed states) and output (FP64 sums, FP32 mean) as device pointers, in the layouts
+ * the context uses. The launch's scratch memory (work counter, counters, error word and the
+ * table of RNG jump constants, 65,792 bytes) is a file-scope __device__ array that every GPU
+ * loading the library holds until exit; it is cleared at the start of each call. Limits: spp per
+ * call <= VPT_NOALLOC_MAX_SPP (larger requests fail with VPT_ERR_INVALID_ARGUMENT). All calls
+ * share the one array, so calls that overlap on the GPU race. The first call with a device
+ * current looks the array's address up (cudaGetSymbolAddress): make it before any stream
+ * capture. Work counters and device error bits of these launches are not reported. */
+#define VPT_NOALLOC_MAX_SPP 4096u
+typedef struct VptNoAllocTrace {
+    VptFrameParams frame;
+    int32_t width, height;
+    uint32_t spp;
+    uint32_t accum_base;        /* samples already in sum/mean (numAccumFrames of the first) */
+    uint32_t stream_base;       /* sample-parallel streams: index of the first sample */
+    const int32_t* leaf_table;  /* ceil(n/8)^3 slots, -1 = empty leaf */
+    const float* leaf_values;   /* 512 values per slot, order x<<6 | y<<3 | z */
+    const float* majorants;     /* mx*my*mz cells of 2^frame.majorant_cell_log2 voxels */
+    int32_t nx, ny, nz;
+    int32_t mx, my, mz;
+    float voxel_size;
+    float origin[3];
+    float global_majorant;
+    const float* env_texels;    /* env_w * env_h float4 (RGB + unused) */
+    int32_t env_w, env_h;
+    const float* imp_mips;      /* importance mip chain, levels back to back */
+    int32_t map_w, map_h, num_mips;
+    float imp_integral;
+    uint64_t* rng;              /* width*height seed states */
+    double* sum_rgb;            /* 3 per pixel */
+    float* mean_rgb;            /* 3 per pixel */
+} VptNoAllocTrace;
+int vpt_launch_plain_noalloc(const VptNoAllocTrace* args, void* stream);
 int vpt_reset_accumulation(VptContext* ctx);
 
 /* Reads back the accumulation: FP64 per-pixel RGB sums and sample count, FP32 running mean. */

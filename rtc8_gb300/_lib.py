@@ -47,6 +47,24 @@ class VptFrameParams(C.Structure):
     ]
 
 
+class VptNoAllocTrace(C.Structure):
+    """Mirror of ``VptNoAllocTrace`` (include/rtc8_vpt.h): arguments of the allocation-free launch."""
+
+    _fields_ = [
+        ("frame", VptFrameParams),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("spp", C.c_uint32), ("accum_base", C.c_uint32), ("stream_base", C.c_uint32),
+        ("leaf_table", C.c_void_p), ("leaf_values", C.c_void_p), ("majorants", C.c_void_p),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("mx", C.c_int32), ("my", C.c_int32), ("mz", C.c_int32),
+        ("voxel_size", C.c_float), ("origin", C.c_float * 3), ("global_majorant", C.c_float),
+        ("env_texels", C.c_void_p), ("env_w", C.c_int32), ("env_h", C.c_int32),
+        ("imp_mips", C.c_void_p), ("map_w", C.c_int32), ("map_h", C.c_int32), ("num_mips", C.c_int32),
+        ("imp_integral", C.c_float),
+        ("rng", C.c_void_p), ("sum_rgb", C.c_void_p), ("mean_rgb", C.c_void_p),
+    ]
+
+
 # name -> (restype, argtypes)
 _VPT = {
     "vpt_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -72,6 +90,7 @@ _VPT = {
     "vpt_set_frame_params": (C.c_int, [C.c_void_p, C.POINTER(VptFrameParams)]),
     "vpt_launch_plain": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vpt_launch_plain_logged": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vpt_launch_plain_noalloc": (C.c_int, [C.POINTER(VptNoAllocTrace), C.c_void_p]),
     "vpt_reset_accumulation": (C.c_int, [C.c_void_p]),
     "vpt_download_sum": (C.c_int, [C.c_void_p, c_double_p, c_u32_p]),
     "vpt_download_mean": (C.c_int, [C.c_void_p, c_float_p]),
