@@ -50,9 +50,10 @@ void encode(int encoding, const float* q, float* out) {
     } else {
         for (int a = 0; a < 3; ++a)
             for (int f = 0; f < 12; ++f) {
-                float arg = q[a] * static_cast<float>(1 << f) * 3.14159265f;
-                out[k++] = std::sin(arg);
-                out[k++] = std::cos(arg);
+                // sin / cos of pi * (x * 2^f), with the product x * 2^f exact in float
+                double arg = kPi * static_cast<double>(q[a] * static_cast<float>(1 << f));
+                out[k++] = static_cast<float>(std::sin(arg));
+                out[k++] = static_cast<float>(std::cos(arg));
             }
         const float scale[2] = {1.0f / 3.14159265f, 1.0f / 6.28318531f};
         for (int a = 0; a < 2; ++a) {

@@ -233,3 +233,60 @@ def render_plain(sc: OracleScene, rng: np.ndarray, spp: int, accum_base: int = 0
     n = lib().orc_render_plain(sc.ref, p(rng, C.c_uint64), accum_base, spp, p(sum_rgb, C.c_double),
                                p(mean_rgb, C.c_float), p(dlog, C.c_uint32) if log else None, r0, r1, threads)
     return {"sum": sum_rgb, "mean": mean_rgb, "log": dlog, "lookups": int(n)}
+
+
+# ------------------------------------------------------------------------------ radiance cache
+_NRC_FUNCS = {
+    "orc_nrc_in_dim": (C.c_int, [C.c_int]),
+    "orc_nrc_num_params": (C.c_int64, [C.c_int, C.c_int]),
+    "orc_nrc_encode": (None, [C.c_int, f32p, C.c_int, f32p]),
+    "orc_nrc_forward": (None, [C.c_int, C.c_int, C.c_int, f32p, f32p, C.c_int, f32p]),
+    "orc_nrc_loss_grad": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_float, f32p, f32p, f32p, C.c_int, f32p]),
+    "orc_adam": (None, [f32p, f32p, f32p, f32p, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                        C.c_int]),
+}
+
+
+def nrc_lib():
+    L = lib()
+    for name, (res, args) in _NRC_FUNCS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def nrc_encode(encoding: int, queries: np.ndarray) -> np.ndarray:
+    q = np.ascontiguousarray(queries, np.float32)
+    n = len(q)
+    d = nrc_lib().orc_nrc_in_dim(encoding)
+    out = np.zeros((n, d), np.float32)
+    nrc_lib().orc_nrc_encode(encoding, p(q, C.c_float), n, p(out, C.c_float))
+    return out
+
+
+def nrc_forward(encoding: int, hidden: int, out_act: int, params: np.ndarray, queries: np.ndarray) -> np.ndarray:
+    w = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    out = np.zeros((len(q), 3), np.float32)
+    nrc_lib().orc_nrc_forward(encoding, hidden, out_act, p(w, C.c_float), p(q, C.c_float), len(q), p(out, C.c_float))
+    return out
+
+
+def nrc_loss_grad(encoding: int, hidden: int, out_act: int, loss_scale: float, params: np.ndarray,
+                  queries: np.ndarray, targets: np.ndarray):
+    w = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    t = np.ascontiguousarray(targets, np.float32)
+    g = np.zeros_like(w)
+    loss = nrc_lib().orc_nrc_loss_grad(encoding, hidden, out_act, loss_scale, p(w, C.c_float), p(q, C.c_float),
+                                       p(t, C.c_float), len(q), p(g, C.c_float))
+    return float(loss), g
+
+
+def adam(w, m, v, grad, lr, beta1, beta2, eps, l2, step):
+    w, m, v = (np.ascontiguousarray(a, np.float32).copy() for a in (w, m, v))
+    g = np.ascontiguousarray(grad, np.float32)
+    nrc_lib().orc_adam(p(w, C.c_float), p(m, C.c_float), p(v, C.c_float), p(g, C.c_float), len(w), lr, beta1, beta2,
+                       eps, l2, step)
+    return w, m, v

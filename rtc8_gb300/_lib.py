@@ -102,7 +102,36 @@ _VPT = {
     "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
 }
 
+class NrcConfig(C.Structure):
+    _fields_ = [
+        ("encoding", C.c_int32), ("num_hidden_layers", C.c_int32), ("output_activation", C.c_int32),
+        ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+        ("l2_reg", C.c_float), ("ema_decay", C.c_float), ("loss_scale", C.c_float), ("seed", C.c_uint32),
+    ]
+
+
+_NRC = {
+    "nrc_default_config": (None, [C.c_int32, C.POINTER(NrcConfig)]),
+    "nrc_create": (C.c_int, [C.POINTER(NrcConfig), C.POINTER(C.c_void_p)]),
+    "nrc_destroy": (C.c_int, [C.c_void_p]),
+    "nrc_last_error": (C.c_char_p, []),
+    "nrc_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "nrc_infer_device_count": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "nrc_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, c_float_p]),
+    "nrc_get_layout": (C.c_int, [C.c_void_p, c_i32_p, c_i32_p, c_i32_p, c_i64_p]),
+    "nrc_get_params": (C.c_int, [C.c_void_p, c_float_p]),
+    "nrc_set_params": (C.c_int, [C.c_void_p, c_float_p]),
+    "nrc_get_gradients": (C.c_int, [C.c_void_p, c_float_p]),
+    "nrc_encode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "nrc_step_count": (C.c_uint64, [C.c_void_p]),
+    "nrc_device_errors": (C.c_uint32, [C.c_void_p]),
+    "nrc_selftest_mma": (C.c_int, [c_float_p, c_float_p, C.c_int32, C.c_int32, c_float_p]),
+}
+
+
+
 EXPORTS: dict[str, tuple] = dict(_VPT)
+EXPORTS.update(_NRC)
 
 _lib: C.CDLL | None = None
 

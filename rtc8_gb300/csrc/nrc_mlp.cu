@@ -1,0 +1,911 @@
+// Neural radiance cache: a fully fused FP16 MLP (64-wide hidden layers, ReLU, no biases) on the
+// Blackwell tensor cores. Replaces tiny-cuda-nn's FullyFusedMLP + encodings + Trainer
+// (renderer/network_interface.cu:50-192).
+//
+// One CTA of 128 threads works on 128-row tiles (one thread per row): the encoded input tile
+// and every hidden activation tile are FP16 in shared memory (core-matrix layout, nrc_tc.cuh),
+// the weights are copied once per CTA into shared memory in the same layout, and each layer is
+// one chain of tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) into an FP32 TMEM
+// accumulator, read back with tcgen05.ld for the ReLU / FP16 epilogue. Training keeps all
+// activations of a tile on chip; the backward pass reads activations and weights transposed
+// through MN-major descriptors (no transposed copies) and reduces weight gradients with FP32
+// vector atomics. Adam (with L2 regularisation) and an optional EMA of the weights run in one
+// elementwise kernel that also repacks the FP16 weight images.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/rtc8_nrc.h"
+#include "nrc_tc.cuh"
+
+namespace nrc {
+namespace {
+
+thread_local std::string g_err;
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+#define NRC_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(NRC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kTile = 128;
+constexpr int kWidth = 64;
+constexpr int kOutPad = 16;
+constexpr int kMaxMats = 8;
+constexpr float kPiF = 3.14159265358979323846f;
+
+// Network shape: matrix j maps in[j] -> out[j] features; matrix 0 reads the encoded input.
+struct NetLayout {
+    int enc;
+    int in_dim;
+    int in_real;           // encoded features before padding
+    int L;                 // number of weight matrices (hidden layers + 1)
+    int in[kMaxMats], out[kMaxMats];
+    int poff[kMaxMats];    // FP32 parameter offset of matrix j
+    uint32_t boff[kMaxMats];  // byte offset of matrix j in the FP16 weight image
+    int nparams;
+    uint32_t blob_bytes;
+    int out_act;
+    float loss_scale;
+};
+
+NetLayout make_layout(int enc, int hidden, int out_act, float loss_scale) {
+    NetLayout l{};
+    l.enc = enc;
+    l.in_dim = enc == NRC_ENCODING_REFERENCE ? 64 : 144;
+    l.in_real = enc == NRC_ENCODING_REFERENCE ? 62 : 138;
+    l.L = hidden + 1;
+    int po = 0;
+    uint32_t bo = 0;
+    for (int j = 0; j < l.L; ++j) {
+        l.in[j] = j == 0 ? l.in_dim : kWidth;
+        l.out[j] = j == l.L - 1 ? kOutPad : kWidth;
+        l.poff[j] = po;
+        l.boff[j] = bo;
+        po += l.in[j] * l.out[j];
+        bo += static_cast<uint32_t>(l.in[j] * l.out[j] * 2);
+    }
+    l.nparams = po;
+    l.blob_bytes = bo;
+    l.out_act = out_act;
+    l.loss_scale = loss_scale;
+    return l;
+}
+
+// ------------------------------------------------------------------------------ encodings
+// Writes the FP16 encoded input of one query into row `r` of a [128][in_dim] core-matrix tile.
+// Features are produced 8 at a time (one 16-byte store per core-matrix row).
+struct RowWriter {
+    uint8_t* base;
+    int r, K;
+    float buf[8];
+    int n = 0, chunk = 0;
+    __device__ __forceinline__ void push(float v) {
+        buf[n++] = v;
+        if (n == 8) flush();
+    }
+    __device__ __forceinline__ void flush() {
+        uint4 w;
+        w.x = pack_half2(buf[0], buf[1]);
+        w.y = pack_half2(buf[2], buf[3]);
+        w.z = pack_half2(buf[4], buf[5]);
+        w.w = pack_half2(buf[6], buf[7]);
+        *reinterpret_cast<uint4*>(base + cm_offset(r, chunk * 8, K)) = w;
+        ++chunk;
+        n = 0;
+    }
+    __device__ __forceinline__ void pad_to(int K_) {
+        while (chunk * 8 + n < K_) push(0.0f);
+    }
+};
+
+__device__ __forceinline__ float one_blob(float x, int b, int nbins) {
+    float z = (x - (b + 0.5f) / nbins) * nbins;
+    return __expf(-0.5f * z * z);
+}
+
+// NRC_ENCODING_REFERENCE: TriangleWave(12) x 3, OneBlob(4) x 5 (angles / pi, / 2pi), identity x 6.
+// NRC_ENCODING_VOLUME: sin/cos(pi 2^f x) x 12 x 3, OneBlob(32) on vOut theta / pi and phi / 2pi,
+// identity on the local density (roughness slot) and the albedo (diffuse.r).
+__device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* tile, int r, int K) {
+    RowWriter w{tile, r, K};
+    if (enc == NRC_ENCODING_REFERENCE) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int f = 0; f < 12; ++f) {
+                float v = q[a] * static_cast<float>(1 << f);
+                float fr = v - floorf(v);
+                w.push(2.0f * fabsf(fr - 0.5f));
+            }
+        const float scale[5] = {1.0f / 3.14159265f, 1.0f / 6.28318531f, 1.0f / 3.14159265f, 1.0f / 6.28318531f, 1.0f};
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            float x = q[3 + a] * scale[a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) w.push(one_blob(x, b, 4));
+        }
+#pragma unroll
+        for (int a = 0; a < 6; ++a) w.push(q[8 + a]);
+        w.pad_to(64);
+    } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int f = 0; f < 12; ++f) {
+                float s, c;
+                sincospif(q[a] * static_cast<float>(1 << f), &s, &c);
+                w.push(s);
+                w.push(c);
+            }
+        const float scale[2] = {1.0f / 3.14159265f, 1.0f / 6.28318531f};
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            float x = q[5 + a] * scale[a];
+#pragma unroll
+            for (int b = 0; b < 32; ++b) w.push(one_blob(x, b, 32));
+        }
+        w.push(q[7]);
+        w.push(q[8]);
+        w.pad_to(144);
+    }
+}
+
+__device__ __forceinline__ void load_query(const float* __restrict__ in, uint32_t row, uint32_t n, float* q) {
+    if (row < n) {
+        const float2* p = reinterpret_cast<const float2*>(in + static_cast<size_t>(row) * 14);
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            float2 v = __ldg(p + i);
+            q[2 * i] = v.x;
+            q[2 * i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 14; ++i) q[i] = 0.0f;
+    }
+}
+
+// ------------------------------------------------------------------------------ MMA helpers
+// D (128 x N, TMEM) = A (128 x K, smem, K-major) * W^T where W is N x K (K-major).
+__device__ __forceinline__ void issue_layer(uint32_t tmem_d, uint32_t a_addr, uint32_t w_addr, int K, int N) {
+    const uint32_t idesc = idesc_f16(kTile, N, 0, 0);
+    for (int ks = 0; ks < K / 16; ++ks) {
+        uint64_t ad = smem_desc(a_addr + ks * 256, 128, static_cast<uint32_t>(K * 16));
+        uint64_t bd = smem_desc(w_addr + ks * 256, 128, static_cast<uint32_t>(K * 16));
+        mma_f16(tmem_d, ad, bd, idesc, ks > 0 ? 1u : 0u);
+    }
+}
+
+// Writes 16 FP32 values (columns c0..c0+15 of row r) as FP16 into a [128][K] core-matrix tile.
+__device__ __forceinline__ void store_row16(uint8_t* tile, int r, int c0, int K, const float (&v)[16]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        uint4 w;
+        w.x = pack_half2(v[8 * h + 0], v[8 * h + 1]);
+        w.y = pack_half2(v[8 * h + 2], v[8 * h + 3]);
+        w.z = pack_half2(v[8 * h + 4], v[8 * h + 5]);
+        w.w = pack_half2(v[8 * h + 6], v[8 * h + 7]);
+        *reinterpret_cast<uint4*>(tile + cm_offset(r, c0 + 8 * h, K)) = w;
+    }
+}
+// Reads 16 FP16 values (columns c0..c0+15 of row r) of a core-matrix tile.
+__device__ __forceinline__ void load_row16(const uint8_t* tile, int r, int c0, int K, float (&v)[16]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        uint4 w = *reinterpret_cast<const uint4*>(tile + cm_offset(r, c0 + 8 * h, K));
+        const __half2* p = reinterpret_cast<const __half2*>(&w);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float2 f = __half22float2(p[i]);
+            v[8 * h + 2 * i] = f.x;
+            v[8 * h + 2 * i + 1] = f.y;
+        }
+    }
+}
+
+constexpr uint32_t kErrTimeout = 1u;
+
+__host__ __device__ __forceinline__ uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
+
+// ------------------------------------------------------------------------------ inference
+template <int IN>
+__global__ void __launch_bounds__(kTile) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+                                                          const float* __restrict__ in, const uint32_t* __restrict__ dev_n,
+                                                          uint32_t n_max, float* __restrict__ out,
+                                                          unsigned int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    uint8_t* s_w = smem;
+    uint8_t* s_a0 = smem + align_up(ly.blob_bytes, 1024);
+    uint8_t* s_h = s_a0 + kTile * IN * 2;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_h + kTile * kWidth * 2);
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_bar + 1);
+
+    for (uint32_t i = tid; i < ly.blob_bytes / 16; i += kTile)
+        reinterpret_cast<uint4*>(s_w)[i] = __ldg(reinterpret_cast<const uint4*>(blob) + i);
+    if (warp == 0) tmem_alloc(s_slot, 64);
+    if (tid == 0) {
+        mbar_init(s_bar, 1);
+        mbar_fence_init();
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_slot;
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const uint32_t n = dev_n ? min(*dev_n, n_max) : n_max;
+    const uint32_t ntiles = (n + kTile - 1) / kTile;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const uint32_t row = tile * kTile + tid;
+        float q[14];
+        load_query(in, row, n, q);
+        encode_row(ly.enc, q, s_a0, tid, IN);
+        fence_async_smem();
+        __syncthreads();
+        for (int j = 0; j < ly.L && ok; ++j) {
+            if (tid == 0) {
+                tc_fence_after();
+                issue_layer(tmem, smem_u32(j == 0 ? s_a0 : s_h), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
+                mma_commit(s_bar);
+            }
+            ok = __syncthreads_and(mbar_wait(s_bar, phase));  // block-uniform decision
+            phase ^= 1;
+            tc_fence_after();
+            if (!ok) break;
+            if (j < ly.L - 1) {
+#pragma unroll
+                for (int c = 0; c < kWidth / 16; ++c) {
+                    float v[16];
+                    tmem_ld16(tmem + lane_base + c * 16, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
+                    store_row16(s_h, tid, c * 16, kWidth, v);
+                }
+                tc_fence_before();
+                fence_async_smem();
+                __syncthreads();
+            } else {
+                float v[16];
+                tmem_ld16(tmem + lane_base, v);
+                tmem_wait_ld();
+                if (row < n) {
+                    float* o = out + static_cast<size_t>(row) * 3;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) o[c] = ly.out_act == NRC_OUTPUT_EXP ? __expf(v[c]) : v[c];
+                }
+                tc_fence_before();
+                __syncthreads();
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicOr(err, kErrTimeout);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// ------------------------------------------------------------------------------ training
+// One CTA per 128-sample tile: forward keeping all activations, relative-L2-luminance loss
+// gradient (denominator held constant), backward with weight gradients reduced into `grad`
+// (scaled by loss_scale) and the batch loss added to `loss`.
+template <int IN>
+__global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+                                                          const float* __restrict__ in, const float* __restrict__ target,
+                                                          uint32_t n, float* __restrict__ grad, float* __restrict__ loss,
+                                                          unsigned int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int L = ly.L;
+    uint8_t* s_w = smem;
+    uint8_t* s_act0 = smem + align_up(ly.blob_bytes, 1024);
+    uint8_t* s_acts = s_act0 + kTile * IN * 2;             // act_1 .. act_{L-1}, 16 KB each
+    uint8_t* s_dza = s_acts + (L - 1) * kTile * kWidth * 2;
+    uint8_t* s_dzb = s_dza + kTile * kWidth * 2;
+    uint8_t* s_dzo = s_dzb + kTile * kWidth * 2;            // output gradient tile, 128 x 16
+    uint8_t* s_slack = s_dzo + kTile * kOutPad * 2;         // absorbs MN-major over-reads
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_slack + 2048);
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_bar + 1);
+    auto act = [&](int j) -> uint8_t* { return j == 0 ? s_act0 : s_acts + (j - 1) * kTile * kWidth * 2; };
+
+    for (uint32_t i = tid; i < ly.blob_bytes / 16; i += kTile)
+        reinterpret_cast<uint4*>(s_w)[i] = __ldg(reinterpret_cast<const uint4*>(blob) + i);
+    for (uint32_t i = tid; i < 2048 / 16; i += kTile) reinterpret_cast<uint4*>(s_slack)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) tmem_alloc(s_slot, 256);
+    if (tid == 0) {
+        mbar_init(s_bar, 1);
+        mbar_fence_init();
+    }
+    const uint32_t row = blockIdx.x * kTile + tid;
+    float q[14];
+    load_query(in, row, n, q);
+    encode_row(ly.enc, q, s_act0, tid, IN);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_slot;
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    // ---- forward
+    for (int j = 0; j < L && ok; ++j) {
+        if (tid == 0) {
+            tc_fence_after();
+            issue_layer(tmem, smem_u32(act(j)), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
+            mma_commit(s_bar);
+        }
+        ok = __syncthreads_and(mbar_wait(s_bar, phase));  // block-uniform decision
+        phase ^= 1;
+        tc_fence_after();
+        if (!ok) break;
+        if (j < L - 1) {
+#pragma unroll
+            for (int c = 0; c < kWidth / 16; ++c) {
+                float v[16];
+                tmem_ld16(tmem + lane_base + c * 16, v);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
+                store_row16(act(j + 1), tid, c * 16, kWidth, v);
+            }
+        } else {
+            // output, loss and its gradient (rows beyond n contribute nothing)
+            float v[16];
+            tmem_ld16(tmem + lane_base, v);
+            tmem_wait_ld();
+            float g[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) g[i] = 0.0f;
+            float l = 0.0f;
+            if (row < n) {
+                float y[3], t[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    y[c] = ly.out_act == NRC_OUTPUT_EXP ? __expf(v[c]) : v[c];
+                    t[c] = __ldg(target + static_cast<size_t>(row) * 3 + c);
+                }
+                float lum = 0.2126f * y[0] + 0.7152f * y[1] + 0.0722f * y[2];
+                float denom = lum * lum + 0.01f;
+                float inv = 1.0f / (3.0f * static_cast<float>(n));
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float d = y[c] - t[c];
+                    l += d * d / denom * inv;
+                    float gy = 2.0f * d / denom * inv;
+                    float gz = ly.out_act == NRC_OUTPUT_EXP ? gy * y[c] : gy;
+                    g[c] = gz * ly.loss_scale;
+                }
+            }
+            store_row16(s_dzo, tid, 0, kOutPad, g);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+            if ((tid & 31) == 0) atomicAdd(loss, l);
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+    }
+
+    // ---- backward: for matrix j, dW_j = dPre_{j+1}^T act_j and dPre_j = (dPre_{j+1} W_j) * relu'(act_j)
+    uint8_t* dz = s_dzo;
+    uint8_t* dz_next = s_dza;
+    const uint32_t tm_dx = tmem;        // columns [0, 64)
+    const uint32_t tm_dw = tmem + 64;   // columns [64, 64 + in_j)
+    for (int j = L - 1; j >= 0 && ok; --j) {
+        const int K_out = ly.out[j], N_in = ly.in[j];
+        if (tid == 0) {
+            tc_fence_after();
+            // weight gradient: M = 128 (output features, rows beyond out_j unused), N = in_j, K = 128 samples
+            const uint32_t idw = idesc_f16(kTile, N_in, 1, 1);
+            for (int ks = 0; ks < kTile / 16; ++ks) {
+                uint64_t ad = smem_desc(smem_u32(dz) + ks * 2 * (K_out * 16), static_cast<uint32_t>(K_out * 16), 128);
+                uint64_t bd = smem_desc(smem_u32(act(j)) + ks * 2 * (N_in * 16), static_cast<uint32_t>(N_in * 16), 128);
+                mma_f16(tm_dw, ad, bd, idw, ks > 0 ? 1u : 0u);
+            }
+            if (j > 0) {
+                // input gradient: M = 128 samples, N = in_j, K = out_j; W_j read MN-major
+                const uint32_t idx = idesc_f16(kTile, N_in, 0, 1);
+                for (int ks = 0; ks < K_out / 16; ++ks) {
+                    uint64_t ad = smem_desc(smem_u32(dz) + ks * 256, 128, static_cast<uint32_t>(K_out * 16));
+                    uint64_t bd = smem_desc(smem_u32(s_w + ly.boff[j]) + ks * 2 * (N_in * 16),
+                                            static_cast<uint32_t>(N_in * 16), 128);
+                    mma_f16(tm_dx, ad, bd, idx, ks > 0 ? 1u : 0u);
+                }
+            }
+            mma_commit(s_bar);
+        }
+        ok = __syncthreads_and(mbar_wait(s_bar, phase));  // block-uniform decision
+        phase ^= 1;
+        tc_fence_after();
+        if (!ok) break;
+        // Weight-gradient rows: TMEM lane = output feature. The TMEM load is warp-collective, so
+        // every lane of a warp that holds gradient rows takes part; only real rows are reduced.
+        const int out_real = j == L - 1 ? 3 : K_out;
+        if (warp * 32 < out_real) {
+            float* gdst = grad + ly.poff[j] + tid * N_in;
+            for (int c = 0; c < N_in / 16; ++c) {
+                float v[16];
+                tmem_ld16(tm_dw + lane_base + c * 16, v);
+                tmem_wait_ld();
+                if (tid < out_real) {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 4)
+                        atomicAdd(reinterpret_cast<float4*>(gdst + c * 16 + i),
+                                  make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]));
+                }
+            }
+        }
+        if (j > 0) {
+#pragma unroll
+            for (int c = 0; c < kWidth / 16; ++c) {
+                float v[16], a[16];
+                tmem_ld16(tm_dx + lane_base + c * 16, v);
+                tmem_wait_ld();
+                load_row16(act(j), tid, c * 16, kWidth, a);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = a[i] > 0.0f ? v[i] : 0.0f;
+                store_row16(dz_next, tid, c * 16, kWidth, v);
+            }
+            dz = dz_next;
+            dz_next = dz_next == s_dza ? s_dzb : s_dza;
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicOr(err, kErrTimeout);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// ------------------------------------------------------------------------------ elementwise kernels
+struct ParamIndex {
+    int j, o, i;
+};
+__device__ __forceinline__ ParamIndex param_index(const NetLayout& ly, int p) {
+    int j = 0;
+    while (j + 1 < ly.L && p >= ly.poff[j + 1]) ++j;
+    int r = p - ly.poff[j];
+    return {j, r / ly.in[j], r % ly.in[j]};
+}
+
+// FP16 weight image in the shared-memory layout (matrix j as [out][in] core matrices).
+__global__ void pack_kernel(const NetLayout ly, const float* __restrict__ w, uint8_t* __restrict__ blob) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ly.nparams) return;
+    ParamIndex x = param_index(ly, p);
+    *reinterpret_cast<__half*>(blob + ly.boff[x.j] + cm_offset(x.o, x.i, ly.in[x.j])) = __float2half_rn(w[p]);
+}
+
+// Adam with L2 regularisation on unscaled gradients, optional EMA of the weights (inference
+// weights = bias-corrected EMA), and repacking of both FP16 images.
+__global__ void adam_kernel(const NetLayout ly, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ grad, float* __restrict__ ema, uint8_t* __restrict__ blob_train,
+                            uint8_t* __restrict__ blob_infer, float lr, float beta1, float beta2, float eps, float l2,
+                            float inv_scale, float c1, float c2, float ema_decay, float ema_corr) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ly.nparams) return;
+    ParamIndex x = param_index(ly, p);
+    bool real = x.i < (x.j == 0 ? ly.in_real : ly.in[x.j]) && x.o < (x.j == ly.L - 1 ? 3 : ly.out[x.j]);
+    float wi = w[p];
+    if (real) {
+        float g = grad[p] * inv_scale + l2 * wi;
+        float mi = beta1 * m[p] + (1.0f - beta1) * g;
+        float vi = beta2 * v[p] + (1.0f - beta2) * g * g;
+        m[p] = mi;
+        v[p] = vi;
+        wi -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[p] = wi;
+    }
+    uint32_t off = cm_offset(x.o, x.i, ly.in[x.j]);
+    *reinterpret_cast<__half*>(blob_train + ly.boff[x.j] + off) = __float2half_rn(wi);
+    float wi_inf = wi;
+    if (ema_decay > 0.0f) {
+        float e = ema_decay * ema[p] + (1.0f - ema_decay) * wi;
+        ema[p] = e;
+        wi_inf = e / ema_corr;
+    }
+    *reinterpret_cast<__half*>(blob_infer + ly.boff[x.j] + off) = __float2half_rn(wi_inf);
+}
+
+template <int IN>
+__global__ void encode_kernel(const NetLayout ly, const float* __restrict__ in, uint32_t n, float* __restrict__ out) {
+    // Encodes one 128-row tile per CTA into shared memory, then writes FP32 rows.
+    __shared__ __align__(128) uint8_t tile[kTile * IN * 2];
+    uint32_t row = blockIdx.x * kTile + threadIdx.x;
+    float q[14];
+    load_query(in, row, n, q);
+    encode_row(ly.enc, q, tile, threadIdx.x, IN);
+    if (row < n)
+        for (int c = 0; c < IN; c += 16) {
+            float v[16];
+            load_row16(tile, threadIdx.x, c, IN, v);
+            for (int i = 0; i < 16; ++i) out[static_cast<size_t>(row) * IN + c + i] = v[i];
+        }
+}
+
+// Tensor-core self test (see nrc_selftest_mma).
+__global__ void selftest_kernel(const float* __restrict__ A, const float* __restrict__ B, int a_mn, int b_mn,
+                                float* __restrict__ D, unsigned int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr int M = 128, N = 64, K = 64;
+    uint8_t* sa = smem;              // 16 KB
+    uint8_t* sb = smem + 16384;      // 8 KB
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 65536);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int e = tid; e < M * K; e += blockDim.x) {
+        int m = e / K, k = e % K;
+        uint32_t off = a_mn ? cm_offset(k, m, M) : cm_offset(m, k, K);
+        *reinterpret_cast<__half*>(sa + off) = __float2half_rn(A[e]);
+    }
+    for (int e = tid; e < N * K; e += blockDim.x) {
+        int nn = e / K, k = e % K;
+        uint32_t off = b_mn ? cm_offset(k, nn, N) : cm_offset(nn, k, K);
+        *reinterpret_cast<__half*>(sb + off) = __float2half_rn(B[e]);
+    }
+    if (warp == 0) tmem_alloc(slot, 64);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    if (tid == 0) {
+        // mode 1: MN-major with leading offset along K and stride offset along M/N (the kernels'
+        // convention); mode 2: the two offsets exchanged (diagnostic).
+        const uint32_t id = idesc_f16(M, N, a_mn ? 1 : 0, b_mn ? 1 : 0);
+        for (int ks = 0; ks < K / 16; ++ks) {
+            uint64_t ad = a_mn == 1   ? smem_desc(smem_u32(sa) + ks * 2 * (M * 16), M * 16, 128)
+                          : a_mn == 2 ? smem_desc(smem_u32(sa) + ks * 2 * (M * 16), 128, M * 16)
+                                      : smem_desc(smem_u32(sa) + ks * 256, 128, K * 16);
+            uint64_t bd = b_mn == 1   ? smem_desc(smem_u32(sb) + ks * 2 * (N * 16), N * 16, 128)
+                          : b_mn == 2 ? smem_desc(smem_u32(sb) + ks * 2 * (N * 16), 128, N * 16)
+                                      : smem_desc(smem_u32(sb) + ks * 256, 128, K * 16);
+            mma_f16(tmem, ad, bd, id, ks > 0 ? 1u : 0u);
+        }
+        mma_commit(bar);
+    }
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    tc_fence_after();
+    if (ok) {
+        for (int c = 0; c < N / 16; ++c) {
+            float v[16];
+            tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 16, v);
+            tmem_wait_ld();
+            for (int i = 0; i < 16; ++i) D[tid * N + c * 16 + i] = v[i];
+        }
+    } else if (tid == 0) {
+        atomicOr(err, kErrTimeout);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// ------------------------------------------------------------------------------ host side
+uint32_t infer_smem(const NetLayout& l) {
+    return align_up(l.blob_bytes, 1024) + kTile * l.in_dim * 2 + kTile * kWidth * 2 + 16;
+}
+uint32_t train_smem(const NetLayout& l) {
+    return align_up(l.blob_bytes, 1024) + kTile * l.in_dim * 2 + (l.L - 1) * kTile * kWidth * 2 +
+           2 * kTile * kWidth * 2 + kTile * kOutPad * 2 + 2048 + 16;
+}
+
+}  // namespace
+}  // namespace nrc
+
+using namespace nrc;
+
+struct NrcHandle {
+    NrcConfig cfg;
+    NetLayout ly;
+    int num_sms = 0;
+    float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *ema = nullptr, *loss = nullptr;
+    uint8_t *blob_train = nullptr, *blob_infer = nullptr;
+    unsigned int* err = nullptr;
+    uint64_t steps = 0;
+};
+
+namespace {
+template <typename T>
+int alloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    if (e != cudaSuccess) return fail(NRC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return NRC_OK;
+}
+
+int set_kernel_smem(const void* k, uint32_t bytes) {
+    NRC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    return NRC_OK;
+}
+
+int repack(NrcHandle* h, cudaStream_t s) {
+    int n = h->ly.nparams;
+    pack_kernel<<<(n + 255) / 256, 256, 0, s>>>(h->ly, h->w, h->blob_train);
+    pack_kernel<<<(n + 255) / 256, 256, 0, s>>>(h->ly, h->cfg.ema_decay > 0 ? h->ema : h->w, h->blob_infer);
+    NRC_CUDA(cudaGetLastError());
+    return NRC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char* nrc_last_error(void) { return g_err.c_str(); }
+
+void nrc_default_config(int32_t encoding, NrcConfig* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->encoding = encoding;
+    c->beta1 = 0.9f;
+    c->beta2 = 0.99f;
+    c->learning_rate = 1e-2f;
+    c->loss_scale = 128.0f;
+    c->seed = 1;
+    if (encoding == NRC_ENCODING_REFERENCE) {
+        // network_interface.cu:83-129 (TriangleWave option): 2 hidden layers, EMA 0.99, l2 1e-6,
+        // epsilon 1e-8, output activation None.
+        c->num_hidden_layers = 2;
+        c->epsilon = 1e-8f;
+        c->l2_reg = 1e-6f;
+        c->ema_decay = 0.99f;
+        c->output_activation = NRC_OUTPUT_NONE;
+    } else {
+        // The volume cache: 5 hidden layers, exp output, Adam lr 1e-2, betas 0.9 / 0.99.
+        c->num_hidden_layers = 5;
+        c->epsilon = 1e-8f;
+        c->l2_reg = 0.0f;
+        c->ema_decay = 0.0f;
+        c->output_activation = NRC_OUTPUT_EXP;
+    }
+}
+
+int nrc_create(const NrcConfig* cfg, NrcHandle** out) {
+    if (!cfg || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: null argument");
+    if (cfg->encoding != NRC_ENCODING_REFERENCE && cfg->encoding != NRC_ENCODING_VOLUME)
+        return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: unknown encoding");
+    int max_hidden = cfg->encoding == NRC_ENCODING_VOLUME ? 5 : 7;  // training tile must fit in shared memory
+    if (cfg->num_hidden_layers < 1 || cfg->num_hidden_layers > max_hidden)
+        return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: num_hidden_layers out of range (1..5 volume, 1..7 reference)");
+    if (!(cfg->learning_rate > 0) || !(cfg->loss_scale > 0) || cfg->ema_decay < 0 || cfg->ema_decay >= 1)
+        return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: bad optimiser settings");
+    auto* h = new NrcHandle();
+    h->cfg = *cfg;
+    h->ly = make_layout(cfg->encoding, cfg->num_hidden_layers, cfg->output_activation, cfg->loss_scale);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    const int np = h->ly.nparams;
+    int rc;
+    if ((rc = alloc(&h->w, np)) || (rc = alloc(&h->m, np)) || (rc = alloc(&h->v, np)) || (rc = alloc(&h->grad, np)) ||
+        (rc = alloc(&h->ema, np)) || (rc = alloc(&h->loss, 1)) || (rc = alloc(&h->blob_train, h->ly.blob_bytes)) ||
+        (rc = alloc(&h->blob_infer, h->ly.blob_bytes)) || (rc = alloc(&h->err, 1))) {
+        nrc_destroy(h);
+        return rc;
+    }
+    // Uniform initialisation with bound sqrt(6 / (fan_in + fan_out)); padded rows/columns are 0.
+    std::vector<float> w(np, 0.0f);
+    std::mt19937 gen(cfg->seed);
+    for (int j = 0; j < h->ly.L; ++j) {
+        int in_real = j == 0 ? h->ly.in_real : h->ly.in[j];
+        int out_real = j == h->ly.L - 1 ? 3 : h->ly.out[j];
+        float bound = std::sqrt(6.0f / static_cast<float>(in_real + out_real));
+        std::uniform_real_distribution<float> u(-bound, bound);
+        for (int o = 0; o < out_real; ++o)
+            for (int i = 0; i < in_real; ++i) w[h->ly.poff[j] + o * h->ly.in[j] + i] = u(gen);
+    }
+    if (cudaMemcpy(h->w, w.data(), np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(h->m, 0, np * sizeof(float)) != cudaSuccess || cudaMemset(h->v, 0, np * sizeof(float)) != cudaSuccess ||
+        cudaMemset(h->grad, 0, np * sizeof(float)) != cudaSuccess ||
+        cudaMemset(h->ema, 0, np * sizeof(float)) != cudaSuccess || cudaMemset(h->err, 0, sizeof(unsigned int)) != cudaSuccess) {
+        nrc_destroy(h);
+        return fail(NRC_ERR_CUDA, "nrc_create: initial upload failed");
+    }
+    if (cfg->ema_decay > 0)
+        cudaMemcpy(h->ema, w.data(), np * sizeof(float), cudaMemcpyHostToDevice);
+    if ((rc = repack(h, 0))) {
+        nrc_destroy(h);
+        return rc;
+    }
+    const bool vol = cfg->encoding == NRC_ENCODING_VOLUME;
+    if ((rc = set_kernel_smem(vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144>)
+                                  : reinterpret_cast<const void*>(mlp_infer_kernel<64>),
+                              infer_smem(h->ly))) ||
+        (rc = set_kernel_smem(vol ? reinterpret_cast<const void*>(mlp_train_kernel<144>)
+                                  : reinterpret_cast<const void*>(mlp_train_kernel<64>),
+                              train_smem(h->ly)))) {
+        nrc_destroy(h);
+        return rc;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        nrc_destroy(h);
+        return fail(NRC_ERR_CUDA, "nrc_create: initialisation failed");
+    }
+    *out = h;
+    return NRC_OK;
+}
+
+int nrc_destroy(NrcHandle* h) {
+    if (!h) return NRC_OK;
+    cudaFree(h->w);
+    cudaFree(h->m);
+    cudaFree(h->v);
+    cudaFree(h->grad);
+    cudaFree(h->ema);
+    cudaFree(h->loss);
+    cudaFree(h->blob_train);
+    cudaFree(h->blob_infer);
+    cudaFree(h->err);
+    delete h;
+    return NRC_OK;
+}
+
+static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_t* dev_n, uint32_t n, float* out) {
+    if (!h || !in || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer: null argument");
+    if (n == 0) return NRC_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t tiles = (n + kTile - 1) / kTile;
+    uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(h->num_sms) * 2);
+    uint32_t smem = infer_smem(h->ly);
+    if (h->cfg.encoding == NRC_ENCODING_VOLUME)
+        mlp_infer_kernel<144><<<grid, kTile, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    else
+        mlp_infer_kernel<64><<<grid, kTile, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    NRC_CUDA(cudaGetLastError());
+    return NRC_OK;
+}
+
+int nrc_infer(NrcHandle* h, void* stream, const float* in, uint32_t n, float* out) {
+    return infer_impl(h, stream, in, nullptr, n, out);
+}
+
+int nrc_infer_device_count(NrcHandle* h, void* stream, const float* in, const uint32_t* dev_n, uint32_t n_max,
+                           float* out) {
+    if (!dev_n) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer_device_count: null count");
+    return infer_impl(h, stream, in, dev_n, n_max, out);
+}
+
+int nrc_train(NrcHandle* h, void* stream, const float* in, const float* target, uint32_t n, float* loss_out) {
+    if (!h || !in || !target) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_train: null argument");
+    if (n == 0) return NRC_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const NetLayout& ly = h->ly;
+    NRC_CUDA(cudaMemsetAsync(h->grad, 0, ly.nparams * sizeof(float), s));
+    NRC_CUDA(cudaMemsetAsync(h->loss, 0, sizeof(float), s));
+    uint32_t tiles = (n + kTile - 1) / kTile;
+    uint32_t smem = train_smem(ly);
+    if (h->cfg.encoding == NRC_ENCODING_VOLUME)
+        mlp_train_kernel<144><<<tiles, kTile, smem, s>>>(ly, h->blob_train, in, target, n, h->grad, h->loss, h->err);
+    else
+        mlp_train_kernel<64><<<tiles, kTile, smem, s>>>(ly, h->blob_train, in, target, n, h->grad, h->loss, h->err);
+    ++h->steps;
+    const NrcConfig& c = h->cfg;
+    float c1 = 1.0f - std::pow(c.beta1, static_cast<float>(h->steps));
+    float c2 = 1.0f - std::pow(c.beta2, static_cast<float>(h->steps));
+    // The EMA starts from the initial weights (not from zero), so it needs no bias correction.
+    const float ema_corr = 1.0f;
+    adam_kernel<<<(ly.nparams + 255) / 256, 256, 0, s>>>(ly, h->w, h->m, h->v, h->grad, h->ema, h->blob_train,
+                                                         h->blob_infer, c.learning_rate, c.beta1, c.beta2, c.epsilon,
+                                                         c.l2_reg, 1.0f / c.loss_scale, c1, c2, c.ema_decay, ema_corr);
+    NRC_CUDA(cudaGetLastError());
+    if (loss_out) {
+        NRC_CUDA(cudaMemcpyAsync(loss_out, h->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        NRC_CUDA(cudaStreamSynchronize(s));
+    }
+    return NRC_OK;
+}
+
+int nrc_get_layout(NrcHandle* h, int32_t* num_layers, int32_t* in_dims, int32_t* out_dims, int64_t* total) {
+    if (!h) return fail(NRC_ERR_INVALID_ARGUMENT, "null handle");
+    if (num_layers) *num_layers = h->ly.L;
+    for (int j = 0; j < h->ly.L; ++j) {
+        if (in_dims) in_dims[j] = h->ly.in[j];
+        if (out_dims) out_dims[j] = h->ly.out[j];
+    }
+    if (total) *total = h->ly.nparams;
+    return NRC_OK;
+}
+
+int nrc_get_params(NrcHandle* h, float* host) {
+    if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
+    NRC_CUDA(cudaDeviceSynchronize());
+    NRC_CUDA(cudaMemcpy(host, h->w, h->ly.nparams * sizeof(float), cudaMemcpyDeviceToHost));
+    return NRC_OK;
+}
+
+int nrc_set_params(NrcHandle* h, const float* host) {
+    if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
+    NRC_CUDA(cudaDeviceSynchronize());
+    NRC_CUDA(cudaMemcpy(h->w, host, h->ly.nparams * sizeof(float), cudaMemcpyHostToDevice));
+    NRC_CUDA(cudaMemcpy(h->ema, host, h->ly.nparams * sizeof(float), cudaMemcpyHostToDevice));
+    int rc = repack(h, 0);
+    if (rc) return rc;
+    NRC_CUDA(cudaDeviceSynchronize());
+    return NRC_OK;
+}
+
+int nrc_get_gradients(NrcHandle* h, float* host) {
+    if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
+    NRC_CUDA(cudaDeviceSynchronize());
+    NRC_CUDA(cudaMemcpy(host, h->grad, h->ly.nparams * sizeof(float), cudaMemcpyDeviceToHost));
+    const float inv = 1.0f / h->cfg.loss_scale;
+    for (int i = 0; i < h->ly.nparams; ++i) host[i] *= inv;
+    return NRC_OK;
+}
+
+int nrc_encode(NrcHandle* h, void* stream, const float* in, uint32_t n, float* out) {
+    if (!h || !in || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
+    if (n == 0) return NRC_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t tiles = (n + kTile - 1) / kTile;
+    if (h->cfg.encoding == NRC_ENCODING_VOLUME)
+        encode_kernel<144><<<tiles, kTile, 0, s>>>(h->ly, in, n, out);
+    else
+        encode_kernel<64><<<tiles, kTile, 0, s>>>(h->ly, in, n, out);
+    NRC_CUDA(cudaGetLastError());
+    return NRC_OK;
+}
+
+uint64_t nrc_step_count(NrcHandle* h) { return h ? h->steps : 0; }
+
+uint32_t nrc_device_errors(NrcHandle* h) {
+    if (!h) return 0;
+    unsigned int e = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess) return 0xffffffffu;
+    if (cudaMemcpy(&e, h->err, sizeof(e), cudaMemcpyDeviceToHost) != cudaSuccess) return 0xffffffffu;
+    cudaMemset(h->err, 0, sizeof(unsigned int));
+    return e;
+}
+
+int nrc_selftest_mma(const float* a, const float* b, int32_t a_mn, int32_t b_mn, float* d) {
+    if (!a || !b || !d) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
+    float *da = nullptr, *db = nullptr, *dd = nullptr;
+    unsigned int* derr = nullptr;
+    int rc;
+    if ((rc = alloc(&da, 128 * 64)) || (rc = alloc(&db, 64 * 64)) || (rc = alloc(&dd, 128 * 64)) || (rc = alloc(&derr, 1)))
+        return rc;
+    cudaMemcpy(da, a, 128 * 64 * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(db, b, 64 * 64 * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemset(derr, 0, sizeof(unsigned int));
+    const uint32_t smem = 65536 + 64;
+    cudaFuncSetAttribute(selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    selftest_kernel<<<1, 128, smem>>>(da, db, std::min(std::max(a_mn, 0), 2), std::min(std::max(b_mn, 0), 2), dd, derr);
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned int herr = 0;
+    if (e == cudaSuccess) {
+        cudaMemcpy(d, dd, 128 * 64 * sizeof(float), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&herr, derr, sizeof(herr), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dd);
+    cudaFree(derr);
+    if (e != cudaSuccess) return fail(NRC_ERR_CUDA, std::string("selftest: ") + cudaGetErrorString(e));
+    if (herr) return fail(NRC_ERR_DEVICE, "selftest: tensor-core completion wait timed out");
+    return NRC_OK;
+}
+
+}  // extern "C"

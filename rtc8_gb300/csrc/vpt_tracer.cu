@@ -38,7 +38,7 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 // Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp.
 constexpr int kCellStepsPerPass = 1;
 // Parked lanes of a warp that trigger a joint event phase.
-constexpr int kParkThreshold = 12;
+constexpr int kParkThreshold = 24;
 
 struct DdaState {
     int cell[3];

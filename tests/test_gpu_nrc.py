@@ -1,0 +1,143 @@
+"""GPU radiance-cache MLP (tcgen05) against the oracle network, through the C ABI.
+
+Tolerances: FP16 weights / activations with FP32 accumulation (GPU) against FP64 accumulation
+with the same FP16 rounding points (oracle): outputs within 2e-2 relative, gradient vectors
+within 3e-2 relative L2 error (cosine > 0.999), loss within 1e-3 relative, Adam updates within
+1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import orc
+from rtc8_gb300 import nrc
+
+pytestmark = pytest.mark.gpu
+
+
+def _queries(n, seed=0, volume=True):
+    rng = np.random.default_rng(seed)
+    q = np.zeros((n, 14), np.float32)
+    q[:, 0:3] = rng.random((n, 3))
+    q[:, 3] = rng.random(n) * np.pi
+    q[:, 4] = rng.random(n) * 2 * np.pi
+    q[:, 5] = rng.random(n) * np.pi
+    q[:, 6] = rng.random(n) * 2 * np.pi
+    q[:, 7] = rng.random(n) if volume else 0.0
+    q[:, 8:11] = rng.random((n, 3))
+    q[:, 11:14] = 0.0 if volume else rng.random((n, 3))
+    return q
+
+
+def _target(q):
+    """A smooth radiance-like field of position and direction."""
+    p = q[:, 0:3]
+    base = 0.5 + 0.4 * np.sin(3 * p[:, 0:1] + 2 * p[:, 1:2]) * np.cos(2 * p[:, 2:3] + q[:, 5:6])
+    return np.concatenate([base, 0.8 * base, 0.6 * base + 0.1], axis=1).astype(np.float32)
+
+
+@pytest.mark.parametrize("a_mode,b_mode", [(0, 0), (1, 1), (0, 1), (1, 0)])
+def test_tensor_core_descriptor_layouts(cuda_device, a_mode, b_mode):
+    rng = np.random.default_rng(a_mode * 2 + b_mode)
+    a = rng.standard_normal((128, 64)).astype(np.float32)
+    b = rng.standard_normal((64, 64)).astype(np.float32)
+    ah = a.astype(np.float16).astype(np.float64)
+    bh = b.astype(np.float16).astype(np.float64)
+    ref = ah @ bh.T
+    d = nrc.selftest_mma(a, b, a_mode, b_mode)
+    err = np.abs(d - ref).max() / np.abs(ref).max()
+    if err > 1e-3 and (a_mode or b_mode):
+        alt = nrc.selftest_mma(a, b, 2 if a_mode else 0, 2 if b_mode else 0)
+        alt_err = np.abs(alt - ref).max() / np.abs(ref).max()
+        pytest.fail(f"MN-major layout mismatch: err {err:.3e}; exchanged offsets give {alt_err:.3e}")
+    assert err < 1e-3
+
+
+@pytest.mark.parametrize("encoding", [nrc.NRC_ENCODING_REFERENCE, nrc.NRC_ENCODING_VOLUME])
+def test_encodings_match_oracle(cuda_device, encoding):
+    import torch
+
+    cfg = nrc.default_config(encoding)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    q = _queries(300, 1, volume=encoding == nrc.NRC_ENCODING_VOLUME)
+    tq = torch.from_numpy(q).cuda()
+    d = orc.nrc_lib().orc_nrc_in_dim(encoding)
+    out = torch.zeros((300, d), dtype=torch.float32, device="cuda")
+    cache.encode(None, tq, 300, out)
+    torch.cuda.synchronize()
+    ref = orc.nrc_encode(encoding, q).astype(np.float16).astype(np.float32)
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=2e-3, atol=2e-3)
+    cache.finalize()
+
+
+@pytest.mark.parametrize("encoding,hidden", [(nrc.NRC_ENCODING_VOLUME, 5), (nrc.NRC_ENCODING_REFERENCE, 2)])
+def test_inference_matches_oracle(cuda_device, encoding, hidden):
+    import torch
+
+    cfg = nrc.default_config(encoding)
+    cfg.num_hidden_layers = hidden
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    w = cache.params()
+    n = 1000  # not a multiple of 128
+    q = _queries(n, 2, volume=encoding == nrc.NRC_ENCODING_VOLUME)
+    tq = torch.from_numpy(q).cuda()
+    out = torch.full((n, 3), -7.0, dtype=torch.float32, device="cuda")
+    cache.infer(None, tq, n, out)
+    torch.cuda.synchronize()
+    ref = orc.nrc_forward(encoding, hidden, cfg.output_activation, w, q)
+    got = out.cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got, ref, rtol=2e-2, atol=2e-2 * scale)
+    assert cache.device_errors() == 0
+    cache.finalize()
+
+
+@pytest.mark.parametrize("encoding,hidden", [(nrc.NRC_ENCODING_VOLUME, 5), (nrc.NRC_ENCODING_REFERENCE, 2)])
+def test_gradients_loss_and_adam_match_oracle(cuda_device, encoding, hidden):
+    import torch
+
+    cfg = nrc.default_config(encoding)
+    cfg.num_hidden_layers = hidden
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    w0 = cache.params()
+    n = 640
+    q = _queries(n, 3, volume=encoding == nrc.NRC_ENCODING_VOLUME)
+    t = _target(q)
+    loss = cache.train(None, torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda(), n, loss=True)
+    g_gpu = cache.gradients()
+    ref_loss, g_ref = orc.nrc_loss_grad(encoding, hidden, cfg.output_activation, cfg.loss_scale, w0, q, t)
+    assert loss == pytest.approx(ref_loss, rel=1e-3)
+    rel = np.linalg.norm(g_gpu - g_ref) / np.linalg.norm(g_ref)
+    cos = float(g_gpu @ g_ref / (np.linalg.norm(g_gpu) * np.linalg.norm(g_ref)))
+    assert rel < 3e-2 and cos > 0.999, (rel, cos)
+    # one Adam step on the GPU's own gradient, restated on the host
+    w1 = cache.params()
+    lay = cache.layout()
+    ref_w1, _, _ = orc.adam(w0, np.zeros_like(w0), np.zeros_like(w0), g_gpu, cfg.learning_rate, cfg.beta1,
+                            cfg.beta2, cfg.epsilon, cfg.l2_reg, 1)
+    # padded rows / columns stay untouched
+    np.testing.assert_allclose(w1, np.where(g_ref == 0, w0, ref_w1), rtol=1e-5, atol=1e-6)
+    assert lay["total"] == len(w0)
+    cache.finalize()
+
+
+def test_training_reduces_loss(cuda_device):
+    import torch
+
+    cfg = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    n = 16384
+    rng = np.random.default_rng(5)
+    losses = []
+    for step in range(300):
+        q = _queries(n, 100 + step % 8)
+        t = _target(q)
+        l = cache.train(None, torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda(), n, loss=(step % 50 == 0 or step == 299))
+        if l is not None:
+            losses.append(l)
+    assert losses[-1] < 0.2 * losses[0], losses
+    assert cache.device_errors() == 0
+    cache.finalize()
