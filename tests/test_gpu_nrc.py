@@ -117,9 +117,17 @@ def test_gradients_loss_and_adam_match_oracle(cuda_device, encoding, hidden):
     lay = cache.layout()
     ref_w1, _, _ = orc.adam(w0, np.zeros_like(w0), np.zeros_like(w0), g_gpu, cfg.learning_rate, cfg.beta1,
                             cfg.beta2, cfg.epsilon, cfg.l2_reg, 1)
-    # padded rows / columns stay untouched
-    np.testing.assert_allclose(w1, np.where(g_ref == 0, w0, ref_w1), rtol=1e-5, atol=1e-6)
-    assert lay["total"] == len(w0)
+    # padded rows / columns stay untouched; every real weight takes the Adam step (with L2)
+    real = np.zeros_like(w0, dtype=bool)
+    off = 0
+    in_real = 138 if encoding == nrc.NRC_ENCODING_VOLUME else 62
+    for j, (fi, fo) in enumerate(zip(lay["in"], lay["out"])):
+        m = np.zeros((fo, fi), bool)
+        m[: (3 if j == lay["L"] - 1 else fo), : (in_real if j == 0 else fi)] = True
+        real[off: off + fo * fi] = m.reshape(-1)
+        off += fo * fi
+    assert off == lay["total"] == len(w0)
+    np.testing.assert_allclose(w1, np.where(real, ref_w1, w0), rtol=1e-5, atol=1e-6)
     cache.finalize()
 
 
