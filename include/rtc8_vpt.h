@@ -212,6 +212,68 @@ int vpt_synchronize(VptContext* ctx, void* stream);
 int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,
                          int32_t park_threshold);
 
+/* ---- Neural radiance cache passes (renderer/renderer_main.cpp:1553-1637) ----------------
+ * The training and render passes of the tracer, the set-up kernels between them, and one call
+ * that runs a whole frame with a cache from rtc8_nrc.h. Buffers follow the reference's
+ * (renderer/renderer_main.cpp:197-230): RadianceQuery records of 14 floats (inference buffer
+ * roundUp(w*h, 128) records, training buffers 2 x 2^17), TerminalInfo / TrainingVertexInfo
+ * records of 16 bytes, training-suffix terminals of 4 bytes, predictions of 3 floats. The
+ * training image size and the number of training vertices stay on the device. The world box of
+ * the queries is the density grid's box (a volume-only scene, compute_light_probs.cu:139-157). */
+#define VPT_NRC_TRAIN_DATA_PER_FRAME 65536u  /* numTrainingDataPerFrame (renderer_shared.h:12) */
+#define VPT_NRC_TRAIN_BUFFER_SIZE 131072u    /* trainBufferSize (renderer_shared.h:13) */
+#define VPT_NRC_QUERY_FLOATS 14
+
+typedef struct VptNrcBuffers {
+    float* infer_query;          /* inferenceRadianceQueryBuffer: infer_capacity x 14 */
+    void* infer_terminal;        /* inferenceTerminalInfoBuffer: w*h x {float tp[3]; u32 bits} */
+    uint32_t* train_suffix;      /* trainSuffixTerminalInfoBuffer: w*h */
+    float* inferred;             /* inferredRadianceBuffer: infer_capacity x 3 */
+    float* frame_contribution;   /* perFrameContributionBuffer: w*h x 3 */
+    float* train_query[2];       /* trainRadianceQueryBuffer[0..1]: 2^17 x 14 */
+    float* train_target[2];      /* trainTargetBuffer[0..1]: 2^17 x 3 */
+    void* train_vertex;          /* trainVertexInfoBuffer: 2^17 x {float tp[3]; u32 bits} */
+    uint32_t* shufflers;         /* dataShufflerBuffer: 2^16 LCG states */
+    uint32_t* counters;          /* [0..1] numTrainingData, [2..5] trainImageSize (x, y) per
+                                    buffer, [6] offsetToSelectUnbiasedPath, [7] training-pass
+                                    queries (trainW * trainH), [8..15] unused */
+    float* stats;                /* per buffer: targetMinMax (min rgb, max rgb), targetAvg */
+    uint32_t infer_capacity;
+    uint32_t buffer_index;       /* nrcBufferIndex of the last training iteration */
+} VptNrcBuffers;
+
+/* Allocates the cache buffers (once per context; the shufflers start from the LCG seeded with
+ * 471313181, renderer_main.cpp:218-229). Called implicitly by the entry points below. */
+int vpt_nrc_enable(VptContext* ctx);
+int vpt_nrc_get_buffers(VptContext* ctx, VptNrcBuffers* out);
+/* Whether the query's roughness slot carries the local density / density_coeff (for the volume
+ * encoding of rtc8_nrc.h; the reference writes roughness 0 in a medium, 0 = that). The cache's
+ * target scale is VptFrameParams.radiance_scale. */
+int vpt_nrc_set_query_density(VptContext* ctx, int32_t query_density);
+/* prepareNRC(offsetToSelectUnbiasedPath, isNewSequence) on training buffer `buffer_index`
+ * (nrc_set_up_kernels.cu:4-44). */
+int vpt_prepare_nrc(VptContext* ctx, void* stream, uint32_t buffer_index, uint32_t offset, int32_t new_sequence);
+/* generateTrainingData on the training image of buffer `buffer_index`. */
+int vpt_launch_generate_training(VptContext* ctx, void* stream, uint32_t buffer_index);
+/* propagateRadianceValues (nrc_set_up_kernels.cu:46-86), reading the cache's predictions for
+ * the training-pass queries from `inferred`. */
+int vpt_propagate(VptContext* ctx, void* stream);
+/* shuffleTrainingData (nrc_set_up_kernels.cu:88-174) of buffer `buffer_index` into buffer 1. */
+int vpt_shuffle(VptContext* ctx, void* stream, uint32_t buffer_index);
+/* pathTraceWithNRC on the full image: one sample per pixel. */
+int vpt_launch_render_nrc(VptContext* ctx, void* stream);
+/* accumulateInferredRadianceValues (nrc_set_up_kernels.cu:176-219) as sample number
+ * `accum_frames` of the FP32 running mean, also added to the FP64 sums. */
+int vpt_accumulate_inferred(VptContext* ctx, void* stream, uint32_t accum_frames);
+/* One frame of renderer_main.cpp:1553-1637 with the cache `nrc` (an NrcHandle* of
+ * rtc8_nrc.h): `train_iterations` x (prepareNRC with the next offset of mt19937(72139121) and
+ * isNewSequence = new_sequence, training pass, inference on its queries, propagation, shuffle,
+ * 4 training steps of 16384 records), then `spp` x (render pass, inference, accumulation).
+ * Accumulation continues the context's (the reference restarts it every frame: call
+ * vpt_reset_accumulation first for that). Nothing is synchronised. */
+int vpt_nrc_frame(VptContext* ctx, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
+                  int32_t new_sequence);
+
 #ifdef __cplusplus
 }
 #endif

@@ -290,3 +290,129 @@ def adam(w, m, v, grad, lr, beta1, beta2, eps, l2, step):
     nrc_lib().orc_adam(p(w, C.c_float), p(m, C.c_float), p(v, C.c_float), p(g, C.c_float), len(w), lr, beta1, beta2,
                        eps, l2, step)
     return w, m, v
+
+
+# ------------------------------------------------------------------------------ radiance-cache passes
+class OrcNrcSink(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32),
+        ("density_query", C.c_int32),
+        ("img_w", C.c_uint32),
+        ("img_h", C.c_uint32),
+        ("unbiased_offset", C.c_uint32),
+        ("infer_query", f32p),
+        ("terminal_tp", f32p),
+        ("terminal_bits", u32p),
+        ("frame_contribution", f32p),
+        ("train_suffix", u32p),
+        ("train_query", f32p),
+        ("train_target", f32p),
+        ("train_local_tp", f32p),
+        ("train_bits", u32p),
+        ("num_train", u32p),
+    ]
+
+
+TRAIN_BUFFER_SIZE = 131072
+TRAIN_PER_FRAME = 65536
+INVALID_VERTEX = 0x3FFFFF
+
+_PASS_FUNCS = {
+    "orc_nrc_pass": (C.c_int64, [C.POINTER(OrcScene), u64p, C.POINTER(OrcNrcSink), u32p]),
+    "orc_nrc_shufflers": (None, [u32p]),
+    "orc_nrc_prepare": (None, [u32p, f32p, u32p, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32]),
+    "orc_nrc_propagate": (None, [C.c_uint32, u32p, f32p, f32p, f32p, f32p, f32p, C.c_float]),
+    "orc_nrc_shuffle": (None, [C.c_uint32, f32p, u32p, f32p, f32p, f32p, f32p, C.c_float, u32p]),
+    "orc_nrc_accumulate": (None, [C.c_uint32, f32p, f32p, f32p, f32p, C.c_float, C.c_uint32, f64p, f32p]),
+}
+
+
+def pass_lib():
+    L = lib()
+    for name, (res, args) in _PASS_FUNCS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def nrc_pass(sc: OracleScene, rng: np.ndarray, mode: int, img_w: int, img_h: int, unbiased_offset: int = 0,
+             density_query: bool = False, log: bool = False) -> dict:
+    """One radiance-cache pass (mode 1 render, 2 training) on the pass image img_w x img_h;
+    `rng` (the full image's per-pixel states) is advanced in place."""
+    n = img_w * img_h
+    out = {
+        "infer_query": np.zeros((n, 14), np.float32),
+        "terminal_tp": np.zeros((n, 3), np.float32),
+        "terminal_bits": np.zeros(n, np.uint32),
+        "frame_contribution": np.zeros((n, 3), np.float32),
+        "train_suffix": np.full(n, INVALID_VERTEX, np.uint32),
+        "train_query": np.zeros((TRAIN_BUFFER_SIZE, 14), np.float32),
+        "train_target": np.zeros((TRAIN_BUFFER_SIZE, 3), np.float32),
+        "train_local_tp": np.zeros((TRAIN_BUFFER_SIZE, 3), np.float32),
+        "train_bits": np.zeros(TRAIN_BUFFER_SIZE, np.uint32),
+        "num_train": np.zeros(1, np.uint32),
+    }
+    k = OrcNrcSink()
+    k.mode, k.density_query, k.img_w, k.img_h = mode, int(density_query), img_w, img_h
+    k.unbiased_offset = unbiased_offset & 0xFFFFFFFF
+    for name, t in (("infer_query", C.c_float), ("terminal_tp", C.c_float), ("terminal_bits", C.c_uint32),
+                    ("frame_contribution", C.c_float), ("train_suffix", C.c_uint32), ("train_query", C.c_float),
+                    ("train_target", C.c_float), ("train_local_tp", C.c_float), ("train_bits", C.c_uint32),
+                    ("num_train", C.c_uint32)):
+        setattr(k, name, p(out[name], t))
+    dlog = np.zeros((n, 4), np.uint32) if log else None
+    out["lookups"] = int(pass_lib().orc_nrc_pass(sc.ref, p(rng, C.c_uint64), C.byref(k),
+                                                 p(dlog, C.c_uint32) if log else None))
+    out["log"] = dlog
+    return out
+
+
+def nrc_shufflers() -> np.ndarray:
+    out = np.zeros(TRAIN_PER_FRAME, np.uint32)
+    pass_lib().orc_nrc_shufflers(p(out, C.c_uint32))
+    return out
+
+
+def nrc_prepare(counters: np.ndarray, stats: np.ndarray, train_suffix: np.ndarray, width: int, height: int,
+                buf: int, offset: int, new_sequence: bool) -> None:
+    pass_lib().orc_nrc_prepare(p(counters, C.c_uint32), p(stats, C.c_float), p(train_suffix, C.c_uint32), width,
+                               height, buf, offset & 0xFFFFFFFF, int(new_sequence))
+
+
+def nrc_propagate(num_suffixes: int, train_suffix, inferred, infer_query, vertex, train_query0, train_target0,
+                  radiance_scale: float = 0.0) -> None:
+    """vertex: (M, 4) float32 records (local throughput rgb + bits reinterpreted)."""
+    pass_lib().orc_nrc_propagate(num_suffixes, p(train_suffix, C.c_uint32), p(inferred, C.c_float),
+                                 p(infer_query, C.c_float), p(vertex, C.c_float), p(train_query0, C.c_float),
+                                 p(train_target0, C.c_float), radiance_scale)
+
+
+def nrc_shuffle(num_training: int, stats_buf, shufflers, train_query0, train_target0, train_query1, train_target1,
+                radiance_scale: float = 0.0) -> np.ndarray:
+    writers = np.zeros(TRAIN_PER_FRAME, np.uint32)
+    pass_lib().orc_nrc_shuffle(num_training, p(stats_buf, C.c_float), p(shufflers, C.c_uint32),
+                               p(train_query0, C.c_float), p(train_target0, C.c_float), p(train_query1, C.c_float),
+                               p(train_target1, C.c_float), radiance_scale, p(writers, C.c_uint32))
+    return writers
+
+
+def nrc_accumulate(num_pixels: int, terminal, frame_contribution, inferred, infer_query, radiance_scale: float,
+                   accum_frames: int, sum_rgb, mean_rgb) -> None:
+    pass_lib().orc_nrc_accumulate(num_pixels, p(terminal, C.c_float), p(frame_contribution, C.c_float),
+                                  p(inferred, C.c_float), p(infer_query, C.c_float), radiance_scale, accum_frames,
+                                  p(sum_rgb, C.c_double), p(mean_rgb, C.c_float))
+
+
+def suffix_chains(train_suffix: np.ndarray, bits: np.ndarray, n_items: int) -> list:
+    """Per pass pixel, the list of training-vertex indices from the first vertex to the last
+    (walking the prev links back from the suffix terminal)."""
+    chains = []
+    for i in range(n_items):
+        idx = int(train_suffix[i]) & INVALID_VERTEX
+        chain = []
+        while idx != INVALID_VERTEX and len(chain) < TRAIN_BUFFER_SIZE:
+            chain.append(idx)
+            idx = int(bits[idx]) & INVALID_VERTEX
+        chains.append(chain[::-1])
+    return chains

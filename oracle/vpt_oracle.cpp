@@ -555,15 +555,47 @@ inline RGB next_event(const OrcScene& s, Pcg32& rng, V3 pos, const Frame& fr, fl
     return ret;
 }
 
-// optix_pathtracing_kernels.cu:31-434 with withNRC = generateTrainingData = false.
-RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], int64_t* lookups) {
+// RadianceQuery of an in-medium vertex (optix_pathtracing_kernels.cu:14-29; the medium's
+// surface parameters are common_renderer_types.h:2133-2140): position in the world box,
+// normal = vOut (polar angles, slots in the reference's order), roughness 0 (or the local
+// density / density_coeff when density queries are on), diffuse = albedo, specular = 0.
+void write_query(const OrcScene& s, float* q, V3 pos, V3 vout, float roughness) {
+    const float d[3] = {s.world_max[0] - s.world_min[0], s.world_max[1] - s.world_min[1],
+                        s.world_max[2] - s.world_min[2]};
+    const float r[3] = {pos.x - s.world_min[0], pos.y - s.world_min[1], pos.z - s.world_min[2]};
+    for (int a = 0; a < 3; ++a) q[a] = d[a] != 0 ? r[a] / d[a] : 0.0f;
+    float th, ph;
+    to_polar_yup(vout, &th, &ph);
+    q[3] = th;
+    q[4] = ph;
+    q[5] = th;
+    q[6] = ph;
+    q[7] = roughness;
+    q[8] = q[9] = q[10] = s.albedo;
+    q[11] = q[12] = q[13] = 0.0f;
+}
+
+inline uint32_t suffix_bits(uint32_t prev, uint32_t has_query, uint32_t path_length, uint32_t unbiased) {
+    return (prev & ORC_NRC_INVALID_VERTEX) | ((has_query & 1u) << 22) | ((path_length & 0xFFu) << 23) |
+           ((unbiased & 1u) << 31);
+}
+
+// optix_pathtracing_kernels.cu:31-434. nrc == nullptr: pathTrace (withNRC = false). Otherwise
+// pathTraceWithNRC (mode 1) or generateTrainingData (mode 2) writing the pass's records for
+// pixel `item` of the pass image.
+RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], int64_t* lookups,
+               const OrcNrcSink* nrc = nullptr, uint32_t item = 0, bool unbiased = false) {
+    const bool with_nrc = nrc != nullptr;
+    const bool train = with_nrc && nrc->mode == 2;
+    const float img_w = with_nrc ? static_cast<float>(nrc->img_w) : static_cast<float>(s.width);
+    const float img_h = with_nrc ? static_cast<float>(nrc->img_h) : static_cast<float>(s.height);
     V3 origin, dir;
     float dir_pdf;
     {
         float ux = rng.uniform();
-        float fx = (px + ux) / s.width;
+        float fx = (px + ux) / img_w;
         float uy = rng.uniform();
-        float fy = (py + uy) / s.height;
+        float fy = (py + uy) / img_h;
         float vh = 2 * std::tan(s.cam_fovy * 0.5f);
         float vw = s.cam_aspect * vh;
         float sensor_area = vw * vh;
@@ -579,6 +611,10 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
     const float init_importance = luminance(throughput);
     uint32_t path_length = 0;
     uint32_t end_code = 0;
+    float primary_spread = 0.0f, sqrt_spread = 0.0f;
+    uint32_t prev_vertex = ORC_NRC_INVALID_VERTEX;
+    RGB prev_local_tp = rgb(0, 0, 0);
+    bool terminal_written = false;
     while (true) {
         ++path_length;
         if (path_length > kHardVertexCap) {
@@ -612,20 +648,68 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                     float bsdf_pdf = dir_pdf;
                     mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                 }
-                contribution = contribution + throughput * (radiance * mis);
+                RGB implicit = radiance * mis;
+                if (!train) contribution = contribution + throughput * implicit;
+                if (train && prev_vertex != ORC_NRC_INVALID_VERTEX) {
+                    float* tg = nrc->train_target + 3 * static_cast<size_t>(prev_vertex);
+                    RGB add = prev_local_tp * implicit;
+                    tg[0] += add.r;
+                    tg[1] += add.g;
+                    tg[2] += add.b;
+                }
             }
             end_code = ORC_END_ESCAPE;
             break;
         }
+        const V3 seg_origin = origin;
         V3 pos = origin + hit_dist * dir;
         Frame fr = make_frame(-dir);
+        if (with_nrc) {
+            // :200-210, |cos| = 1 in a medium.
+            V3 dv = seg_origin - pos;
+            float dist2 = dv.x * dv.x + dv.y * dv.y + dv.z * dv.z;
+            if (path_length == 1)
+                primary_spread = dist2 / (4 * kPi * 1.0f);
+            else
+                sqrt_spread += std::sqrt(dist2 / (dir_pdf * 1.0f));
+        }
 
-        // Russian roulette (:254-268).
+        // Russian roulette (:254-268), from the third vertex in the training pass.
         float continue_prob = 1.0f;
-        if (static_cast<int32_t>(path_length) >= s.rr_start) {
+        bool rr_kill = false;
+        const int32_t rr_from = train ? std::max(s.rr_start, 3) : s.rr_start;
+        if (static_cast<int32_t>(path_length) >= rr_from) {
             continue_prob = std::fmin(luminance(throughput) / init_importance, 1.0f);
-            if (rng.uniform() >= continue_prob) {
-                end_code = ORC_END_RR;
+            if (rng.uniform() >= continue_prob) rr_kill = true;
+        }
+        if (!with_nrc && rr_kill) {
+            end_code = ORC_END_RR;
+            break;
+        }
+        if (with_nrc) {
+            // :282-330: end with a cache query on RR or when the spread is large enough.
+            bool ends_with_cache = rr_kill;
+            const float spread2 = sqrt_spread * sqrt_spread;
+            if (train) {
+                if (!unbiased) ends_with_cache |= spread2 > 2 * ORC_NRC_TERMINATION_FACTOR * primary_spread;
+            } else {
+                ends_with_cache |= spread2 > ORC_NRC_TERMINATION_FACTOR * primary_spread;
+            }
+            if (ends_with_cache) {
+                float rough = 0.0f;
+                if (nrc->density_query && s.density_coeff > 0) rough = density_at(s, seg_origin, dir, hit_dist) / s.density_coeff;
+                write_query(s, nrc->infer_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(item), pos, -dir, rough);
+                if (train) {
+                    nrc->train_suffix[item] = suffix_bits(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                } else {
+                    float* tp = nrc->terminal_tp + 3 * static_cast<size_t>(item);
+                    tp[0] = throughput.r;
+                    tp[1] = throughput.g;
+                    tp[2] = throughput.b;
+                    nrc->terminal_bits[item] = 1u | ((path_length & 0xFFu) << 1);
+                }
+                terminal_written = true;
+                end_code = ORC_END_CACHE;
                 break;
             }
         }
@@ -638,7 +722,7 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
             end_code = ORC_END_STEP_CAP;
             break;
         }
-        contribution = contribution + throughput * nee;
+        if (!train) contribution = contribution + throughput * nee;
 
         if (s.max_bounces > 0 && static_cast<int32_t>(path_length) >= s.max_bounces) {
             end_code = ORC_END_MAX_BOUNCES;
@@ -653,11 +737,50 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
             break;
         }
         RGB fs = rgb(s.albedo, s.albedo, s.albedo) * pdf;
+        const V3 v_out = -dir;
         dir = from_local(fr, local);
         RGB local_tp = fs * (std::fabs(1.0f) / pdf);
         throughput = throughput * local_tp;
         origin = pos;
         dir_pdf = pdf;
+        if (train) {
+            // :358-409: training vertex (vertices numbered in the order they are made).
+            const uint32_t idx = (*nrc->num_train)++;
+            float rough = 0.0f;
+            if (nrc->density_query && s.density_coeff > 0) rough = density_at(s, seg_origin, v_out * -1.0f, hit_dist) / s.density_coeff;
+            if (idx < ORC_NRC_TRAIN_BUFFER_SIZE) {
+                write_query(s, nrc->train_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(idx), pos, v_out, rough);
+                float* lt = nrc->train_local_tp + 3 * static_cast<size_t>(idx);
+                lt[0] = local_tp.r;
+                lt[1] = local_tp.g;
+                lt[2] = local_tp.b;
+                nrc->train_bits[idx] = (prev_vertex & ORC_NRC_INVALID_VERTEX) | ((path_length & 0xFFu) << 22) |
+                                       ((unbiased ? 1u : 0u) << 30);
+                float* tg = nrc->train_target + 3 * static_cast<size_t>(idx);
+                tg[0] = nee.r;
+                tg[1] = nee.g;
+                tg[2] = nee.b;
+                prev_local_tp = local_tp;
+                prev_vertex = idx;
+            } else {
+                write_query(s, nrc->infer_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(item), pos, v_out, rough);
+                nrc->train_suffix[item] = suffix_bits(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                terminal_written = true;
+                end_code = ORC_END_TRAIN_FULL;
+                break;
+            }
+        }
+    }
+    if (with_nrc && !terminal_written) {
+        if (train) {
+            nrc->train_suffix[item] = suffix_bits(prev_vertex, 0, path_length, unbiased ? 1 : 0);
+        } else {
+            float* tp = nrc->terminal_tp + 3 * static_cast<size_t>(item);
+            tp[0] = throughput.r;
+            tp[1] = throughput.g;
+            tp[2] = throughput.b;
+            nrc->terminal_bits[item] = (path_length & 0xFFu) << 1;
+        }
     }
     rec[0] = path_length;
     rec[3] = end_code;
@@ -885,6 +1008,37 @@ int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum
                 }
             }
             if (s.stream_mode == 0) rng_states[pix] = rng.state;
+        }
+    }
+    return total;
+}
+
+// One radiance-cache pass over the pass image (nrc->img_w x nrc->img_h pixels), pixels in
+// row-major order, RNG states of the full image's per-pixel buffer.
+int64_t orc_nrc_pass(const OrcScene* sc, uint64_t* rng_states, const OrcNrcSink* nrc, uint32_t* dlog) {
+    const OrcScene& s = *sc;
+    int64_t total = 0;
+    for (uint32_t py = 0; py < nrc->img_h; ++py) {
+        for (uint32_t px = 0; px < nrc->img_w; ++px) {
+            const uint32_t item = py * nrc->img_w + px;
+            const int64_t pix = static_cast<int64_t>(py) * s.width + px;
+            Pcg32 rng{rng_states[pix]};
+            // :60-66: one unbiased training suffix per 4x4 tile.
+            const uint32_t tile = (py % 4) * 4 + (px % 4);
+            const bool unbiased = nrc->mode == 2 && (tile + nrc->unbiased_offset) % 16 == 0;
+            uint32_t rec[4] = {0, 0, 0, 0};
+            int64_t lk = 0;
+            RGB c = trace_path(s, rng, static_cast<int>(px), static_cast<int>(py), rec, &lk, nrc, item, unbiased);
+            total += lk;
+            if (dlog) std::memcpy(dlog + 4 * static_cast<size_t>(item), rec, sizeof(rec));
+            rng_states[pix] = rng.state;
+            if (nrc->mode == 1) {
+                if (!all_nonneg_finite(c)) c = rgb(0, 0, 0);
+                float* fc = nrc->frame_contribution + 3 * static_cast<size_t>(item);
+                fc[0] = c.r;
+                fc[1] = c.g;
+                fc[2] = c.b;
+            }
         }
     }
     return total;

@@ -75,7 +75,31 @@ enum {
     ORC_END_PDF_ZERO = 3,
     ORC_END_MAX_BOUNCES = 4,
     ORC_END_STEP_CAP = 5,
+    ORC_END_CACHE = 6,       /* radiance-cache passes: ended with a cache query */
+    ORC_END_TRAIN_FULL = 7,  /* training pass: the training-vertex buffer was full */
 };
+
+/* Radiance-cache pass constants (renderer_shared.h:11-13, 74) and outputs. */
+#define ORC_NRC_INVALID_VERTEX 0x003FFFFFu
+#define ORC_NRC_TRAIN_BUFFER_SIZE 131072u
+#define ORC_NRC_TERMINATION_FACTOR 0.01f
+#define ORC_NRC_QUERY_FLOATS 14
+typedef struct OrcNrcSink {
+    int32_t mode;              /* 1 = pathTraceWithNRC, 2 = generateTrainingData */
+    int32_t density_query;     /* roughness slot = local density / density_coeff */
+    uint32_t img_w, img_h;     /* pass image (training image size in mode 2) */
+    uint32_t unbiased_offset;  /* offsetToSelectUnbiasedPath */
+    float* infer_query;        /* 14 per pass pixel */
+    float* terminal_tp;        /* mode 1: 3 per pixel */
+    uint32_t* terminal_bits;   /* mode 1: hasQuery | pathLength << 1 */
+    float* frame_contribution; /* mode 1: 3 per pixel */
+    uint32_t* train_suffix;    /* mode 2: per pixel, prev | hasQuery << 22 | pathLength << 23 | unbiased << 31 */
+    float* train_query;        /* mode 2: 14 per vertex */
+    float* train_target;       /* mode 2: 3 per vertex */
+    float* train_local_tp;     /* mode 2: 3 per vertex */
+    uint32_t* train_bits;      /* mode 2: prev | pathLength << 22 | unbiased << 30 */
+    uint32_t* num_train;       /* mode 2: vertex counter (numTrainingData) */
+} OrcNrcSink;
 
 int orc_version(void);
 
@@ -114,6 +138,27 @@ void orc_quat_to_matrix(const float* q, float* m9);
 int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng, int32_t accum_base, int32_t spp,
                          double* sum_rgb, float* mean_rgb, uint32_t* dlog, int32_t row0,
                          int32_t row1, int32_t nthreads);
+
+/* One radiance-cache pass (optix_pathtracing_kernels.cu:31-434, withNRC = true), one sample per
+ * pixel of the pass image, continuing the per-pixel PCG32 streams of the full image. dlog (4 x u32
+ * per pass pixel) may be null. Returns the number of density lookups. */
+int64_t orc_nrc_pass(const OrcScene* sc, uint64_t* rng, const OrcNrcSink* nrc, uint32_t* dlog);
+
+/* Set-up kernels between the passes (nrc_setup_oracle.cpp), on host copies of the buffers:
+ * counters (16 u32: numTrainingData[2], trainImageSize[2][2], offset, training queries),
+ * stats (per buffer min rgb, max rgb, avg rgb), vertex / terminal records of 4 words. */
+void orc_nrc_shufflers(uint32_t* out);
+void orc_nrc_prepare(uint32_t* counters, float* stats, uint32_t* train_suffix, int32_t width, int32_t height,
+                     uint32_t buf, uint32_t offset, int32_t new_sequence);
+void orc_nrc_propagate(uint32_t num_suffixes, const uint32_t* train_suffix, const float* inferred,
+                       const float* infer_query, const float* vertex, const float* train_query0,
+                       float* train_target0, float radiance_scale);
+void orc_nrc_shuffle(uint32_t num_training, float* stats_buf, uint32_t* shufflers, const float* train_query0,
+                     const float* train_target0, float* train_query1, float* train_target1,
+                     float radiance_scale, uint32_t* writers);
+void orc_nrc_accumulate(uint32_t num_pixels, const float* terminal, const float* frame_contribution,
+                        const float* inferred, const float* infer_query, float radiance_scale,
+                        uint32_t accum_frames, double* sum, float* mean);
 
 #ifdef __cplusplus
 }

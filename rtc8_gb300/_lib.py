@@ -100,7 +100,37 @@ _VPT = {
     "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
     "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "vpt_nrc_enable": (C.c_int, [C.c_void_p]),
+    "vpt_nrc_get_buffers": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vpt_nrc_set_query_density": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vpt_prepare_nrc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
+    "vpt_launch_generate_training": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_propagate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vpt_shuffle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_launch_render_nrc": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vpt_accumulate_inferred": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_nrc_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
 }
+
+class VptNrcBuffers(C.Structure):
+    """Device pointers of the radiance-cache buffers of a context (rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("infer_query", C.c_void_p),
+        ("infer_terminal", C.c_void_p),
+        ("train_suffix", C.c_void_p),
+        ("inferred", C.c_void_p),
+        ("frame_contribution", C.c_void_p),
+        ("train_query", C.c_void_p * 2),
+        ("train_target", C.c_void_p * 2),
+        ("train_vertex", C.c_void_p),
+        ("shufflers", C.c_void_p),
+        ("counters", C.c_void_p),
+        ("stats", C.c_void_p),
+        ("infer_capacity", C.c_uint32),
+        ("buffer_index", C.c_uint32),
+    ]
+
 
 class NrcConfig(C.Structure):
     _fields_ = [

@@ -1,0 +1,258 @@
+// C ABI of the radiance-cache frame (renderer/renderer_main.cpp:1553-1637): cache buffers of a
+// context, the training and render passes of the tracker, the set-up kernels, and the frame
+// loop with the tcgen05 network of nrc_mlp.cu. Everything is enqueued on one stream; unlike
+// the reference (renderer_main.cpp:1568-1573, 1613) no step waits for the host, because the
+// training image size and the query counts stay on the device.
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rtc8_nrc.h"
+#include "../../include/rtc8_vpt.h"
+#include "nrc_buffers.cuh"
+#include "vpt_ctx.h"
+#include "vpt_tracer.cuh"
+
+namespace {
+
+int fail(int code, const std::string& msg) { return vpt::ctx_set_error(code, msg.c_str()); }
+
+#define NRCP_CUDA(call)                                                                    \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) return fail(VPT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+cudaError_t alloc_zero(T** p, size_t count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return e;
+    }
+    return cudaMemset(*p, 0, count * sizeof(T));
+}
+
+template <typename T>
+void free_ptr(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int ensure_nrc(VptContext* c) {
+    if (c->nrc) return VPT_OK;
+    auto* b = new vpt::NrcBuffers();
+    c->nrc = b;
+    b->width = c->width;
+    b->height = c->height;
+    const size_t npix = static_cast<size_t>(c->width) * c->height;
+    b->max_train_suffixes = static_cast<uint32_t>(npix);
+    b->infer_capacity = static_cast<uint32_t>((npix + 127) / 128 * 128);
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    chk(alloc_zero(&b->infer_query, static_cast<size_t>(b->infer_capacity) * vpt::kQueryFloats));
+    chk(alloc_zero(&b->infer_terminal, npix));
+    chk(alloc_zero(&b->train_suffix, npix));
+    chk(alloc_zero(&b->inferred, static_cast<size_t>(b->infer_capacity) * 3));
+    chk(alloc_zero(&b->frame_contribution, npix * 3));
+    for (int i = 0; i < 2; ++i) {
+        chk(alloc_zero(&b->train_query[i], static_cast<size_t>(vpt::kTrainBufferSize) * vpt::kQueryFloats));
+        chk(alloc_zero(&b->train_target[i], static_cast<size_t>(vpt::kTrainBufferSize) * 3));
+    }
+    chk(alloc_zero(&b->train_vertex, vpt::kTrainBufferSize));
+    chk(alloc_zero(&b->shufflers, vpt::kNumTrainingDataPerFrame));
+    chk(alloc_zero(&b->counters, 16));
+    chk(alloc_zero(&b->stats, 18));
+    if (e != cudaSuccess) {
+        c->release_nrc();
+        return fail(VPT_ERR_OUT_OF_MEMORY, std::string("vpt_nrc_enable: ") + cudaGetErrorString(e));
+    }
+    // renderer_main.cpp:218-229: shuffler i holds the LCG state after i + 1 steps from 471313181
+    // (state = (state * 1103515245 + 12345) mod 2^31 in 32-bit arithmetic, renderer_shared.h:92-109).
+    std::vector<uint32_t> st(vpt::kNumTrainingDataPerFrame);
+    uint32_t s = 471313181u;
+    for (uint32_t i = 0; i < vpt::kNumTrainingDataPerFrame; ++i) {
+        s = (s * 1103515245u + 12345u) % (1u << 31);
+        st[i] = s;
+    }
+    NRCP_CUDA(cudaMemcpy(b->shufflers, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return VPT_OK;
+}
+
+// radianceScale of the frame (renderer_shared.h:160); <= 0 = off.
+float radiance_scale(const VptContext* c) { return c->frame.radiance_scale > 0 ? c->frame.radiance_scale : 0.0f; }
+
+// Launch of a radiance-cache pass of the persistent tracker.
+int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf) {
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::TraceParams tp;
+    if ((rc = vpt::fill_trace_params(c, &tp))) return rc;
+    tp.spp = 1;
+    tp.accum_base = 0;
+    tp.stream_mode = 0;
+    tp.park_threshold = c->park_threshold;
+    tp.nrc = *c->nrc;
+    tp.nrc_buf = buf;
+    tp.nrc_density_query = c->nrc_query_density;
+    NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
+    const int threads = c->threads > 0 ? c->threads : 128;
+    const bool grid_maj = c->frame.majorant_mode == 1;
+    size_t smem = 0;
+    if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {
+        tp.maj_in_smem = 1;
+        smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
+    }
+    const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj), smem);
+    vpt::launch_nrc_pass(tp, mode, grid_maj, ctas, threads, smem, s);
+    NRCP_CUDA(cudaGetLastError());
+    return VPT_OK;
+}
+
+}  // namespace
+
+namespace vpt {
+void VptContextImpl::release_nrc() {
+    if (!nrc) return;
+    free_ptr(nrc->infer_query);
+    free_ptr(nrc->infer_terminal);
+    free_ptr(nrc->train_suffix);
+    free_ptr(nrc->inferred);
+    free_ptr(nrc->frame_contribution);
+    for (int i = 0; i < 2; ++i) {
+        free_ptr(nrc->train_query[i]);
+        free_ptr(nrc->train_target[i]);
+    }
+    free_ptr(nrc->train_vertex);
+    free_ptr(nrc->shufflers);
+    free_ptr(nrc->counters);
+    free_ptr(nrc->stats);
+    delete nrc;
+    nrc = nullptr;
+}
+}  // namespace vpt
+
+extern "C" {
+
+int vpt_nrc_enable(VptContext* c) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_enable: null context");
+    return ensure_nrc(c);
+}
+
+int vpt_nrc_get_buffers(VptContext* c, VptNrcBuffers* out) {
+    if (!c || !out) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_get_buffers: null argument");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    const vpt::NrcBuffers& b = *c->nrc;
+    out->infer_query = b.infer_query;
+    out->infer_terminal = b.infer_terminal;
+    out->train_suffix = b.train_suffix;
+    out->inferred = b.inferred;
+    out->frame_contribution = b.frame_contribution;
+    for (int i = 0; i < 2; ++i) {
+        out->train_query[i] = b.train_query[i];
+        out->train_target[i] = b.train_target[i];
+    }
+    out->train_vertex = b.train_vertex;
+    out->shufflers = b.shufflers;
+    out->counters = b.counters;
+    out->stats = b.stats;
+    out->infer_capacity = b.infer_capacity;
+    out->buffer_index = c->nrc_buf_index;
+    return VPT_OK;
+}
+
+int vpt_nrc_set_query_density(VptContext* c, int32_t query_density) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_set_query_density: null context");
+    c->nrc_query_density = query_density ? 1 : 0;
+    return VPT_OK;
+}
+
+int vpt_prepare_nrc(VptContext* c, void* stream, uint32_t buf, uint32_t offset, int32_t new_sequence) {
+    if (!c || buf > 1) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_prepare_nrc: bad arguments");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::nrc_prepare(*c->nrc, buf, offset, new_sequence != 0, static_cast<cudaStream_t>(stream));
+    NRCP_CUDA(cudaGetLastError());
+    return VPT_OK;
+}
+
+int vpt_launch_generate_training(VptContext* c, void* stream, uint32_t buf) {
+    if (!c || buf > 1) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_launch_generate_training: bad arguments");
+    return launch_pass(c, static_cast<cudaStream_t>(stream), vpt::kModeTrainNrc, buf);
+}
+
+int vpt_propagate(VptContext* c, void* stream) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_propagate: null context");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::nrc_propagate(*c->nrc, radiance_scale(c), static_cast<cudaStream_t>(stream));
+    NRCP_CUDA(cudaGetLastError());
+    return VPT_OK;
+}
+
+int vpt_shuffle(VptContext* c, void* stream, uint32_t buf) {
+    if (!c || buf > 1) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_shuffle: bad arguments");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::nrc_shuffle(*c->nrc, buf, radiance_scale(c), static_cast<cudaStream_t>(stream));
+    NRCP_CUDA(cudaGetLastError());
+    return VPT_OK;
+}
+
+int vpt_launch_render_nrc(VptContext* c, void* stream) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_launch_render_nrc: null context");
+    return launch_pass(c, static_cast<cudaStream_t>(stream), vpt::kModeRenderNrc, 0);
+}
+
+int vpt_accumulate_inferred(VptContext* c, void* stream, uint32_t accum_frames) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_accumulate_inferred: null context");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::nrc_accumulate(*c->nrc, radiance_scale(c), accum_frames, c->d_sum, c->d_mean, c->d_err,
+                        static_cast<cudaStream_t>(stream));
+    NRCP_CUDA(cudaGetLastError());
+    return VPT_OK;
+}
+
+int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
+                  int32_t new_sequence) {
+    if (!c || !nrc) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_frame: null argument");
+    auto* net = static_cast<NrcHandle*>(nrc);
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::NrcBuffers& b = *c->nrc;
+    const uint32_t npix = static_cast<uint32_t>(c->width) * static_cast<uint32_t>(c->height);
+    for (uint32_t it = 0; it < train_iterations; ++it) {
+        c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
+        const uint32_t buf = c->nrc_buf_index;
+        const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
+        if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
+        if ((rc = vpt_launch_generate_training(c, stream, buf))) return rc;
+        // Predictions for the training suffixes' end queries (trainW * trainH of them).
+        if (nrc_infer_device_count(net, stream, b.infer_query, b.counters + 7, b.max_train_suffixes, b.inferred))
+            return fail(VPT_ERR_CUDA, std::string("nrc_infer_device_count: ") + nrc_last_error());
+        if ((rc = vpt_propagate(c, stream))) return rc;
+        if ((rc = vpt_shuffle(c, stream, buf))) return rc;
+        constexpr uint32_t kBatch = vpt::kNumTrainingDataPerFrame / 4;  // renderer_main.cpp:1595
+        for (uint32_t step = 0; step < 4; ++step) {
+            const size_t first = static_cast<size_t>(step) * kBatch;
+            if (nrc_train(net, stream, b.train_query[1] + first * vpt::kQueryFloats, b.train_target[1] + first * 3, kBatch,
+                          nullptr))
+                return fail(VPT_ERR_CUDA, std::string("nrc_train: ") + nrc_last_error());
+        }
+    }
+    for (uint32_t i = 0; i < spp; ++i) {
+        if ((rc = vpt_launch_render_nrc(c, stream))) return rc;
+        if (nrc_infer(net, stream, b.infer_query, npix, b.inferred))
+            return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
+        if ((rc = vpt_accumulate_inferred(c, stream, c->accum_samples))) return rc;
+        ++c->accum_samples;
+    }
+    return VPT_OK;
+}
+
+}  // extern "C"

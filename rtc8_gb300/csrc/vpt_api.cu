@@ -52,11 +52,9 @@ void dev_free(T** p) {
 
 namespace vpt {
 int ctx_set_error(int code, const char* msg) { return set_error(code, msg); }
-void VptContextImpl::release_nrc() {}
 }  // namespace vpt
 
 using vpt::VptContextImpl;
-struct VptContext : VptContextImpl {};
 
 extern "C" {
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <random>
 
 #include "../../include/rtc8_vpt.h"
 
@@ -59,6 +60,9 @@ struct VptContextImpl {
 
     // neural-radiance-cache render/training buffers (allocated on first use)
     NrcBuffers* nrc = nullptr;
+    int32_t nrc_query_density = 0;
+    uint32_t nrc_buf_index = 1;            // the first training iteration uses buffer 0
+    std::mt19937 nrc_offset_rng{72139121}; // perFrameRng (renderer_main.cpp:1500)
     void release_nrc();
 };
 
@@ -70,3 +74,6 @@ int generate_sky_texture(float4* out, int w, int h, const float* states, const f
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);
 
 }  // namespace vpt
+
+// The opaque handle of the C ABI.
+struct VptContext : vpt::VptContextImpl {};

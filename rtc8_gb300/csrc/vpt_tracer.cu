@@ -29,7 +29,15 @@ enum : uint32_t {
     ST_DONE,
 };
 
-enum : uint32_t { END_ESCAPE = 1, END_RR = 2, END_PDF_ZERO = 3, END_MAX_BOUNCES = 4, END_STEP_CAP = 5 };
+enum : uint32_t {
+    END_ESCAPE = 1,
+    END_RR = 2,
+    END_PDF_ZERO = 3,
+    END_MAX_BOUNCES = 4,
+    END_STEP_CAP = 5,
+    END_CACHE = 6,       // radiance-cache passes: ended with a cache query
+    END_TRAIN_FULL = 7,  // training pass: the training-vertex buffer was full
+};
 
 // Limits that apply even when the caller disables the configurable caps, so that no input
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
@@ -81,7 +89,26 @@ __device__ __forceinline__ float cell_maj(const float* maj, const Grid& g, const
     return maj[(d.cell[0] * g.my + d.cell[1]) * g.mz + d.cell[2]];
 }
 
-template <bool kGridMajorant, bool kLog>
+// createRadianceQuery (optix_pathtracing_kernels.cu:14-29) for an in-medium vertex: position in
+// the world box (basic_types.h:2835-2838), normal = vOut as toPolarYUp outputs (the first slot
+// holds acos(y), the second the azimuth), roughness, diffuse = albedo, specular = 0.
+__device__ __forceinline__ void write_query(float* q, V3 pos, V3 vout, float roughness, float albedo, V3 wmin, V3 wmax) {
+    V3 d = wmax - wmin, r = pos - wmin;
+    float a, b;
+    to_polar_yup(vout, &a, &b);
+    float2* p = reinterpret_cast<float2*>(q);
+    p[0] = make_float2(d.x != 0 ? r.x / d.x : 0.0f, d.y != 0 ? r.y / d.y : 0.0f);
+    p[1] = make_float2(d.z != 0 ? r.z / d.z : 0.0f, a);
+    p[2] = make_float2(b, a);
+    p[3] = make_float2(b, roughness);
+    p[4] = make_float2(albedo, albedo);
+    p[5] = make_float2(albedo, 0.0f);
+    p[6] = make_float2(0.0f, 0.0f);
+}
+
+// kMode: kModePlain (pathTrace), kModeRenderNrc (pathTraceWithNRC) or kModeTrainNrc
+// (generateTrainingData), optix_pathtracing_kernels.cu:438-448.
+template <bool kGridMajorant, bool kLog, int kMode>
 __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P) {
     extern __shared__ float s_maj[];
     const Grid& g = P.grid;
@@ -131,6 +158,24 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
     unsigned int err = 0;
     LeafCache leaf_cache;
 
+    // Radiance-cache passes: one sample per pixel of the pass image (the training image has the
+    // adaptive size prepared on the device), RNG states of the full image's per-pixel buffer.
+    constexpr bool kNrc = kMode != kModePlain;
+    constexpr bool kTrain = kMode == kModeTrainNrc;
+    uint32_t img_w = static_cast<uint32_t>(P.width), img_h = static_cast<uint32_t>(P.height);
+    uint32_t num_items = num_pixels;
+    if constexpr (kTrain) {
+        img_w = P.nrc.counters[2 + 2 * P.nrc_buf];
+        img_h = P.nrc.counters[3 + 2 * P.nrc_buf];
+        num_items = min(img_w * img_h, num_pixels);
+    }
+    const V3 wmin = bmin, wmax = bmax;
+    uint32_t rng_index = 0;
+    float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
+    uint32_t prev_vertex = kInvalidVertex;
+    RGB prev_local_tp = rgb(0, 0, 0), nee_value = rgb(0, 0, 0);
+    bool unbiased = false, terminal_written = false;
+
     while (true) {
         // Warp-level event batching: lanes whose path reached an event (segment end, collision,
         // new sample) park until at least kParkThreshold lanes of the warp are parked, or no lane
@@ -154,6 +199,24 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 if (static_cast<int>(lane) == leader) base = atomicAdd(P.work_counter, __popc(need));
                 base = __shfl_sync(need, base, leader);
                 const uint32_t item = base + __popc(need & ((1u << lane) - 1u));
+                if constexpr (kNrc) {
+                    if (item >= num_items) {
+                        st = ST_DONE;
+                        break;
+                    }
+                    pixel = item;  // linear index in the pass image
+                    const uint32_t px = item % img_w, py = item / img_w;
+                    rng_index = py * static_cast<uint32_t>(P.width) + px;
+                    rng.state = P.rng[rng_index];
+                    sample = 0;
+                    if constexpr (kTrain) {
+                        // optix_pathtracing_kernels.cu:60-66: one unbiased suffix per 4x4 tile.
+                        const uint32_t tile_index = (py % 4) * 4 + (px % 4);
+                        unbiased = (tile_index + P.nrc.counters[6]) % 16 == 0;
+                    }
+                    st = ST_CAMERA;
+                    break;
+                }
                 if (P.stream_mode == 1) {
                     // One (pixel, sample) per work item, samples of all pixels interleaved.
                     if (item >= num_pixels * P.spp) {
@@ -187,12 +250,15 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
             }
             case ST_CAMERA: {
                 // optix_pathtracing_kernels.cu:43-55, 76-81.
-                uint32_t px = pixel % static_cast<uint32_t>(P.width);
-                uint32_t py = pixel / static_cast<uint32_t>(P.width);
+                uint32_t px = pixel % img_w;
+                uint32_t py = pixel / img_w;
                 float ux = rng.uniform();
-                float fx = (px + ux) / P.width;
+                float fx = (px + ux) / static_cast<float>(img_w);
                 float uy = rng.uniform();
-                float fy = (py + uy) / P.height;
+                float fy = (py + uy) / static_cast<float>(img_h);
+                sqrt_spread = 0.0f;
+                prev_vertex = kInvalidVertex;
+                terminal_written = false;
                 float vh = 2 * tanf(P.cam_fovy * 0.5f);
                 float vw = P.cam_aspect * vh;
                 float sensor_area = vw * vh;
@@ -308,7 +374,18 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         float bsdf_pdf = dir_pdf;
                         mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                     }
-                    contribution = contribution + throughput * (radiance * mis);
+                    const RGB implicit = radiance * mis;
+                    if constexpr (!kTrain) contribution = contribution + throughput * implicit;
+                    if constexpr (kTrain) {
+                        // :148-152: the environment hit completes the previous vertex's target.
+                        if (prev_vertex != kInvalidVertex) {
+                            float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(prev_vertex);
+                            RGB add = prev_local_tp * implicit;
+                            tg[0] += add.r;
+                            tg[1] += add.g;
+                            tg[2] += add.b;
+                        }
+                    }
                 }
                 end_code = END_ESCAPE;
                 st = ST_END_SAMPLE;
@@ -317,12 +394,57 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
             case ST_VERTEX: {
                 // In-medium vertex (:176-182), Russian roulette (:254-268, 332), NEE set-up
                 // (renderer_kernel_common.h:297-358).
+                const V3 seg_origin = origin;
                 origin = origin + t * dir;
+                if constexpr (kNrc) {
+                    // optix_pathtracing_kernels.cu:200-210: path spread (|cos| = 1 in a medium).
+                    V3 dv = seg_origin - origin;
+                    float dist2 = dv.x * dv.x + dv.y * dv.y + dv.z * dv.z;
+                    if (path_length == 1)
+                        primary_spread = dist2 / (4 * kPi * 1.0f);
+                    else
+                        sqrt_spread += sqrtf(dist2 / (dir_pdf * 1.0f));
+                }
                 float continue_prob = 1.0f;
-                if (static_cast<int32_t>(path_length) >= P.rr_start) {
+                bool rr_kill = false;
+                // Training suffixes apply Russian roulette from the third vertex (:256-257).
+                const int32_t rr_from = kTrain ? max(P.rr_start, 3) : P.rr_start;
+                if (static_cast<int32_t>(path_length) >= rr_from) {
                     continue_prob = fminf(luminance(throughput) / init_importance, 1.0f);
-                    if (rng.uniform() >= continue_prob) {
+                    if (rng.uniform() >= continue_prob) rr_kill = true;
+                }
+                if constexpr (!kNrc) {
+                    if (rr_kill) {
                         end_code = END_RR;
+                        st = ST_END_SAMPLE;
+                        break;
+                    }
+                } else {
+                    // :282-330: the path ends with a cache query on Russian roulette or once its
+                    // spread exceeds the primary footprint (twice that for biased training suffixes).
+                    bool ends_with_cache = rr_kill;
+                    const float spread2 = sqrt_spread * sqrt_spread;
+                    if constexpr (kTrain) {
+                        if (!unbiased) ends_with_cache |= spread2 > 2 * kPathTerminationFactor * primary_spread;
+                    } else {
+                        ends_with_cache |= spread2 > kPathTerminationFactor * primary_spread;
+                    }
+                    if (ends_with_cache) {
+                        const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
+                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(pixel), origin, -dir, rough,
+                                    P.albedo, wmin, wmax);
+                        if constexpr (kTrain) {
+                            P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                        } else {
+                            TerminalInfo ti;
+                            ti.tp[0] = throughput.r;
+                            ti.tp[1] = throughput.g;
+                            ti.tp[2] = throughput.b;
+                            ti.bits = 1u | ((path_length & 0xFFu) << 1);
+                            P.nrc.infer_terminal[pixel] = ti;
+                        }
+                        terminal_written = true;
+                        end_code = END_CACHE;
                         st = ST_END_SAMPLE;
                         break;
                     }
@@ -396,6 +518,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
             }
             case ST_NEE_DONE: {
                 // renderer_kernel_common.h:385-402, then phase sampling (:341-356).
+                nee_value = rgb(0, 0, 0);
                 if (vis > 0.0f) {
                     V3 sdir = -light_dir;
                     Frame fr = make_frame(-dir);
@@ -415,7 +538,8 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         float gterm = lp_cos * 1.0f / 1.0f;
                         nee = fs * le * (vis * mis * gterm / area_pdf);
                     }
-                    contribution = contribution + throughput * nee;
+                    if constexpr (!kTrain) contribution = contribution + throughput * nee;
+                    nee_value = nee;
                 }
                 if (P.max_bounces > 0 && static_cast<int32_t>(path_length) >= P.max_bounces) {
                     end_code = END_MAX_BOUNCES;
@@ -433,16 +557,76 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     break;
                 }
                 RGB fs = rgb(P.albedo, P.albedo, P.albedo) * pdf;
+                const V3 v_out = -dir;
                 dir = from_local(fr, local);
                 RGB local_tp = fs * (fabsf(1.0f) / pdf);
                 throughput = throughput * local_tp;
                 dir_pdf = pdf;
+                if constexpr (kTrain) {
+                    // :358-409: record the training vertex (query, local throughput, link to the
+                    // previous vertex, target initialised with the NEE estimate); a full buffer
+                    // ends the suffix with a cache query.
+                    const uint32_t idx = atomicAdd(P.nrc.counters + P.nrc_buf, 1u);
+                    const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
+                    if (idx < kTrainBufferSize) {
+                        write_query(P.nrc.train_query[0] + kQueryFloats * static_cast<size_t>(idx), origin, v_out, rough,
+                                    P.albedo, wmin, wmax);
+                        TrainVertexInfo vi;
+                        vi.local_tp[0] = local_tp.r;
+                        vi.local_tp[1] = local_tp.g;
+                        vi.local_tp[2] = local_tp.b;
+                        vi.bits = (prev_vertex & kInvalidVertex) | ((path_length & 0xFFu) << 22) | ((unbiased ? 1u : 0u) << 30);
+                        P.nrc.train_vertex[idx] = vi;
+                        float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(idx);
+                        tg[0] = nee_value.r;
+                        tg[1] = nee_value.g;
+                        tg[2] = nee_value.b;
+                        prev_local_tp = local_tp;
+                        prev_vertex = idx;
+                    } else {
+                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(pixel), origin, v_out, rough,
+                                    P.albedo, wmin, wmax);
+                        P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                        terminal_written = true;
+                        err |= VPT_DEVERR_TRAIN_FULL;
+                        end_code = END_TRAIN_FULL;
+                        st = ST_END_SAMPLE;
+                        break;
+                    }
+                }
                 st = ST_SEGMENT;
                 break;
             }
             case ST_END_SAMPLE: {
                 // optix_pathtracing_kernels.cu:413-432 (non-finite samples are dropped).
                 ++n_samples;
+                if constexpr (kNrc) {
+                    if constexpr (kTrain) {
+                        if (!terminal_written)
+                            P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
+                    } else {
+                        if (!terminal_written) {
+                            TerminalInfo ti;
+                            ti.tp[0] = throughput.r;
+                            ti.tp[1] = throughput.g;
+                            ti.tp[2] = throughput.b;
+                            ti.bits = (path_length & 0xFFu) << 1;
+                            P.nrc.infer_terminal[pixel] = ti;
+                        }
+                        RGB c = contribution;
+                        if (!all_nonneg_finite(c)) {
+                            err |= VPT_DEVERR_NONFINITE;
+                            c = rgb(0, 0, 0);
+                        }
+                        float* fc = P.nrc.frame_contribution + 3 * static_cast<size_t>(pixel);
+                        fc[0] = c.r;
+                        fc[1] = c.g;
+                        fc[2] = c.b;
+                    }
+                    P.rng[rng_index] = rng.state;
+                    st = ST_FETCH;
+                    break;
+                }
                 if constexpr (kLog) {
                     uint4 rec = make_uint4(path_length, rec_primary, rec_shadow, end_code);
                     reinterpret_cast<uint4*>(P.dlog)[static_cast<uint64_t>(pixel) * P.spp + sample] = rec;
@@ -504,7 +688,10 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 vis *= (1 - density / maj);
             } else {
                 ++rec_primary;
-                if (rng.uniform() < density / maj) st = ST_VERTEX;
+                if (rng.uniform() < density / maj) {
+                    st = ST_VERTEX;
+                    last_density = density;
+                }
             }
             if (st == ST_STEP && seg_steps >= step_cap) {
                 err |= VPT_DEVERR_STEP_CAP;
@@ -566,24 +753,48 @@ void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int m
 }
 
 const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
-    if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true>)
-                                     : reinterpret_cast<const void*>(plain_trace_kernel<false, true>);
-    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false>)
-                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false>);
+    if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true, kModePlain>)
+                                     : reinterpret_cast<const void*>(plain_trace_kernel<false, true, kModePlain>);
+    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModePlain>)
+                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModePlain>);
 }
 
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s) {
     dim3 grid(grid_ctas), block(threads);
     if (p.dlog) {
         if (grid_majorant)
-            plain_trace_kernel<true, true><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, true, kModePlain><<<grid, block, smem, s>>>(p);
         else
-            plain_trace_kernel<false, true><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, true, kModePlain><<<grid, block, 0, s>>>(p);
     } else {
         if (grid_majorant)
-            plain_trace_kernel<true, false><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, false, kModePlain><<<grid, block, smem, s>>>(p);
         else
-            plain_trace_kernel<false, false><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, false, kModePlain><<<grid, block, 0, s>>>(p);
+    }
+}
+
+const void* nrc_kernel_ptr(int mode, bool grid_majorant) {
+    if (mode == kModeTrainNrc)
+        return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeTrainNrc>)
+                             : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeTrainNrc>);
+    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeRenderNrc>)
+                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeRenderNrc>);
+}
+
+void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
+                     cudaStream_t s) {
+    dim3 grid(grid_ctas), block(threads);
+    if (mode == kModeTrainNrc) {
+        if (grid_majorant)
+            plain_trace_kernel<true, false, kModeTrainNrc><<<grid, block, smem, s>>>(p);
+        else
+            plain_trace_kernel<false, false, kModeTrainNrc><<<grid, block, 0, s>>>(p);
+    } else {
+        if (grid_majorant)
+            plain_trace_kernel<true, false, kModeRenderNrc><<<grid, block, smem, s>>>(p);
+        else
+            plain_trace_kernel<false, false, kModeRenderNrc><<<grid, block, 0, s>>>(p);
     }
 }
 

@@ -1,10 +1,16 @@
 // Launch parameters and kernel declarations of the persistent volumetric tracker.
 #pragma once
 
+#include "nrc_buffers.cuh"
 #include "vpt_device.cuh"
 #include "../../include/rtc8_vpt.h"
 
 namespace vpt {
+
+// Tracer passes (the reference's ray-generation programs).
+constexpr int kModePlain = 0;      // pathTrace: accumulate full paths
+constexpr int kModeRenderNrc = 1;  // pathTraceWithNRC: short paths ending in a cache query
+constexpr int kModeTrainNrc = 2;   // generateTrainingData: training suffixes on the training image
 
 struct Sun {
     float dir[3];
@@ -47,12 +53,21 @@ struct TraceParams {
     unsigned int* work_counter;
     unsigned long long* counters;  // lookups, vertices, samples
     unsigned int* error_flags;
+
+    // Radiance-cache passes only.
+    NrcBuffers nrc;
+    uint32_t nrc_buf;           // training buffer of this frame (nrcBufferIndex)
+    int32_t nrc_density_query;  // 1: the query's roughness slot carries density / density_coeff
 };
 
 // Majorant grids up to this many cells are staged in shared memory (32 KB).
 constexpr int kMajSmemCells = 8192;
 
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
+// Radiance-cache render (kModeRenderNrc) or training (kModeTrainNrc) pass.
+void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
+                     cudaStream_t s);
+const void* nrc_kernel_ptr(int mode, bool grid_majorant);
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
 void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int mx, int my, int mz, int factor,
                     cudaStream_t s);

@@ -16,6 +16,27 @@ from ._lib import VptFrameParams, check, ptr
 from .configs import SceneConfig, camera_for, sun_direction, volume_box
 
 
+TRAIN_BUFFER_SIZE = 131072  # VPT_NRC_TRAIN_BUFFER_SIZE
+TRAIN_PER_FRAME = 65536     # VPT_NRC_TRAIN_DATA_PER_FRAME
+
+
+class _DeviceArray:
+    """Exposes a raw device allocation through __cuda_array_interface__ (version 3)."""
+
+    def __init__(self, ptr: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def device_view(ptr: int, shape: tuple, typestr: str):
+    """A torch tensor aliasing `shape` elements of type `typestr` at device address `ptr`."""
+    import torch
+
+    if not ptr:
+        raise ValueError("null device pointer")
+    return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device="cuda")
+
+
 class Renderer:
     def __init__(self, width: int, height: int):
         self.lib = _lib.load()
@@ -162,6 +183,65 @@ class Renderer:
 
     def device_errors(self) -> int:
         return int(self.lib.vpt_get_device_errors(self.ctx))
+
+    # ------------------------------------------------------------------ radiance cache
+    # The entry points of the reference's NRC frame (renderer_main.cpp:1553-1637).
+    def nrc_buffers(self) -> _lib.VptNrcBuffers:
+        b = _lib.VptNrcBuffers()
+        check(self.lib.vpt_nrc_get_buffers(self.ctx, C.byref(b)), "vpt_nrc_get_buffers")
+        return b
+
+    def nrc_views(self) -> dict:
+        """torch tensors aliasing the context's radiance-cache buffers (no copies)."""
+        b = self.nrc_buffers()
+        n = self.width * self.height
+        cap = b.infer_capacity
+        tb = TRAIN_BUFFER_SIZE
+        return {
+            "infer_query": device_view(b.infer_query, (cap, 14), "<f4"),
+            "infer_terminal": device_view(b.infer_terminal, (n, 4), "<f4"),
+            "train_suffix": device_view(b.train_suffix, (n,), "<i4"),
+            "inferred": device_view(b.inferred, (cap, 3), "<f4"),
+            "frame_contribution": device_view(b.frame_contribution, (n, 3), "<f4"),
+            "train_query0": device_view(b.train_query[0], (tb, 14), "<f4"),
+            "train_query1": device_view(b.train_query[1], (tb, 14), "<f4"),
+            "train_target0": device_view(b.train_target[0], (tb, 3), "<f4"),
+            "train_target1": device_view(b.train_target[1], (tb, 3), "<f4"),
+            "train_vertex": device_view(b.train_vertex, (tb, 4), "<f4"),
+            "shufflers": device_view(b.shufflers, (TRAIN_PER_FRAME,), "<i4"),
+            "counters": device_view(b.counters, (16,), "<i4"),
+            "stats": device_view(b.stats, (18,), "<f4"),
+        }
+
+    def nrc_set_query_density(self, on: bool) -> None:
+        check(self.lib.vpt_nrc_set_query_density(self.ctx, int(on)), "vpt_nrc_set_query_density")
+
+    def prepare_nrc(self, buffer_index: int, offset: int, new_sequence: bool, stream: int | None = None) -> None:
+        check(self.lib.vpt_prepare_nrc(self.ctx, C.c_void_p(stream or 0), buffer_index, offset & 0xFFFFFFFF,
+                                       int(new_sequence)), "vpt_prepare_nrc")
+
+    def launch_generate_training(self, buffer_index: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_launch_generate_training(self.ctx, C.c_void_p(stream or 0), buffer_index),
+              "vpt_launch_generate_training")
+
+    def propagate(self, stream: int | None = None) -> None:
+        check(self.lib.vpt_propagate(self.ctx, C.c_void_p(stream or 0)), "vpt_propagate")
+
+    def shuffle(self, buffer_index: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_shuffle(self.ctx, C.c_void_p(stream or 0), buffer_index), "vpt_shuffle")
+
+    def launch_render_nrc(self, stream: int | None = None) -> None:
+        check(self.lib.vpt_launch_render_nrc(self.ctx, C.c_void_p(stream or 0)), "vpt_launch_render_nrc")
+
+    def accumulate_inferred(self, accum_frames: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_accumulate_inferred(self.ctx, C.c_void_p(stream or 0), accum_frames),
+              "vpt_accumulate_inferred")
+
+    def nrc_frame(self, cache, train_iterations: int, spp: int, new_sequence: bool,
+                  stream: int | None = None) -> None:
+        """One frame with the radiance cache `cache` (a :class:`rtc8_gb300.nrc.NeuralRadianceCache`)."""
+        check(self.lib.vpt_nrc_frame(self.ctx, cache.h, C.c_void_p(stream or 0), train_iterations, spp,
+                                     int(new_sequence)), "vpt_nrc_frame")
 
     _dims = (0, 0, 0)
 

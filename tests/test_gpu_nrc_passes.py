@@ -1,0 +1,285 @@
+"""GPU radiance-cache passes against the oracle, through the C ABI.
+
+The render and training passes of the tracer use the same per-pixel PCG32 streams as the
+oracle's restatement, so path decisions are compared pixel by pixel: the bar is >= 99.9% of
+pixels with the same final RNG state and the same terminal record. Records of agreeing pixels
+must match (queries and throughputs within 1e-4 relative: FP32 on both sides, no FMA
+contraction on either). Training vertices are numbered by a device atomic, so suffixes are
+compared as chains (first vertex to last). The set-up kernels run on buffers downloaded from
+the device and are compared with their restatement on the same inputs: exact for integer and
+copy work, 1e-5 relative for arithmetic, the batch average within 1e-4 (summation order).
+"""
+import numpy as np
+import pytest
+
+from oracle import orc
+from rtc8_gb300 import nrc
+from rtc8_gb300.renderer import Renderer, constant_environment, setup_scene
+
+from ._scenes import small_config_mode, small_reference_mode, volume_for
+
+pytestmark = pytest.mark.gpu
+
+DECISION_PARITY = 0.999
+
+
+def _setup(cfg, vox, env):
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg, volume=vox)
+    r.set_environment_rgb(env)
+    return r
+
+
+def _np(t):
+    return t.cpu().numpy()
+
+
+def _scene(cfg):
+    vox = volume_for(cfg)
+    env = constant_environment(cfg.env_constant if cfg.env_constant is not None else 0.5)
+    return vox, env
+
+
+@pytest.mark.parametrize("density_query", [False, True])
+def test_render_pass_matches_oracle(cuda_device, density_query):
+    import torch
+
+    cfg = small_reference_mode(size=48, n=32, sigma=60.0)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    r.nrc_set_query_density(density_query)
+    rng0 = r.rng_states().copy()
+    r.launch_render_nrc()
+    torch.cuda.synchronize()
+    v = r.nrc_views()
+    n = cfg.width * cfg.height
+    g_rng = r.rng_states()
+    g_term = _np(v["infer_terminal"])
+    g_bits = g_term[:, 3].copy().view(np.uint32)
+    g_query = _np(v["infer_query"])[:n]
+    g_fc = _np(v["frame_contribution"])
+    assert r.device_errors() == 0
+
+    sc = orc.scene_from_config(cfg, vox, env)
+    o_rng = rng0.copy()
+    o = orc.nrc_pass(sc, o_rng, 1, cfg.width, cfg.height, density_query=density_query)
+    same = (g_rng == o_rng) & (g_bits == o["terminal_bits"])
+    assert same.mean() >= DECISION_PARITY, f"identical pixels {same.mean():.5f}"
+    has_q = same & ((o["terminal_bits"] & 1) == 1)
+    assert has_q.sum() > n // 10  # a good share of paths ends with a cache query
+    assert (o["terminal_bits"] >> 1).max() > 2
+    np.testing.assert_allclose(g_term[same, :3], o["terminal_tp"][same], rtol=1e-4, atol=1e-7)
+    np.testing.assert_allclose(g_query[has_q], o["infer_query"][has_q], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(g_fc[same], o["frame_contribution"][same], rtol=1e-4, atol=1e-7)
+    if density_query:
+        assert g_query[has_q, 7].max() > 0.05
+    r.close()
+
+
+def _train_pass(cfg, vox, env, offset, density_query=False):
+    import torch
+
+    r = _setup(cfg, vox, env)
+    r.nrc_set_query_density(density_query)
+    rng0 = r.rng_states().copy()
+    r.prepare_nrc(0, offset, True)
+    r.launch_generate_training(0)
+    torch.cuda.synchronize()
+    return r, rng0
+
+
+@pytest.mark.parametrize("cfg_kind", ["reference", "config"])
+def test_training_pass_matches_oracle(cuda_device, cfg_kind):
+    if cfg_kind == "reference":
+        cfg = small_reference_mode(size=64, n=32, sigma=60.0)
+    else:
+        cfg = small_config_mode(size=64, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=0)
+    vox, env = _scene(cfg)
+    offset = 2654435761
+    r, rng0 = _train_pass(cfg, vox, env, offset)
+    v = r.nrc_views()
+    cnt = _np(v["counters"]).view(np.uint32)
+    tw, th = int(cnt[2]), int(cnt[3])
+    assert (tw, th) == (cfg.width // 4, cfg.height // 4)
+    assert cnt[6] == offset and cnt[7] == tw * th
+    ni = tw * th
+    g_suffix = _np(v["train_suffix"]).view(np.uint32)[:ni]
+    g_vert = _np(v["train_vertex"])
+    g_vbits = g_vert[:, 3].copy().view(np.uint32)
+    g_query = _np(v["train_query0"])
+    g_target = _np(v["train_target0"])
+    g_iq = _np(v["infer_query"])[:ni]
+    g_rng = r.rng_states()
+    assert r.device_errors() == 0
+
+    sc = orc.scene_from_config(cfg, vox, env)
+    o_rng = rng0.copy()
+    o = orc.nrc_pass(sc, o_rng, 2, tw, th, unbiased_offset=offset)
+    g_chains = orc.suffix_chains(g_suffix, g_vbits, ni)
+    o_chains = orc.suffix_chains(o["train_suffix"], o["train_bits"], ni)
+    # pixel (px, py) of the training image uses the full image's stream py * width + px
+    pix = np.array([(i // tw) * cfg.width + i % tw for i in range(ni)])
+    same = (g_rng[pix] == o_rng[pix]) & ((g_suffix >> 22) == (o["train_suffix"] >> 22))
+    same &= np.array([len(a) == len(b) for a, b in zip(g_chains, o_chains)])
+    assert same.mean() >= DECISION_PARITY, f"identical suffixes {same.mean():.5f}"
+    if same.all():
+        assert int(cnt[0]) == int(o["num_train"][0])
+    assert sum(len(c) for c in o_chains) > ni // 4 and max(len(c) for c in o_chains) > 2
+    unb = (o["train_suffix"] >> 31) & 1
+    assert 0 < unb.sum() <= ni // 16 + tw + th
+    for i in np.nonzero(same)[0]:
+        for gi, oi in zip(g_chains[i], o_chains[i]):
+            assert (g_vbits[gi] >> 22) == (o["train_bits"][oi] >> 22)
+            np.testing.assert_allclose(g_vert[gi, :3], o["train_local_tp"][oi], rtol=1e-4, atol=1e-7)
+            np.testing.assert_allclose(g_query[gi], o["train_query"][oi], rtol=1e-4, atol=1e-5)
+            np.testing.assert_allclose(g_target[gi], o["train_target"][oi], rtol=1e-4, atol=1e-6)
+        if (o["train_suffix"][i] >> 22) & 1:
+            np.testing.assert_allclose(g_iq[i], o["infer_query"][i], rtol=1e-4, atol=1e-5)
+    r.close()
+
+
+def test_propagate_shuffle_accumulate_match_oracle(cuda_device):
+    """The three set-up kernels on the buffers of a real training pass and render pass, with
+    random cache predictions, against their restatement on the same inputs."""
+    import torch
+
+    cfg = small_reference_mode(size=64, n=32, sigma=60.0)
+    vox, env = _scene(cfg)
+    r, _ = _train_pass(cfg, vox, env, 7)
+    v = r.nrc_views()
+    cnt = _np(v["counters"]).view(np.uint32).copy()
+    ni = int(cnt[7])
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    v["inferred"].copy_(torch.rand(v["inferred"].shape, device="cuda", generator=gen) * 2 - 0.5)
+    torch.cuda.synchronize()
+    before = {k: _np(v[k]).copy() for k in ("train_suffix", "inferred", "infer_query", "train_vertex",
+                                            "train_query0", "train_target0", "shufflers", "stats")}
+    # propagate
+    r.propagate()
+    torch.cuda.synchronize()
+    tgt = before["train_target0"].copy()
+    orc.nrc_propagate(ni, before["train_suffix"].view(np.uint32), before["inferred"], before["infer_query"],
+                      before["train_vertex"], before["train_query0"], tgt, 0.0)
+    np.testing.assert_allclose(_np(v["train_target0"]), tgt, rtol=1e-5, atol=1e-7)
+    assert np.abs(tgt - before["train_target0"]).max() > 0  # propagation changed targets
+    # shuffle
+    prop_q, prop_t = _np(v["train_query0"]).copy(), _np(v["train_target0"]).copy()
+    r.shuffle(0)
+    torch.cuda.synchronize()
+    sh = before["shufflers"].view(np.uint32).copy()
+    stats = before["stats"].copy()
+    q1 = np.zeros((orc.TRAIN_BUFFER_SIZE, 14), np.float32)
+    t1 = np.zeros((orc.TRAIN_BUFFER_SIZE, 3), np.float32)
+    writers = orc.nrc_shuffle(int(cnt[0]), stats[0:9], sh, prop_q, prop_t, q1, t1, 0.0)
+    assert np.array_equal(_np(v["shufflers"]).view(np.uint32), sh)
+    one = writers == 1
+    assert one.mean() > 0.3
+    np.testing.assert_array_equal(_np(v["train_query1"])[:orc.TRAIN_PER_FRAME][one], q1[:orc.TRAIN_PER_FRAME][one])
+    np.testing.assert_array_equal(_np(v["train_target1"])[:orc.TRAIN_PER_FRAME][one], t1[:orc.TRAIN_PER_FRAME][one])
+    g_stats = _np(v["stats"])
+    np.testing.assert_array_equal(g_stats[0:6], stats[0:6])
+    np.testing.assert_allclose(g_stats[6:9], stats[6:9], rtol=1e-4)
+    # render pass, random predictions, accumulate (as sample 0 and sample 1)
+    r.launch_render_nrc()
+    v["inferred"].copy_(torch.rand(v["inferred"].shape, device="cuda", generator=gen))
+    torch.cuda.synchronize()
+    n = cfg.width * cfg.height
+    term, fc = _np(v["infer_terminal"]).copy(), _np(v["frame_contribution"]).copy()
+    inf, iq = _np(v["inferred"]).copy(), _np(v["infer_query"]).copy()
+    r.reset_accumulation()
+    r.accumulate_inferred(0)
+    r.accumulate_inferred(1)
+    s_g, _ = r.download_sum()
+    m_g = r.download_mean()
+    s_o = np.zeros((n, 3), np.float64)
+    m_o = np.zeros((n, 3), np.float32)
+    orc.nrc_accumulate(n, term, fc, inf, iq, 0.0, 0, s_o, m_o)
+    orc.nrc_accumulate(n, term, fc, inf, iq, 0.0, 1, s_o, m_o)
+    np.testing.assert_allclose(s_g.reshape(n, 3), s_o, rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(m_g.reshape(n, 3), m_o, rtol=1e-6, atol=1e-9)
+    assert r.device_errors() == 0
+    r.close()
+
+
+def test_prepare_adapts_training_image(cuda_device):
+    """prepareNRC's adaptive size: from numTrainingData of the previous buffer."""
+    import torch
+
+    cfg = small_reference_mode(size=64, n=32)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    r.prepare_nrc(0, 1, True)
+    torch.cuda.synchronize()
+    v = r.nrc_views()
+    for prev_count in (0, 16384, 65536, 200000):
+        cnt = _np(v["counters"]).view(np.uint32).copy()
+        cnt[0] = prev_count
+        cnt[2], cnt[3] = 16, 12
+        v["counters"].copy_(torch.from_numpy(cnt.view(np.int32)).cuda())
+        r.prepare_nrc(1, 99, False)
+        torch.cuda.synchronize()
+        g = _np(v["counters"]).view(np.uint32)
+        o = cnt.copy()
+        stats = np.zeros(18, np.float32)
+        suffix = np.zeros(cfg.width * cfg.height, np.uint32)
+        orc.nrc_prepare(o, stats, suffix, cfg.width, cfg.height, 1, 99, False)
+        assert np.array_equal(g[:8], o[:8]), (prev_count, g[:8], o[:8])
+    assert np.all(_np(v["train_suffix"]).view(np.uint32) == orc.INVALID_VERTEX)
+    r.close()
+
+
+def _blocks(img, k=16):
+    h, w, _ = img.shape
+    return img.reshape(h // k, k, w // k, k, 3).mean(axis=(1, 3))
+
+
+def _rel(a, b):
+    return float(np.mean((a - b) ** 2) / np.mean(b ** 2))
+
+
+def test_nrc_frame_loop_gain_over_truncated_paths(cuda_device):
+    """The composite frame call runs the reference's loop with the tcgen05 cache. With the
+    trained cache the image agrees with the plain estimate of the same scene (block averages of
+    16 x 16 pixels, so that noise does not dominate); the same short render paths without the
+    network (predictions forced to 0) are far darker: what the network adds is the radiance of
+    the truncated path tails."""
+    import torch
+
+    cfg = small_config_mode(size=128, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=0)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    net_cfg = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=net_cfg)
+    r.nrc_set_query_density(True)
+    r.nrc_frame(cache, 8, 1, True)
+    for _ in range(40):
+        r.nrc_frame(cache, 1, 1, False)
+    torch.cuda.synchronize()
+    assert r.device_errors() == 0 and cache.device_errors() == 0
+    assert cache.lib.nrc_step_count(cache.h) == 4 * 48
+    r.reset_accumulation()
+    for _ in range(64):
+        r.nrc_frame(cache, 1, 1, False)
+    img_nrc = r.image()
+    assert np.all(np.isfinite(img_nrc))
+    # the same render passes with the cache's predictions replaced by 0
+    v = r.nrc_views()
+    r.reset_accumulation()
+    for i in range(64):
+        r.launch_render_nrc()
+        v["inferred"].zero_()
+        r.accumulate_inferred(i)
+    img_trunc = r.image()
+    p = Renderer(cfg.width, cfg.height)
+    setup_scene(p, cfg, volume=vox)
+    p.set_environment_rgb(env)
+    p.launch_plain(256)
+    img_plain = p.image()
+    rel_nrc = _rel(_blocks(img_nrc), _blocks(img_plain))
+    rel_trunc = _rel(_blocks(img_trunc), _blocks(img_plain))
+    assert rel_nrc < 0.02 and rel_nrc < 0.25 * rel_trunc, (rel_nrc, rel_trunc)
+    assert r.device_errors() == 0
+    cache.finalize()
+    r.close()
+    p.close()
