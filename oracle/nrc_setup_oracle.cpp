@@ -84,12 +84,12 @@ void orc_nrc_propagate(uint32_t num_suffixes, const uint32_t* train_suffix, cons
     for (uint32_t i = 0; i < num_suffixes; ++i) {
         const uint32_t term = train_suffix[i];
         uint32_t idx = term & ORC_NRC_INVALID_VERTEX;
-        if (idx == ORC_NRC_INVALID_VERTEX) continue;
+        if (idx >= ORC_NRC_TRAIN_BUFFER_SIZE) continue;
         float contribution[3] = {0, 0, 0};
         if ((term >> 22) & 1u)
             terminal_radiance(inferred + 3 * static_cast<size_t>(i), infer_query + 14 * static_cast<size_t>(i),
                               radiance_scale, contribution);
-        for (uint32_t guard = 0; idx != ORC_NRC_INVALID_VERTEX && guard < ORC_NRC_TRAIN_BUFFER_SIZE; ++guard) {
+        for (uint32_t guard = 0; idx < ORC_NRC_TRAIN_BUFFER_SIZE && guard < ORC_NRC_TRAIN_BUFFER_SIZE; ++guard) {
             const float* v = vertex + 4 * static_cast<size_t>(idx);
             float* target = train_target0 + 3 * static_cast<size_t>(idx);
             const float* q = train_query0 + 14 * static_cast<size_t>(idx);

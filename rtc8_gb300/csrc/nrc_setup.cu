@@ -65,7 +65,7 @@ __global__ void propagate_kernel(NrcBuffers b, float radiance_scale) {
          i += gridDim.x * blockDim.x) {
         uint32_t term = b.train_suffix[i];
         uint32_t idx = term & kInvalidVertex;
-        if (idx == kInvalidVertex) continue;
+        if (idx >= kTrainBufferSize) continue;  // no vertex (kInvalidVertex) or a corrupt link
         RGB contribution = rgb(0, 0, 0);
         if ((term >> 22) & 1u) {
             contribution = max0(load_rgb(b.inferred + 3 * static_cast<size_t>(i)));
@@ -73,7 +73,7 @@ __global__ void propagate_kernel(NrcBuffers b, float radiance_scale) {
             contribution = contribution * reflectance(b.infer_query + kQueryFloats * static_cast<size_t>(i));
         }
         // Walk the suffix backwards; vertex indices decrease along it, so the walk ends.
-        for (uint32_t guard = 0; idx != kInvalidVertex && guard < kTrainBufferSize; ++guard) {
+        for (uint32_t guard = 0; idx < kTrainBufferSize && guard < kTrainBufferSize; ++guard) {
             const TrainVertexInfo vi = b.train_vertex[idx];
             float* target = b.train_target[0] + 3 * static_cast<size_t>(idx);
             RGB indirect = rgb(vi.local_tp[0], vi.local_tp[1], vi.local_tp[2]) * contribution;

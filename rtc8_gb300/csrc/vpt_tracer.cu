@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
     uint32_t img_w = static_cast<uint32_t>(P.width), img_h = static_cast<uint32_t>(P.height);
     uint32_t num_items = num_pixels;
     if constexpr (kTrain) {
-        img_w = P.nrc.counters[2 + 2 * P.nrc_buf];
-        img_h = P.nrc.counters[3 + 2 * P.nrc_buf];
+        img_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
+        img_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
         num_items = min(img_w * img_h, num_pixels);
     }
     const V3 wmin = bmin, wmax = bmax;
