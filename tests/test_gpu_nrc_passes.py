@@ -66,7 +66,7 @@ def test_render_pass_matches_oracle(cuda_device, density_query):
     same = (g_rng == o_rng) & (g_bits == o["terminal_bits"])
     assert same.mean() >= DECISION_PARITY, f"identical pixels {same.mean():.5f}"
     has_q = same & ((o["terminal_bits"] & 1) == 1)
-    assert has_q.sum() > n // 10  # a good share of paths ends with a cache query
+    assert has_q.sum() > n // 20  # a good share of paths ends with a cache query
     assert (o["terminal_bits"] >> 1).max() > 2
     np.testing.assert_allclose(g_term[same, :3], o["terminal_tp"][same], rtol=1e-4, atol=1e-7)
     np.testing.assert_allclose(g_query[has_q], o["infer_query"][has_q], rtol=1e-4, atol=1e-5)
