@@ -240,6 +240,8 @@ typedef struct VptNrcBuffers {
     float* stats;                /* per buffer: targetMinMax (min rgb, max rgb), targetAvg */
     uint32_t infer_capacity;
     uint32_t buffer_index;       /* nrcBufferIndex of the last training iteration */
+    uint32_t render_spp;         /* sample slots per pixel of the render-pass buffers (records of
+                                    sample s of pixel p at s * w * h + p) */
 } VptNrcBuffers;
 
 /* Allocates the cache buffers (once per context; the shufflers start from the LCG seeded with
@@ -263,12 +265,23 @@ int vpt_shuffle(VptContext* ctx, void* stream, uint32_t buffer_index);
 /* pathTraceWithNRC on the full image: one sample per pixel. */
 int vpt_launch_render_nrc(VptContext* ctx, void* stream);
 /* accumulateInferredRadianceValues (nrc_set_up_kernels.cu:176-219) as sample number
- * `accum_frames` of the FP32 running mean, also added to the FP64 sums. */
+ * `accum_frames` of the FP32 running mean, also added to the FP64 sums; the context's sample
+ * count becomes accum_frames + 1. */
 int vpt_accumulate_inferred(VptContext* ctx, void* stream, uint32_t accum_frames);
+/* GB300 form of the render passes of one frame: `spp` samples per pixel in ONE persistent launch
+ * on sample-parallel streams (VptFrameParams.rng_stream_mode must be 1; the reference runs one
+ * launch per sample on per-pixel streams, renderer_main.cpp:1617-1637). The render-pass buffers
+ * grow to `spp` slots per pixel (the first call with a larger spp synchronises the device). */
+int vpt_launch_render_nrc_batch(VptContext* ctx, void* stream, uint32_t spp);
+/* Accumulation of the `spp` samples of a batched render pass: FP64 sums, and the mean as the sum
+ * over accum_frames + spp samples (which becomes the context's sample count). */
+int vpt_accumulate_inferred_batch(VptContext* ctx, void* stream, uint32_t accum_frames, uint32_t spp);
 /* One frame of renderer_main.cpp:1553-1637 with the cache `nrc` (an NrcHandle* of
  * rtc8_nrc.h): `train_iterations` x (prepareNRC with the next offset of mt19937(72139121) and
  * isNewSequence = new_sequence, training pass, inference on its queries, propagation, shuffle,
- * 4 training steps of 16384 records), then `spp` x (render pass, inference, accumulation).
+ * 4 training steps of 16384 records), then `spp` x (render pass, inference, accumulation), or,
+ * with sample-parallel streams (rng_stream_mode 1), one batched render pass of `spp` samples,
+ * one inference and one accumulation.
  * Accumulation continues the context's (the reference restarts it every frame: call
  * vpt_reset_accumulation first for that). Nothing is synchronised. */
 int vpt_nrc_frame(VptContext* ctx, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,

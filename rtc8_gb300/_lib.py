@@ -109,6 +109,8 @@ _VPT = {
     "vpt_shuffle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vpt_launch_render_nrc": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_accumulate_inferred": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_launch_render_nrc_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vpt_accumulate_inferred_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
     "vpt_nrc_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
 }
 
@@ -129,6 +131,7 @@ class VptNrcBuffers(C.Structure):
         ("stats", C.c_void_p),
         ("infer_capacity", C.c_uint32),
         ("buffer_index", C.c_uint32),
+        ("render_spp", C.c_uint32),
     ]
 
 

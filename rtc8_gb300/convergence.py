@@ -1,0 +1,137 @@
+"""Equal-error comparison of the radiance-cache renderer with the plain path tracer.
+
+Both estimators render the same scene; after every chunk of work the accumulated image is
+compared with an FP64-accumulated high-spp image of the plain tracer made from independent
+RNG streams (the "oracle image"). The error measure is the relative MSE
+
+    relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 0.01)
+
+(the 0.01 keeps dark pixels from dominating). Time is GPU time of the estimator's own launches
+(CUDA events on its stream), excluding the error evaluation. The radiance-cache estimator runs
+the reference's frame loop (renderer/renderer_main.cpp:1553-1637): every frame trains the cache
+on that frame's training suffixes and renders one sample per pixel; the first frame trains
+eight times (a new sequence).
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from .configs import SceneConfig
+from .renderer import Renderer, setup_scene
+
+REL_EPS = 1e-2
+
+
+def rel_mse(img, ref) -> float:
+    import torch
+
+    a = torch.as_tensor(img, dtype=torch.float64)
+    b = torch.as_tensor(ref, dtype=torch.float64)
+    return float(((a - b) ** 2 / (b * b + REL_EPS)).mean())
+
+
+def oracle_image(cfg: SceneConfig, spp: int, seed_offset: int = 1, chunk: int = 256, stream=None) -> np.ndarray:
+    """FP64-accumulated plain image with `spp` samples per pixel from RNG streams independent of
+    the configuration's own (seed + seed_offset)."""
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg)
+    r.seed_rng(cfg.rng_seed + seed_offset)
+    done = 0
+    while done < spp:
+        n = min(chunk, spp - done)
+        r.launch_plain(n, stream)
+        done += n
+    r.synchronize(stream)
+    img = r.image()
+    r.close()
+    return img
+
+
+def _timed(stream, fn) -> float:
+    import torch
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / 1000.0
+
+
+def plain_curve(cfg: SceneConfig, ref: np.ndarray, target: float, chunk_spp: int = 16, max_spp: int = 16384,
+                time_budget: float = 60.0) -> dict:
+    """relMSE of the plain tracer after each chunk of `chunk_spp` samples per pixel."""
+    import torch
+
+    s = torch.cuda.Stream()
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg)
+    curve, t, spp, reached = [], 0.0, 0, None
+    wall0 = time.perf_counter()
+    while spp < max_spp and time.perf_counter() - wall0 < time_budget:
+        t += _timed(s, lambda: r.launch_plain(chunk_spp, s.cuda_stream))
+        spp += chunk_spp
+        e = rel_mse(r.image(), ref)
+        curve.append((spp, t, e))
+        if e <= target and reached is None:
+            reached = {"spp": spp, "seconds": t}
+            break
+    r.close()
+    return {"curve": curve, "reached": reached}
+
+
+def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None, spp_per_frame: int = 8,
+              eval_every: int = 1, max_frames: int = 4096, time_budget: float = 60.0,
+              query_density: bool = True) -> dict:
+    """relMSE of the radiance-cache renderer after every `eval_every` frames of `spp_per_frame`
+    samples per pixel (the reference renders 8 samples per frame, renderer_main.cpp:359)."""
+    import torch
+
+    from . import nrc
+
+    s = torch.cuda.Stream()
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg)
+    r.nrc_set_query_density(query_density)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=net_config or nrc.default_config(nrc.NRC_ENCODING_VOLUME))
+    curve, t, frames, reached = [], 0.0, 0, None
+    t += _timed(s, lambda: r.nrc_frame(cache, 8, spp_per_frame, True, s.cuda_stream))
+    frames = 1
+    wall0 = time.perf_counter()
+    while frames < max_frames and time.perf_counter() - wall0 < time_budget:
+        def run():
+            for _ in range(eval_every):
+                r.nrc_frame(cache, 1, spp_per_frame, False, s.cuda_stream)
+        t += _timed(s, run)
+        frames += eval_every
+        e = rel_mse(r.image(), ref)
+        curve.append((frames * spp_per_frame, t, e))
+        if e <= target and reached is None:
+            reached = {"frames": frames, "spp": frames * spp_per_frame, "seconds": t}
+            break
+    errors = r.device_errors() | cache.device_errors()
+    best = min(c[2] for c in curve) if curve else math.inf
+    r.close()
+    cache.finalize()
+    return {"curve": curve, "reached": reached, "best_rel_mse": best, "device_errors": errors}
+
+
+def compare(cfg: SceneConfig, target: float = 1e-3, oracle_spp: int = 16384, time_budget: float = 60.0) -> dict:
+    """Time to reach relMSE <= target for both estimators on `cfg`."""
+    ref = oracle_image(cfg, oracle_spp)
+    plain = plain_curve(cfg, ref, target, time_budget=time_budget)
+    cache = nrc_curve(cfg, ref, target, time_budget=time_budget)
+    out = {"target_rel_mse": target, "oracle_spp": oracle_spp, "rel_mse_eps": REL_EPS,
+           "plain": {"reached": plain["reached"], "last": plain["curve"][-1] if plain["curve"] else None},
+           "nrc": {"reached": cache["reached"], "last": cache["curve"][-1] if cache["curve"] else None,
+                   "best_rel_mse": cache["best_rel_mse"], "device_errors": cache["device_errors"]}}
+    if plain["reached"] and cache["reached"]:
+        out["speedup"] = plain["reached"]["seconds"] / cache["reached"]["seconds"]
+    else:
+        out["speedup"] = None
+    out["curves"] = {"plain": plain["curve"], "nrc": cache["curve"]}
+    return out

@@ -35,13 +35,14 @@ __host__ __device__ __forceinline__ uint32_t pack_suffix(uint32_t prev, uint32_t
 struct NrcBuffers {
     int32_t width = 0, height = 0;   // render image
     uint32_t max_train_suffixes = 0; // = width * height (renderer_main.cpp:113)
-    uint32_t infer_capacity = 0;     // roundUp(width * height, 128)
+    uint32_t infer_capacity = 0;     // roundUp(width * height * render_spp, 128)
+    uint32_t render_spp = 1;         // sample slots per pixel of the render-pass buffers
 
     float* infer_query = nullptr;        // infer_capacity * 14
-    TerminalInfo* infer_terminal = nullptr;  // width * height
+    TerminalInfo* infer_terminal = nullptr;  // width * height * render_spp
     uint32_t* train_suffix = nullptr;    // max_train_suffixes
     float* inferred = nullptr;           // infer_capacity * 3
-    float* frame_contribution = nullptr; // width * height * 3
+    float* frame_contribution = nullptr; // width * height * render_spp * 3
     float* train_query[2] = {nullptr, nullptr};   // kTrainBufferSize * 14
     float* train_target[2] = {nullptr, nullptr};  // kTrainBufferSize * 3
     TrainVertexInfo* train_vertex = nullptr;      // kTrainBufferSize
@@ -58,7 +59,7 @@ struct NrcBuffers {
 void nrc_prepare(const NrcBuffers& b, uint32_t buf, uint32_t offset, bool new_sequence, cudaStream_t s);
 void nrc_propagate(const NrcBuffers& b, float radiance_scale, cudaStream_t s);
 void nrc_shuffle(const NrcBuffers& b, uint32_t buf, float radiance_scale, cudaStream_t s);
-void nrc_accumulate(const NrcBuffers& b, float radiance_scale, uint32_t accum_frames, double* sum, float* mean,
-                    unsigned int* err, cudaStream_t s);
+void nrc_accumulate(const NrcBuffers& b, float radiance_scale, uint32_t accum_frames, uint32_t spp, bool from_sums,
+                    double* sum, float* mean, unsigned int* err, cudaStream_t s);
 
 }  // namespace vpt

@@ -85,15 +85,49 @@ int ensure_nrc(VptContext* c) {
 // radianceScale of the frame (renderer_shared.h:160); <= 0 = off.
 float radiance_scale(const VptContext* c) { return c->frame.radiance_scale > 0 ? c->frame.radiance_scale : 0.0f; }
 
-// Launch of a radiance-cache pass of the persistent tracker.
-int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf) {
+// Grows the render-pass buffers (queries, terminals, predictions, contributions) to `spp`
+// sample slots per pixel. Waits for the device before freeing the old buffers.
+int ensure_render_slots(VptContext* c, uint32_t spp) {
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    vpt::NrcBuffers& b = *c->nrc;
+    if (spp <= b.render_spp) return VPT_OK;
+    const size_t slots = static_cast<size_t>(c->width) * c->height * spp;
+    if (slots >= (1ull << 31)) return fail(VPT_ERR_INVALID_ARGUMENT, "too many render-pass samples in one launch");
+    NRCP_CUDA(cudaDeviceSynchronize());
+    free_ptr(b.infer_query);
+    free_ptr(b.infer_terminal);
+    free_ptr(b.inferred);
+    free_ptr(b.frame_contribution);
+    const uint32_t cap = static_cast<uint32_t>((slots + 127) / 128 * 128);
+    cudaError_t e = alloc_zero(&b.infer_query, static_cast<size_t>(cap) * vpt::kQueryFloats);
+    if (e == cudaSuccess) e = alloc_zero(&b.infer_terminal, slots);
+    if (e == cudaSuccess) e = alloc_zero(&b.inferred, static_cast<size_t>(cap) * 3);
+    if (e == cudaSuccess) e = alloc_zero(&b.frame_contribution, slots * 3);
+    if (e != cudaSuccess) {
+        c->release_nrc();
+        return fail(VPT_ERR_OUT_OF_MEMORY, std::string("render-pass buffers: ") + cudaGetErrorString(e));
+    }
+    b.infer_capacity = cap;
+    b.render_spp = spp;
+    return VPT_OK;
+}
+
+// Launch of a radiance-cache pass of the persistent tracker: the training pass or a render pass
+// of one sample per pixel on the per-pixel streams (stream_mode 0), or a render pass of `spp`
+// samples per pixel on sample-parallel streams (stream_mode 1).
+int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0) {
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;
     if ((rc = vpt::fill_trace_params(c, &tp))) return rc;
-    tp.spp = 1;
+    tp.spp = spp;
     tp.accum_base = 0;
-    tp.stream_mode = 0;
+    tp.stream_mode = stream_mode;
+    if (stream_mode == 1) {
+        if ((rc = vpt::upload_sample_jumps(c, c->stream_samples, spp, s))) return rc;
+        tp.sample_jumps = c->d_jumps;
+    }
     tp.park_threshold = c->park_threshold;
     tp.nrc = *c->nrc;
     tp.nrc_buf = buf;
@@ -109,6 +143,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf) {
     const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj), smem);
     vpt::launch_nrc_pass(tp, mode, grid_maj, ctas, threads, smem, s);
     NRCP_CUDA(cudaGetLastError());
+    if (stream_mode == 1) c->stream_samples += spp;
     return VPT_OK;
 }
 
@@ -161,6 +196,7 @@ int vpt_nrc_get_buffers(VptContext* c, VptNrcBuffers* out) {
     out->counters = b.counters;
     out->stats = b.stats;
     out->infer_capacity = b.infer_capacity;
+    out->render_spp = b.render_spp;
     out->buffer_index = c->nrc_buf_index;
     return VPT_OK;
 }
@@ -212,9 +248,31 @@ int vpt_accumulate_inferred(VptContext* c, void* stream, uint32_t accum_frames) 
     if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_accumulate_inferred: null context");
     int rc = ensure_nrc(c);
     if (rc) return rc;
-    vpt::nrc_accumulate(*c->nrc, radiance_scale(c), accum_frames, c->d_sum, c->d_mean, c->d_err,
+    vpt::nrc_accumulate(*c->nrc, radiance_scale(c), accum_frames, 1, false, c->d_sum, c->d_mean, c->d_err,
                         static_cast<cudaStream_t>(stream));
     NRCP_CUDA(cudaGetLastError());
+    c->accum_samples = accum_frames + 1;
+    return VPT_OK;
+}
+
+int vpt_launch_render_nrc_batch(VptContext* c, void* stream, uint32_t spp) {
+    if (!c || spp == 0) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_launch_render_nrc_batch: bad arguments");
+    if (c->has_frame && c->frame.rng_stream_mode != 1)
+        return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_launch_render_nrc_batch needs sample-parallel streams");
+    int rc = ensure_render_slots(c, spp);
+    if (rc) return rc;
+    return launch_pass(c, static_cast<cudaStream_t>(stream), vpt::kModeRenderNrc, 0, spp, 1);
+}
+
+int vpt_accumulate_inferred_batch(VptContext* c, void* stream, uint32_t accum_frames, uint32_t spp) {
+    if (!c || spp == 0) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_accumulate_inferred_batch: bad arguments");
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    if (spp > c->nrc->render_spp) return fail(VPT_ERR_INVALID_ARGUMENT, "more samples than render-pass slots");
+    vpt::nrc_accumulate(*c->nrc, radiance_scale(c), accum_frames, spp, true, c->d_sum, c->d_mean, c->d_err,
+                        static_cast<cudaStream_t>(stream));
+    NRCP_CUDA(cudaGetLastError());
+    c->accum_samples = accum_frames + spp;
     return VPT_OK;
 }
 
@@ -245,12 +303,20 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
                 return fail(VPT_ERR_CUDA, std::string("nrc_train: ") + nrc_last_error());
         }
     }
+    if (spp == 0) return VPT_OK;
+    if (c->frame.rng_stream_mode == 1) {
+        // All samples of the frame in one render pass on sample-parallel streams, one inference
+        // over every sample's query, one accumulation.
+        if ((rc = vpt_launch_render_nrc_batch(c, stream, spp))) return rc;
+        if (nrc_infer(net, stream, b.infer_query, npix * spp, b.inferred))
+            return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
+        return vpt_accumulate_inferred_batch(c, stream, c->accum_samples, spp);
+    }
     for (uint32_t i = 0; i < spp; ++i) {
         if ((rc = vpt_launch_render_nrc(c, stream))) return rc;
         if (nrc_infer(net, stream, b.infer_query, npix, b.inferred))
             return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
         if ((rc = vpt_accumulate_inferred(c, stream, c->accum_samples))) return rc;
-        ++c->accum_samples;
     }
     return VPT_OK;
 }

@@ -91,75 +91,131 @@ __device__ __forceinline__ bool all_finite_query(const float* q) {
     return ok;
 }
 
-// nrc_set_up_kernels.cu:88-174 (one thread per slot of the 2^16-sample training batch).
-__global__ void shuffle_kernel(NrcBuffers b, uint32_t buf, float radiance_scale) {
+// nrc_set_up_kernels.cu:88-174 (one thread per slot of the 2^16-sample training batch). The batch
+// statistics are reduced per block first (warp shuffles, then shared memory), so each block
+// issues one atomic per statistic, as the reference's block-level atomics do (:132-150).
+constexpr int kShuffleThreads = 256;
+__global__ void __launch_bounds__(kShuffleThreads) shuffle_kernel(NrcBuffers b, uint32_t buf, float radiance_scale) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kNumTrainingDataPerFrame) return;
-    const uint32_t num = b.counters[buf];
-    if (num > 0) {
+    const bool active = i < kNumTrainingDataPerFrame;
+    const uint32_t num = b.counters[buf];  // uniform over the grid
+    if (num == 0) {
+        if (!active) return;
+#pragma unroll
+        for (int k = 0; k < kQueryFloats; ++k) b.train_query[1][kQueryFloats * static_cast<size_t>(i) + k] = 0.0f;
+        store_rgb(b.train_target[1] + 3 * static_cast<size_t>(i), rgb(0, 0, 0));
+        return;
+    }
+    // Neutral values for threads beyond the batch (none with the exact grid used below).
+    RGB target = rgb(0, 0, 0);
+    RGB tmin = rgb(INFINITY, INFINITY, INFINITY), tmax = rgb(-INFINITY, -INFINITY, -INFINITY);
+    RGB tavg = rgb(0, 0, 0);
+    uint32_t dst = 0;
+    float q[kQueryFloats];
+    if (active) {
         // renderer_shared.h:92-109: state = (state * 1103515245 + 12345) mod 2^31 (u32 arithmetic).
         uint32_t st = b.shufflers[i];
         st = (st * 1103515245u + 12345u) % (1u << 31);
         b.shufflers[i] = st;
-        const uint32_t dst = st % kNumTrainingDataPerFrame;
+        dst = st % kNumTrainingDataPerFrame;
         const uint32_t src = i % num;
-        float q[kQueryFloats];
 #pragma unroll
         for (int k = 0; k < kQueryFloats; ++k) q[k] = b.train_query[0][kQueryFloats * static_cast<size_t>(src) + k];
-        RGB target = load_rgb(b.train_target[0] + 3 * static_cast<size_t>(src));
+        target = load_rgb(b.train_target[0] + 3 * static_cast<size_t>(src));
         if (!all_finite_query(q)) {
 #pragma unroll
             for (int k = 0; k < kQueryFloats; ++k) q[k] = 0.0f;
         }
         if (!all_nonneg_finite(target)) target = rgb(0, 0, 0);
-        // Batch statistics (targetMinMax / targetAvg): non-negative floats order like their bits.
-        float* s = b.stats + 9 * buf;
-        atomicMin(reinterpret_cast<unsigned int*>(s + 0), __float_as_uint(target.r));
-        atomicMin(reinterpret_cast<unsigned int*>(s + 1), __float_as_uint(target.g));
-        atomicMin(reinterpret_cast<unsigned int*>(s + 2), __float_as_uint(target.b));
-        atomicMax(reinterpret_cast<int*>(s + 3), __float_as_int(target.r));
-        atomicMax(reinterpret_cast<int*>(s + 4), __float_as_int(target.g));
-        atomicMax(reinterpret_cast<int*>(s + 5), __float_as_int(target.b));
-        atomicAdd(s + 6, target.r / kNumTrainingDataPerFrame);
-        atomicAdd(s + 7, target.g / kNumTrainingDataPerFrame);
-        atomicAdd(s + 8, target.b / kNumTrainingDataPerFrame);
-        if (radiance_scale > 0) target = target * radiance_scale;
-        target = rgb(fminf(target.r, 1e6f), fminf(target.g, 1e6f), fminf(target.b, 1e6f));
-#pragma unroll
-        for (int k = 0; k < kQueryFloats; ++k) b.train_query[1][kQueryFloats * static_cast<size_t>(dst) + k] = q[k];
-        store_rgb(b.train_target[1] + 3 * static_cast<size_t>(dst), target);
-    } else {
-#pragma unroll
-        for (int k = 0; k < kQueryFloats; ++k) b.train_query[1][kQueryFloats * static_cast<size_t>(i) + k] = 0.0f;
-        store_rgb(b.train_target[1] + 3 * static_cast<size_t>(i), rgb(0, 0, 0));
+        tmin = tmax = target;
+        tavg = rdiv(target, static_cast<float>(kNumTrainingDataPerFrame));
     }
+    // Batch statistics (targetMinMax / targetAvg).
+    float v[9] = {tmin.r, tmin.g, tmin.b, tmax.r, tmax.g, tmax.b, tavg.r, tavg.g, tavg.b};
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fminf(v[c], __shfl_xor_sync(0xffffffffu, v[c], off));
+            v[3 + c] = fmaxf(v[3 + c], __shfl_xor_sync(0xffffffffu, v[3 + c], off));
+            v[6 + c] += __shfl_xor_sync(0xffffffffu, v[6 + c], off);
+        }
+    }
+    __shared__ float s_red[kShuffleThreads / 32][9];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) s_red[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        const int k = threadIdx.x;
+        float r = s_red[0][k];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            const float x = s_red[w][k];
+            r = k < 3 ? fminf(r, x) : (k < 6 ? fmaxf(r, x) : r + x);
+        }
+        float* s = b.stats + 9 * buf;
+        // Non-negative floats order like their bit patterns (min starts at +inf, max at -inf).
+        if (k < 3)
+            atomicMin(reinterpret_cast<unsigned int*>(s + k), __float_as_uint(r));
+        else if (k < 6)
+            atomicMax(reinterpret_cast<int*>(s + k), __float_as_int(r));
+        else
+            atomicAdd(s + k, r);
+    }
+    if (!active) return;
+    if (radiance_scale > 0) target = target * radiance_scale;
+    target = rgb(fminf(target.r, 1e6f), fminf(target.g, 1e6f), fminf(target.b, 1e6f));
+#pragma unroll
+    for (int k = 0; k < kQueryFloats; ++k) b.train_query[1][kQueryFloats * static_cast<size_t>(dst) + k] = q[k];
+    store_rgb(b.train_target[1] + 3 * static_cast<size_t>(dst), target);
 }
 
-// nrc_set_up_kernels.cu:176-219, accumulating into both the reference's FP32 running mean and
-// the FP64 sums.
-__global__ void accumulate_kernel(NrcBuffers b, float radiance_scale, uint32_t accum_frames, double* __restrict__ sum,
-                                  float* __restrict__ mean, unsigned int* __restrict__ err) {
+// nrc_set_up_kernels.cu:176-219 for `spp` samples per pixel (slot = sample * pixels + pixel),
+// added to the FP64 sums. spp == 1 without `from_sums` keeps the reference's FP32 running mean
+// as sample `accum_frames`; otherwise the mean is the FP64 sum over accum_frames + spp samples.
+__global__ void accumulate_kernel(NrcBuffers b, float radiance_scale, uint32_t accum_frames, uint32_t spp,
+                                  int from_sums, double* __restrict__ sum, float* __restrict__ mean,
+                                  unsigned int* __restrict__ err) {
     const uint32_t npix = static_cast<uint32_t>(b.width) * static_cast<uint32_t>(b.height);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
-        const TerminalInfo t = b.infer_terminal[i];
-        RGB direct = load_rgb(b.frame_contribution + 3 * static_cast<size_t>(i));
-        RGB radiance = rgb(0, 0, 0);
-        if (t.bits & 1u) {
-            radiance = max0(load_rgb(b.inferred + 3 * static_cast<size_t>(i)));
-            if (radiance_scale > 0) radiance = rdiv(radiance, radiance_scale);
-            radiance = radiance * reflectance(b.infer_query + kQueryFloats * static_cast<size_t>(i));
+        double acc[3] = {0, 0, 0};
+        RGB c = rgb(0, 0, 0);
+        for (uint32_t smp = 0; smp < spp; ++smp) {
+            const size_t slot = static_cast<size_t>(smp) * npix + i;
+            const TerminalInfo t = b.infer_terminal[slot];
+            RGB direct = load_rgb(b.frame_contribution + 3 * slot);
+            RGB radiance = rgb(0, 0, 0);
+            if (t.bits & 1u) {
+                radiance = max0(load_rgb(b.inferred + 3 * slot));
+                if (radiance_scale > 0) radiance = rdiv(radiance, radiance_scale);
+                radiance = radiance * reflectance(b.infer_query + kQueryFloats * slot);
+            }
+            c = direct + rgb(t.tp[0], t.tp[1], t.tp[2]) * radiance;
+            if (!all_nonneg_finite(c)) {
+                atomicOr(err, 2u);
+                c = rgb(0, 0, 0);
+            }
+            acc[0] += c.r;
+            acc[1] += c.g;
+            acc[2] += c.b;
         }
-        RGB c = direct + rgb(t.tp[0], t.tp[1], t.tp[2]) * radiance;
-        if (!all_nonneg_finite(c)) {
-            atomicOr(err, 2u);
-            c = rgb(0, 0, 0);
+        const double s0 = sum[3 * static_cast<size_t>(i)] + acc[0];
+        const double s1 = sum[3 * static_cast<size_t>(i) + 1] + acc[1];
+        const double s2 = sum[3 * static_cast<size_t>(i) + 2] + acc[2];
+        sum[3 * static_cast<size_t>(i)] = s0;
+        sum[3 * static_cast<size_t>(i) + 1] = s1;
+        sum[3 * static_cast<size_t>(i) + 2] = s2;
+        if (spp == 1 && !from_sums) {
+            RGB prev = accum_frames > 0 ? load_rgb(mean + 3 * static_cast<size_t>(i)) : rgb(0, 0, 0);
+            float w = 1.0f / (accum_frames + 1);
+            store_rgb(mean + 3 * static_cast<size_t>(i), (1 - w) * prev + w * c);
+        } else {
+            const double inv = 1.0 / (static_cast<double>(accum_frames) + spp);
+            store_rgb(mean + 3 * static_cast<size_t>(i), rgb(static_cast<float>(s0 * inv), static_cast<float>(s1 * inv),
+                                                               static_cast<float>(s2 * inv)));
         }
-        RGB prev = accum_frames > 0 ? load_rgb(mean + 3 * static_cast<size_t>(i)) : rgb(0, 0, 0);
-        float w = 1.0f / (accum_frames + 1);
-        store_rgb(mean + 3 * static_cast<size_t>(i), (1 - w) * prev + w * c);
-        sum[3 * static_cast<size_t>(i)] += c.r;
-        sum[3 * static_cast<size_t>(i) + 1] += c.g;
-        sum[3 * static_cast<size_t>(i) + 2] += c.b;
     }
 }
 
@@ -174,12 +230,13 @@ void nrc_propagate(const NrcBuffers& b, float radiance_scale, cudaStream_t s) {
     propagate_kernel<<<(n + 255) / 256, 256, 0, s>>>(b, radiance_scale);
 }
 void nrc_shuffle(const NrcBuffers& b, uint32_t buf, float radiance_scale, cudaStream_t s) {
-    shuffle_kernel<<<kNumTrainingDataPerFrame / 256, 256, 0, s>>>(b, buf, radiance_scale);
+    shuffle_kernel<<<kNumTrainingDataPerFrame / kShuffleThreads, kShuffleThreads, 0, s>>>(b, buf, radiance_scale);
 }
-void nrc_accumulate(const NrcBuffers& b, float radiance_scale, uint32_t accum_frames, double* sum, float* mean,
-                    unsigned int* err, cudaStream_t s) {
+void nrc_accumulate(const NrcBuffers& b, float radiance_scale, uint32_t accum_frames, uint32_t spp, bool from_sums,
+                    double* sum, float* mean, unsigned int* err, cudaStream_t s) {
     uint32_t n = static_cast<uint32_t>(b.width) * static_cast<uint32_t>(b.height);
-    accumulate_kernel<<<(n + 255) / 256, 256, 0, s>>>(b, radiance_scale, accum_frames, sum, mean, err);
+    accumulate_kernel<<<(n + 255) / 256, 256, 0, s>>>(b, radiance_scale, accum_frames, spp, from_sums ? 1 : 0, sum, mean,
+                                                      err);
 }
 
 }  // namespace vpt

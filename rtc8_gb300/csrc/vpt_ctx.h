@@ -69,6 +69,8 @@ struct VptContextImpl {
 int ctx_set_error(int code, const char* msg);
 int fill_trace_params(VptContextImpl* c, TraceParams* tp);
 int persistent_grid(VptContextImpl* c, int threads, const void* kernel, size_t smem);
+// Jump table (A, C) of sample-parallel streams first .. first + count - 1, enqueued on `s`.
+int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);

@@ -168,7 +168,12 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
         img_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
         img_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
         num_items = min(img_w * img_h, num_pixels);
+    } else if constexpr (kNrc) {
+        // Sample-parallel streams: P.spp samples per pixel in one render pass, each its own
+        // work item and record slot (sample-major: slot = sample * num_pixels + pixel).
+        if (P.stream_mode == 1) num_items = num_pixels * P.spp;
     }
+    uint32_t slot = 0;  // record index of the current sample in the pass buffers
     const V3 wmin = bmin, wmax = bmax;
     uint32_t rng_index = 0;
     float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
@@ -202,6 +207,15 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 if constexpr (kNrc) {
                     if (item >= num_items) {
                         st = ST_DONE;
+                        break;
+                    }
+                    slot = item;
+                    if (!kTrain && P.stream_mode == 1) {
+                        pixel = item % num_pixels;
+                        sample = item / num_pixels;
+                        const ulonglong2 jump = P.sample_jumps[sample];
+                        rng.state = jump.x * P.rng[pixel] + jump.y;
+                        st = ST_CAMERA;
                         break;
                     }
                     pixel = item;  // linear index in the pass image
@@ -431,17 +445,17 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     }
                     if (ends_with_cache) {
                         const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
-                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(pixel), origin, -dir, rough,
+                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough,
                                     P.albedo, wmin, wmax);
                         if constexpr (kTrain) {
-                            P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                            P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         } else {
                             TerminalInfo ti;
                             ti.tp[0] = throughput.r;
                             ti.tp[1] = throughput.g;
                             ti.tp[2] = throughput.b;
                             ti.bits = 1u | ((path_length & 0xFFu) << 1);
-                            P.nrc.infer_terminal[pixel] = ti;
+                            P.nrc.infer_terminal[slot] = ti;
                         }
                         terminal_written = true;
                         end_code = END_CACHE;
@@ -584,9 +598,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         prev_local_tp = local_tp;
                         prev_vertex = idx;
                     } else {
-                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(pixel), origin, v_out, rough,
+                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(slot), origin, v_out, rough,
                                     P.albedo, wmin, wmax);
-                        P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                        P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         terminal_written = true;
                         err |= VPT_DEVERR_TRAIN_FULL;
                         end_code = END_TRAIN_FULL;
@@ -603,7 +617,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 if constexpr (kNrc) {
                     if constexpr (kTrain) {
                         if (!terminal_written)
-                            P.nrc.train_suffix[pixel] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
+                            P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
                     } else {
                         if (!terminal_written) {
                             TerminalInfo ti;
@@ -611,19 +625,19 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                             ti.tp[1] = throughput.g;
                             ti.tp[2] = throughput.b;
                             ti.bits = (path_length & 0xFFu) << 1;
-                            P.nrc.infer_terminal[pixel] = ti;
+                            P.nrc.infer_terminal[slot] = ti;
                         }
                         RGB c = contribution;
                         if (!all_nonneg_finite(c)) {
                             err |= VPT_DEVERR_NONFINITE;
                             c = rgb(0, 0, 0);
                         }
-                        float* fc = P.nrc.frame_contribution + 3 * static_cast<size_t>(pixel);
+                        float* fc = P.nrc.frame_contribution + 3 * static_cast<size_t>(slot);
                         fc[0] = c.r;
                         fc[1] = c.g;
                         fc[2] = c.b;
                     }
-                    P.rng[rng_index] = rng.state;
+                    if (kTrain || P.stream_mode != 1) P.rng[rng_index] = rng.state;
                     st = ST_FETCH;
                     break;
                 }

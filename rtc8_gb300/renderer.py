@@ -194,7 +194,7 @@ class Renderer:
     def nrc_views(self) -> dict:
         """torch tensors aliasing the context's radiance-cache buffers (no copies)."""
         b = self.nrc_buffers()
-        n = self.width * self.height
+        n = self.width * self.height * b.render_spp
         cap = b.infer_capacity
         tb = TRAIN_BUFFER_SIZE
         return {
@@ -236,6 +236,14 @@ class Renderer:
     def accumulate_inferred(self, accum_frames: int, stream: int | None = None) -> None:
         check(self.lib.vpt_accumulate_inferred(self.ctx, C.c_void_p(stream or 0), accum_frames),
               "vpt_accumulate_inferred")
+
+    def launch_render_nrc_batch(self, spp: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_launch_render_nrc_batch(self.ctx, C.c_void_p(stream or 0), spp),
+              "vpt_launch_render_nrc_batch")
+
+    def accumulate_inferred_batch(self, accum_frames: int, spp: int, stream: int | None = None) -> None:
+        check(self.lib.vpt_accumulate_inferred_batch(self.ctx, C.c_void_p(stream or 0), accum_frames, spp),
+              "vpt_accumulate_inferred_batch")
 
     def nrc_frame(self, cache, train_iterations: int, spp: int, new_sequence: bool,
                   stream: int | None = None) -> None:

@@ -283,3 +283,72 @@ def test_nrc_frame_loop_gain_over_truncated_paths(cuda_device):
     cache.finalize()
     r.close()
     p.close()
+
+
+def _pcg_jump(states: np.ndarray, delta: int) -> np.ndarray:
+    """PCG32 state advanced by `delta` draws (LCG jump-ahead by squaring, Brown 1994)."""
+    mult, plus = 6364136223846793005, 1
+    acc_mult, acc_plus = 1, 0
+    m64 = (1 << 64) - 1
+    while delta:
+        if delta & 1:
+            acc_mult = (acc_mult * mult) & m64
+            acc_plus = (acc_plus * mult + plus) & m64
+        plus = ((mult + 1) * plus) & m64
+        mult = (mult * mult) & m64
+        delta >>= 1
+    return np.array([(acc_mult * int(s) + acc_plus) & m64 for s in states], dtype=np.uint64)
+
+
+def test_batched_render_pass_matches_oracle(cuda_device):
+    """spp samples per pixel in one launch on sample-parallel streams: sample s of pixel p starts
+    2^40 * (base + s) draws into the pixel's stream; each slot matches the oracle's render pass
+    started from that state, and the batched accumulation equals the restated one."""
+    import torch
+
+    cfg = small_config_mode(size=40, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=1)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    seeds = r.rng_states().copy()
+    spp = 3
+    r.launch_plain(2)  # sample-parallel streams continue after the plain launch's two samples
+    r.reset_accumulation()
+    r.launch_render_nrc_batch(spp)
+    torch.cuda.synchronize()
+    v = r.nrc_views()
+    n = cfg.width * cfg.height
+    assert r.nrc_buffers().render_spp >= spp
+    g_term = _np(v["infer_terminal"])[: n * spp]
+    g_bits = g_term[:, 3].copy().view(np.uint32)
+    g_fc = _np(v["frame_contribution"])[: n * spp]
+    g_q = _np(v["infer_query"])[: n * spp]
+    assert np.array_equal(r.rng_states(), seeds)  # seeds are not modified
+    sc = orc.scene_from_config(cfg, vox, env)
+    same_all = []
+    for s in range(spp):
+        st = _pcg_jump(seeds, (2 + s) << 40)
+        o = orc.nrc_pass(sc, st, 1, cfg.width, cfg.height)
+        sl = slice(s * n, (s + 1) * n)
+        same = g_bits[sl] == o["terminal_bits"]
+        same_all.append(same)
+        np.testing.assert_allclose(g_fc[sl][same], o["frame_contribution"][same], rtol=1e-4, atol=1e-7)
+        hq = same & ((o["terminal_bits"] & 1) == 1)
+        np.testing.assert_allclose(g_q[sl][hq], o["infer_query"][hq], rtol=1e-4, atol=1e-5)
+    assert np.concatenate(same_all).mean() >= DECISION_PARITY
+    # batched accumulation with random predictions
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    v["inferred"].copy_(torch.rand(v["inferred"].shape, device="cuda", generator=gen))
+    torch.cuda.synchronize()
+    inf, iq = _np(v["inferred"]).copy(), _np(v["infer_query"]).copy()
+    r.accumulate_inferred_batch(0, spp)
+    s_g, cnt = r.download_sum()
+    assert cnt == spp
+    s_o = np.zeros((n, 3), np.float64)
+    m_o = np.zeros((n, 3), np.float32)
+    for s in range(spp):
+        sl = slice(s * n, (s + 1) * n)
+        orc.nrc_accumulate(n, g_term[sl].copy(), g_fc[sl].copy(), inf[sl].copy(), iq[sl].copy(), 0.0, s, s_o, m_o)
+    np.testing.assert_allclose(s_g.reshape(n, 3), s_o, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(r.download_mean().reshape(n, 3), s_o / spp, rtol=1e-6, atol=1e-9)
+    assert r.device_errors() == 0
+    r.close()
