@@ -233,6 +233,10 @@ typedef struct VptNrcBuffers {
     float* train_query[2];       /* trainRadianceQueryBuffer[0..1]: 2^17 x 14 */
     float* train_target[2];      /* trainTargetBuffer[0..1]: 2^17 x 3 */
     void* train_vertex;          /* trainVertexInfoBuffer: 2^17 x {float tp[3]; u32 bits} */
+    float* train_end_query;      /* end queries of the training suffixes: w*h x 14 (the reference
+                                    shares the render pass's inference buffer) */
+    float* train_end_inferred;   /* their predictions: w*h x 3 */
+    uint64_t* train_rng;         /* training-pass PCG32 states when rng_stream_mode = 1 */
     uint32_t* shufflers;         /* dataShufflerBuffer: 2^16 LCG states */
     uint32_t* counters;          /* [0..1] numTrainingData, [2..5] trainImageSize (x, y) per
                                     buffer, [6] offsetToSelectUnbiasedPath, [7] training-pass
@@ -283,7 +287,10 @@ int vpt_accumulate_inferred_batch(VptContext* ctx, void* stream, uint32_t accum_
  * with sample-parallel streams (rng_stream_mode 1), one batched render pass of `spp` samples,
  * one inference and one accumulation.
  * Accumulation continues the context's (the reference restarts it every frame: call
- * vpt_reset_accumulation first for that). Nothing is synchronised. */
+ * vpt_reset_accumulation first for that). Nothing is synchronised. With sample-parallel streams
+ * the render pass runs on a second stream of the context, concurrently with the training
+ * iterations, and joins `stream` before its inference; the training pass then draws from its own
+ * per-pixel states (train_rng) so the two passes share no state. */
 int vpt_nrc_frame(VptContext* ctx, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
                   int32_t new_sequence);
 

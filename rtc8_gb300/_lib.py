@@ -126,6 +126,9 @@ class VptNrcBuffers(C.Structure):
         ("train_query", C.c_void_p * 2),
         ("train_target", C.c_void_p * 2),
         ("train_vertex", C.c_void_p),
+        ("train_end_query", C.c_void_p),
+        ("train_end_inferred", C.c_void_p),
+        ("train_rng", C.c_void_p),
         ("shufflers", C.c_void_p),
         ("counters", C.c_void_p),
         ("stats", C.c_void_p),

@@ -9,8 +9,8 @@ RNG streams (the "oracle image"). The error measure is the relative MSE
 (the 0.01 keeps dark pixels from dominating). Time is GPU time of the estimator's own launches
 (CUDA events on its stream), excluding the error evaluation. The radiance-cache estimator runs
 the reference's frame loop (renderer/renderer_main.cpp:1553-1637): every frame trains the cache
-on that frame's training suffixes and renders one sample per pixel; the first frame trains
-eight times (a new sequence).
+on that frame's training suffixes and renders `spp_per_frame` samples per pixel (batched into one
+render pass on sample-parallel streams); the first frame trains eight times (a new sequence).
 """
 from __future__ import annotations
 

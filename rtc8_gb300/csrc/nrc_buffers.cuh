@@ -46,6 +46,14 @@ struct NrcBuffers {
     float* train_query[2] = {nullptr, nullptr};   // kTrainBufferSize * 14
     float* train_target[2] = {nullptr, nullptr};  // kTrainBufferSize * 3
     TrainVertexInfo* train_vertex = nullptr;      // kTrainBufferSize
+    // End queries of the training suffixes and their predictions (max_train_suffixes records).
+    // The reference keeps them in the render pass's inference buffers and serialises the passes
+    // (renderer_main.cpp:1611-1613); separate buffers let the two passes run concurrently.
+    float* train_end_query = nullptr;             // max_train_suffixes * 14
+    float* train_end_inferred = nullptr;          // max_train_suffixes * 3
+    // Per-pixel PCG32 states of the training pass when the render passes use sample-parallel
+    // streams (the context's states, advanced 2^62 draws); null = the context's states.
+    uint64_t* train_rng = nullptr;
     uint32_t* shufflers = nullptr;                // kNumTrainingDataPerFrame LCG states
     // [0..1] numTrainingData per buffer, [2..5] trainImageSize (x, y) per buffer,
     // [6] offsetToSelectUnbiasedPath, [7] training-pass query count of the current buffer

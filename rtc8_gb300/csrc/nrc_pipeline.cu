@@ -63,6 +63,12 @@ int ensure_nrc(VptContext* c) {
         chk(alloc_zero(&b->train_target[i], static_cast<size_t>(vpt::kTrainBufferSize) * 3));
     }
     chk(alloc_zero(&b->train_vertex, vpt::kTrainBufferSize));
+    chk(alloc_zero(&b->train_end_query, npix * vpt::kQueryFloats));
+    chk(alloc_zero(&b->train_end_inferred, npix * 3));
+    chk(alloc_zero(&b->train_rng, npix));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->nrc_aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->nrc_ev_start, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->nrc_ev_render, cudaEventDisableTiming);
     chk(alloc_zero(&b->shufflers, vpt::kNumTrainingDataPerFrame));
     chk(alloc_zero(&b->counters, 16));
     chk(alloc_zero(&b->stats, 18));
@@ -79,7 +85,13 @@ int ensure_nrc(VptContext* c) {
         st[i] = s;
     }
     NRCP_CUDA(cudaMemcpy(b->shufflers, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    return VPT_OK;
+    return vpt::nrc_reseed_train_rng(c);
+}
+
+__global__ void derive_states_kernel(uint64_t* __restrict__ out, const uint64_t* __restrict__ in, uint32_t n,
+                                     uint64_t mult, uint64_t plus) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = mult * in[i] + plus;
 }
 
 // radianceScale of the frame (renderer_shared.h:160); <= 0 = off.
@@ -116,11 +128,16 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
 // Launch of a radiance-cache pass of the persistent tracker: the training pass or a render pass
 // of one sample per pixel on the per-pixel streams (stream_mode 0), or a render pass of `spp`
 // samples per pixel on sample-parallel streams (stream_mode 1).
-int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0) {
+// `work_slot` selects the work counter, so that two passes can run at the same time.
+int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
+                int work_slot = 0) {
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;
     if ((rc = vpt::fill_trace_params(c, &tp))) return rc;
+    tp.work_counter = c->d_work + work_slot;
+    // With sample-parallel render streams the training pass draws from its own per-pixel states.
+    if (mode == vpt::kModeTrainNrc && c->frame.rng_stream_mode == 1) tp.rng = c->nrc->train_rng;
     tp.spp = spp;
     tp.accum_base = 0;
     tp.stream_mode = stream_mode;
@@ -132,7 +149,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc = *c->nrc;
     tp.nrc_buf = buf;
     tp.nrc_density_query = c->nrc_query_density;
-    NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
+    NRCP_CUDA(cudaMemsetAsync(tp.work_counter, 0, sizeof(unsigned int), s));
     const int threads = c->threads > 0 ? c->threads : 128;
     const bool grid_maj = c->frame.majorant_mode == 1;
     size_t smem = 0;
@@ -150,8 +167,29 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
 }  // namespace
 
 namespace vpt {
+int nrc_reseed_train_rng(VptContextImpl* c) {
+    if (!c->nrc || !c->nrc->train_rng) return VPT_OK;
+    // 2^62 draws ahead: disjoint from the render samples' streams (sample s starts s * 2^40
+    // draws in, s < 2^22) for any realistic run.
+    uint64_t mult, plus;
+    lcg_jump(1ull << 62, &mult, &plus);
+    const uint32_t n = static_cast<uint32_t>(c->width) * static_cast<uint32_t>(c->height);
+    derive_states_kernel<<<(n + 255) / 256, 256>>>(c->nrc->train_rng, c->d_rng, n, mult, plus);
+    NRCP_CUDA(cudaGetLastError());
+    NRCP_CUDA(cudaDeviceSynchronize());
+    return VPT_OK;
+}
+
 void VptContextImpl::release_nrc() {
+    if (nrc_aux) cudaStreamDestroy(nrc_aux);
+    if (nrc_ev_start) cudaEventDestroy(nrc_ev_start);
+    if (nrc_ev_render) cudaEventDestroy(nrc_ev_render);
+    nrc_aux = nullptr;
+    nrc_ev_start = nrc_ev_render = nullptr;
     if (!nrc) return;
+    free_ptr(nrc->train_end_query);
+    free_ptr(nrc->train_end_inferred);
+    free_ptr(nrc->train_rng);
     free_ptr(nrc->infer_query);
     free_ptr(nrc->infer_terminal);
     free_ptr(nrc->train_suffix);
@@ -192,6 +230,9 @@ int vpt_nrc_get_buffers(VptContext* c, VptNrcBuffers* out) {
         out->train_target[i] = b.train_target[i];
     }
     out->train_vertex = b.train_vertex;
+    out->train_end_query = b.train_end_query;
+    out->train_end_inferred = b.train_end_inferred;
+    out->train_rng = b.train_rng;
     out->shufflers = b.shufflers;
     out->counters = b.counters;
     out->stats = b.stats;
@@ -282,8 +323,19 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     auto* net = static_cast<NrcHandle*>(nrc);
     int rc = ensure_nrc(c);
     if (rc) return rc;
-    vpt::NrcBuffers& b = *c->nrc;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t npix = static_cast<uint32_t>(c->width) * static_cast<uint32_t>(c->height);
+    const bool batched = c->frame.rng_stream_mode == 1 && spp > 0;
+    if (batched) {
+        // The render pass traces on the second stream while the training iterations run: its
+        // paths need no network until their queries are inferred, after the training steps.
+        if ((rc = ensure_render_slots(c, spp))) return rc;
+        NRCP_CUDA(cudaEventRecord(c->nrc_ev_start, s));
+        NRCP_CUDA(cudaStreamWaitEvent(c->nrc_aux, c->nrc_ev_start, 0));
+        if ((rc = launch_pass(c, c->nrc_aux, vpt::kModeRenderNrc, 0, spp, 1, 1))) return rc;
+        NRCP_CUDA(cudaEventRecord(c->nrc_ev_render, c->nrc_aux));
+    }
+    vpt::NrcBuffers& b = *c->nrc;
     for (uint32_t it = 0; it < train_iterations; ++it) {
         c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
         const uint32_t buf = c->nrc_buf_index;
@@ -291,7 +343,8 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
         if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
         if ((rc = vpt_launch_generate_training(c, stream, buf))) return rc;
         // Predictions for the training suffixes' end queries (trainW * trainH of them).
-        if (nrc_infer_device_count(net, stream, b.infer_query, b.counters + 7, b.max_train_suffixes, b.inferred))
+        if (nrc_infer_device_count(net, stream, b.train_end_query, b.counters + 7, b.max_train_suffixes,
+                                   b.train_end_inferred))
             return fail(VPT_ERR_CUDA, std::string("nrc_infer_device_count: ") + nrc_last_error());
         if ((rc = vpt_propagate(c, stream))) return rc;
         if ((rc = vpt_shuffle(c, stream, buf))) return rc;
@@ -304,10 +357,8 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
         }
     }
     if (spp == 0) return VPT_OK;
-    if (c->frame.rng_stream_mode == 1) {
-        // All samples of the frame in one render pass on sample-parallel streams, one inference
-        // over every sample's query, one accumulation.
-        if ((rc = vpt_launch_render_nrc_batch(c, stream, spp))) return rc;
+    if (batched) {
+        NRCP_CUDA(cudaStreamWaitEvent(s, c->nrc_ev_render, 0));
         if (nrc_infer(net, stream, b.infer_query, npix * spp, b.inferred))
             return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
         return vpt_accumulate_inferred_batch(c, stream, c->accum_samples, spp);

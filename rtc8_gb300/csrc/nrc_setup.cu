@@ -68,9 +68,9 @@ __global__ void propagate_kernel(NrcBuffers b, float radiance_scale) {
         if (idx >= kTrainBufferSize) continue;  // no vertex (kInvalidVertex) or a corrupt link
         RGB contribution = rgb(0, 0, 0);
         if ((term >> 22) & 1u) {
-            contribution = max0(load_rgb(b.inferred + 3 * static_cast<size_t>(i)));
+            contribution = max0(load_rgb(b.train_end_inferred + 3 * static_cast<size_t>(i)));
             if (radiance_scale > 0) contribution = rdiv(contribution, radiance_scale);
-            contribution = contribution * reflectance(b.infer_query + kQueryFloats * static_cast<size_t>(i));
+            contribution = contribution * reflectance(b.train_end_query + kQueryFloats * static_cast<size_t>(i));
         }
         // Walk the suffix backwards; vertex indices decrease along it, so the walk ends.
         for (uint32_t guard = 0; idx < kTrainBufferSize && guard < kTrainBufferSize; ++guard) {

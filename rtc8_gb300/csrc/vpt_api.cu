@@ -125,6 +125,7 @@ int vpt_seed_rng(VptContext* c, uint64_t seed) {
     for (int64_t i = 0; i < npix; ++i) states[i] = gen();
     VPT_CUDA(cudaMemcpy(c->d_rng, states.data(), npix * sizeof(uint64_t), cudaMemcpyHostToDevice));
     c->stream_samples = 0;
+    if (int rc = vpt::nrc_reseed_train_rng(c)) return rc;
     return vpt_reset_accumulation(c);
 }
 
@@ -132,7 +133,7 @@ int vpt_set_rng_states(VptContext* c, const uint64_t* host) {
     if (!c || !host) return set_error(VPT_ERR_INVALID_ARGUMENT, "null argument");
     int64_t npix = static_cast<int64_t>(c->width) * c->height;
     VPT_CUDA(cudaMemcpy(c->d_rng, host, npix * sizeof(uint64_t), cudaMemcpyHostToDevice));
-    return VPT_OK;
+    return vpt::nrc_reseed_train_rng(c);
 }
 
 int vpt_get_rng_states(VptContext* c, uint64_t* host) {
@@ -382,7 +383,7 @@ int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads, in
 
 namespace vpt {
 // LCG jump (multiplier, increment) of `delta` PCG32 draws (O(log delta) advance, Brown 1994).
-static void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus) {
+void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus) {
     uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
     while (delta > 0) {
         if (delta & 1ULL) {

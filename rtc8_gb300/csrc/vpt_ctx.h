@@ -63,12 +63,19 @@ struct VptContextImpl {
     int32_t nrc_query_density = 0;
     uint32_t nrc_buf_index = 1;            // the first training iteration uses buffer 0
     std::mt19937 nrc_offset_rng{72139121}; // perFrameRng (renderer_main.cpp:1500)
+    // Second stream and events of a frame whose render pass overlaps the training pass.
+    cudaStream_t nrc_aux = nullptr;
+    cudaEvent_t nrc_ev_start = nullptr, nrc_ev_render = nullptr;
     void release_nrc();
 };
 
 int ctx_set_error(int code, const char* msg);
 int fill_trace_params(VptContextImpl* c, TraceParams* tp);
 int persistent_grid(VptContextImpl* c, int threads, const void* kernel, size_t smem);
+// LCG jump (multiplier, increment) that advances a PCG32 state by `delta` draws.
+void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus);
+// Training-pass RNG states derived from the context's per-pixel states (no-op without cache buffers).
+int nrc_reseed_train_rng(VptContextImpl* c);
 // Jump table (A, C) of sample-parallel streams first .. first + count - 1, enqueued on `s`.
 int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,

@@ -445,8 +445,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     }
                     if (ends_with_cache) {
                         const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
-                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough,
-                                    P.albedo, wmin, wmax);
+                        float* qdst = kTrain ? P.nrc.train_end_query : P.nrc.infer_query;
+                        write_query(qdst + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough, P.albedo, wmin,
+                                    wmax);
                         if constexpr (kTrain) {
                             P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         } else {
@@ -598,8 +599,8 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         prev_local_tp = local_tp;
                         prev_vertex = idx;
                     } else {
-                        write_query(P.nrc.infer_query + kQueryFloats * static_cast<size_t>(slot), origin, v_out, rough,
-                                    P.albedo, wmin, wmax);
+                        write_query(P.nrc.train_end_query + kQueryFloats * static_cast<size_t>(slot), origin, v_out,
+                                    rough, P.albedo, wmin, wmax);
                         P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         terminal_written = true;
                         err |= VPT_DEVERR_TRAIN_FULL;

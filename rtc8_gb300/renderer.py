@@ -208,6 +208,9 @@ class Renderer:
             "train_target0": device_view(b.train_target[0], (tb, 3), "<f4"),
             "train_target1": device_view(b.train_target[1], (tb, 3), "<f4"),
             "train_vertex": device_view(b.train_vertex, (tb, 4), "<f4"),
+            "train_end_query": device_view(b.train_end_query, (self.width * self.height, 14), "<f4"),
+            "train_end_inferred": device_view(b.train_end_inferred, (self.width * self.height, 3), "<f4"),
+            "train_rng": device_view(b.train_rng, (self.width * self.height,), "<i8"),
             "shufflers": device_view(b.shufflers, (TRAIN_PER_FRAME,), "<i4"),
             "counters": device_view(b.counters, (16,), "<i4"),
             "stats": device_view(b.stats, (18,), "<f4"),
