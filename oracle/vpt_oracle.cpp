@@ -587,6 +587,7 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                const OrcNrcSink* nrc = nullptr, uint32_t item = 0, bool unbiased = false) {
     const bool with_nrc = nrc != nullptr;
     const bool train = with_nrc && nrc->mode == 2;
+    const float term_factor = with_nrc && nrc->termination > 0 ? nrc->termination : ORC_NRC_TERMINATION_FACTOR;
     const float img_w = with_nrc ? static_cast<float>(nrc->img_w) : static_cast<float>(s.width);
     const float img_h = with_nrc ? static_cast<float>(nrc->img_h) : static_cast<float>(s.height);
     V3 origin, dir;
@@ -691,9 +692,9 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
             bool ends_with_cache = rr_kill;
             const float spread2 = sqrt_spread * sqrt_spread;
             if (train) {
-                if (!unbiased) ends_with_cache |= spread2 > 2 * ORC_NRC_TERMINATION_FACTOR * primary_spread;
+                if (!unbiased) ends_with_cache |= spread2 > 2 * term_factor * primary_spread;
             } else {
-                ends_with_cache |= spread2 > ORC_NRC_TERMINATION_FACTOR * primary_spread;
+                ends_with_cache |= spread2 > term_factor * primary_spread;
             }
             if (ends_with_cache) {
                 float rough = 0.0f;

@@ -89,6 +89,7 @@ typedef struct OrcNrcSink {
     int32_t density_query;     /* roughness slot = local density / density_coeff */
     uint32_t img_w, img_h;     /* pass image (training image size in mode 2) */
     uint32_t unbiased_offset;  /* offsetToSelectUnbiasedPath */
+    float termination;         /* path-spread termination factor (0 = 0.01) */
     float* infer_query;        /* 14 per pass pixel */
     float* terminal_tp;        /* mode 1: 3 per pixel */
     uint32_t* terminal_bits;   /* mode 1: hasQuery | pathLength << 1 */

@@ -149,6 +149,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc = *c->nrc;
     tp.nrc_buf = buf;
     tp.nrc_density_query = c->nrc_query_density;
+    tp.nrc_termination = c->nrc_termination;
     NRCP_CUDA(cudaMemsetAsync(tp.work_counter, 0, sizeof(unsigned int), s));
     const int threads = c->threads > 0 ? c->threads : 128;
     const bool grid_maj = c->frame.majorant_mode == 1;
@@ -245,6 +246,13 @@ int vpt_nrc_get_buffers(VptContext* c, VptNrcBuffers* out) {
 int vpt_nrc_set_query_density(VptContext* c, int32_t query_density) {
     if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_set_query_density: null context");
     c->nrc_query_density = query_density ? 1 : 0;
+    return VPT_OK;
+}
+
+int vpt_nrc_set_termination_factor(VptContext* c, float factor) {
+    if (!c || !(factor >= 0.0f) || !(factor < 1e30f))
+        return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_set_termination_factor: bad arguments");
+    c->nrc_termination = factor;
     return VPT_OK;
 }
 

@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
         if (P.stream_mode == 1) num_items = num_pixels * P.spp;
     }
     uint32_t slot = 0;  // record index of the current sample in the pass buffers
+    const float term_factor = P.nrc_termination > 0 ? P.nrc_termination : kPathTerminationFactor;
     const V3 wmin = bmin, wmax = bmax;
     uint32_t rng_index = 0;
     float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
@@ -439,9 +440,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     bool ends_with_cache = rr_kill;
                     const float spread2 = sqrt_spread * sqrt_spread;
                     if constexpr (kTrain) {
-                        if (!unbiased) ends_with_cache |= spread2 > 2 * kPathTerminationFactor * primary_spread;
+                        if (!unbiased) ends_with_cache |= spread2 > 2 * term_factor * primary_spread;
                     } else {
-                        ends_with_cache |= spread2 > kPathTerminationFactor * primary_spread;
+                        ends_with_cache |= spread2 > term_factor * primary_spread;
                     }
                     if (ends_with_cache) {
                         const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;

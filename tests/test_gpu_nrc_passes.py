@@ -40,14 +40,15 @@ def _scene(cfg):
     return vox, env
 
 
-@pytest.mark.parametrize("density_query", [False, True])
-def test_render_pass_matches_oracle(cuda_device, density_query):
+@pytest.mark.parametrize("density_query,termination", [(False, 0.0), (True, 0.0), (False, 0.05)])
+def test_render_pass_matches_oracle(cuda_device, density_query, termination):
     import torch
 
     cfg = small_reference_mode(size=48, n=32, sigma=60.0)
     vox, env = _scene(cfg)
     r = _setup(cfg, vox, env)
     r.nrc_set_query_density(density_query)
+    r.nrc_set_termination_factor(termination)
     rng0 = r.rng_states().copy()
     r.launch_render_nrc()
     torch.cuda.synchronize()
@@ -62,7 +63,7 @@ def test_render_pass_matches_oracle(cuda_device, density_query):
 
     sc = orc.scene_from_config(cfg, vox, env)
     o_rng = rng0.copy()
-    o = orc.nrc_pass(sc, o_rng, 1, cfg.width, cfg.height, density_query=density_query)
+    o = orc.nrc_pass(sc, o_rng, 1, cfg.width, cfg.height, density_query=density_query, termination=termination)
     same = (g_rng == o_rng) & (g_bits == o["terminal_bits"])
     assert same.mean() >= DECISION_PARITY, f"identical pixels {same.mean():.5f}"
     has_q = same & ((o["terminal_bits"] & 1) == 1)
