@@ -3,6 +3,8 @@
 One step = one launch of the plain tracer over the whole 1024x1024 image at STEP_SPP samples
 per pixel on the sparse 512^3 fBm cloud (sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256
 bounces, sun at 20 degrees + Hosek-Wilkie sky). Metric: paths/s = pixels * spp / time.
+The line also carries `nrc_vs_plain`: GPU time for the radiance-cache renderer and for the plain
+tracer to reach relMSE 1e-3 against a 16384-spp FP64 image on the 256x256 dense 64^3 scene.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2|c1]
 
@@ -165,6 +167,42 @@ def scene_host_inputs(cfg):
     return vox, env
 
 
+def nrc_frame_loop(frames: int, warmup: int) -> dict:
+    """The radiance-cache frame loop (1 training iteration + 8 spp per frame, settings of the
+    equal-error comparison) on the 256x256 dense 64^3 scene; returns the mean frame time."""
+    import torch
+
+    from rtc8_gb300 import convergence, nrc
+    from rtc8_gb300.configs import C1
+    from rtc8_gb300.renderer import Renderer, setup_scene
+
+    st = convergence.NRC_SETTINGS
+    r = Renderer(C1.width, C1.height)
+    setup_scene(r, C1)
+    r.nrc_set_query_density(True)
+    r.nrc_set_termination_factor(st["termination"])
+    net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    net.ema_decay, net.learning_rate = st["ema_decay"], st["learning_rate"]
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=net)
+    s = torch.cuda.Stream()
+    r.nrc_frame(cache, 8, st["spp_per_frame"], True, s.cuda_stream)
+    for _ in range(warmup):
+        r.nrc_frame(cache, 1, st["spp_per_frame"], False, s.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(frames):
+        r.nrc_frame(cache, 1, st["spp_per_frame"], False, s.cuda_stream)
+    b.record(s)
+    torch.cuda.synchronize()
+    out = {"nrc_frame_ms": a.elapsed_time(b) / frames, "frames": frames, "spp_per_frame": st["spp_per_frame"],
+           "device_errors": r.device_errors() | cache.device_errors()}
+    cache.finalize()
+    r.close()
+    return out
+
+
 # ------------------------------------------------------------------------------ main
 def main():
     ap = argparse.ArgumentParser()
@@ -176,6 +214,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
+    ap.add_argument("--no-nrc", action="store_true", help="skip the NRC-vs-plain equal-error comparison")
+    ap.add_argument("--nrc-frames", type=int, default=0,
+                    help="profiling run: only the radiance-cache frame loop on the 256x256 scene, N timed frames")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
 
@@ -216,6 +257,11 @@ def main():
         return
 
     from rtc8_gb300.renderer import Renderer, setup_scene
+
+    if args.nrc_frames:
+        torch.cuda.set_device(local)
+        print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup)), flush=True)
+        return
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -295,6 +341,17 @@ def main():
                 "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs", "traffic_source": prof,
                 "algorithmic_bytes_per_launch": alg_bytes, "lookups_per_launch": lookups_per_launch}
 
+    # ---- radiance cache vs plain at equal error (NRC form of the 256x256 dense 64^3 configuration)
+    nrc_cmp = None
+    if rank == 0 and not args.no_nrc:
+        from rtc8_gb300 import convergence
+        from rtc8_gb300.configs import C1
+        res = convergence.compare(C1, target=1e-3, oracle_spp=16384, time_budget=60.0)
+        nrc_cmp = {k: v for k, v in res.items() if k != "curves"}
+        nrc_cmp["workload"] = (f"{C1.name}: 256x256, dense fBm 64^3, sigma_t max {C1.volume.sigma_t_max}, "
+                               f"albedo {C1.albedo}, HG g {C1.phase_param}, sun + constant env 0.5")
+        nrc_cmp["time"] = "GPU time of each estimator's launches (CUDA events), error evaluation excluded"
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         vox, env = scene_host_inputs(cfg)
@@ -310,7 +367,8 @@ def main():
                            "total_leaves": info["total_leaves"], "parallelism": f"replicas x{world}"},
                 "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": args.steps,
+                "gpu_launches": args.steps * (2 if cfg.rng_stream_mode == 1 else 1),  # tracer + mean finalise
+                "nrc_vs_plain": nrc_cmp,
                 "roofline": roofline,
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),
