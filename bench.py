@@ -367,7 +367,7 @@ def main():
                            "total_leaves": info["total_leaves"], "parallelism": f"replicas x{world}"},
                 "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": args.steps * (2 if cfg.rng_stream_mode == 1 else 1),  # tracer + mean finalise
+                "gpu_launches": args.steps * (3 if cfg.rng_stream_mode == 1 else 1),  # jump table, tracer, mean
                 "nrc_vs_plain": nrc_cmp,
                 "roofline": roofline,
                 "cpu_baseline": cpu,

@@ -292,9 +292,11 @@ int vpt_accumulate_inferred_batch(VptContext* ctx, void* stream, uint32_t accum_
  * one inference and one accumulation.
  * Accumulation continues the context's (the reference restarts it every frame: call
  * vpt_reset_accumulation first for that). Nothing is synchronised. With sample-parallel streams
- * the render pass runs on a second stream of the context, concurrently with the training
- * iterations, and joins `stream` before its inference; the training pass then draws from its own
- * per-pixel states (train_rng) so the two passes share no state. */
+ * the first training pass and the frame's render samples are ONE persistent launch (training
+ * pixels first, then render samples: lanes that finish a training suffix go on with render
+ * samples, so the longest suffixes hold no idle SM slots); the training pass then draws from its
+ * own per-pixel states (train_rng) so the two kinds of work share no state. The render queries
+ * are inferred after the training steps, with the updated network, as in the reference. */
 int vpt_nrc_frame(VptContext* ctx, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
                   int32_t new_sequence);
 

@@ -85,9 +85,11 @@ def plain_curve(cfg: SceneConfig, ref: np.ndarray, target: float, chunk_spp: int
 
 def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None, spp_per_frame: int = 8,
               eval_every: int = 1, max_frames: int = 4096, time_budget: float = 60.0,
-              query_density: bool = True, termination: float = 0.0) -> dict:
+              query_density: bool = True, termination: float = 0.0, warmup_frames: int = 0) -> dict:
     """relMSE of the radiance-cache renderer after every `eval_every` frames of `spp_per_frame`
-    samples per pixel (the reference renders 8 samples per frame, renderer_main.cpp:359)."""
+    samples per pixel (the reference renders 8 samples per frame, renderer_main.cpp:359). The
+    images of the first frame and of `warmup_frames` more frames (rendered while the cache is
+    still young) are dropped from the accumulation; their time counts."""
     import torch
 
     from . import nrc
@@ -101,7 +103,11 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
     cache.initialize(config=net_config or nrc.default_config(nrc.NRC_ENCODING_VOLUME))
     curve, t, frames, reached = [], 0.0, 0, None
     t += _timed(s, lambda: r.nrc_frame(cache, 8, spp_per_frame, True, s.cuda_stream))
-    frames = 1
+    for _ in range(warmup_frames):
+        t += _timed(s, lambda: r.nrc_frame(cache, 1, spp_per_frame, False, s.cuda_stream))
+    frames = 1 + warmup_frames
+    if warmup_frames:
+        r.reset_accumulation()
     wall0 = time.perf_counter()
     while frames < max_frames and time.perf_counter() - wall0 < time_budget:
         def run():

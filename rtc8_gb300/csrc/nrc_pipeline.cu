@@ -66,9 +66,6 @@ int ensure_nrc(VptContext* c) {
     chk(alloc_zero(&b->train_end_query, npix * vpt::kQueryFloats));
     chk(alloc_zero(&b->train_end_inferred, npix * 3));
     chk(alloc_zero(&b->train_rng, npix));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->nrc_aux, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->nrc_ev_start, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->nrc_ev_render, cudaEventDisableTiming);
     chk(alloc_zero(&b->shufflers, vpt::kNumTrainingDataPerFrame));
     chk(alloc_zero(&b->counters, 16));
     chk(alloc_zero(&b->stats, 18));
@@ -128,14 +125,11 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
 // Launch of a radiance-cache pass of the persistent tracker: the training pass or a render pass
 // of one sample per pixel on the per-pixel streams (stream_mode 0), or a render pass of `spp`
 // samples per pixel on sample-parallel streams (stream_mode 1).
-// `work_slot` selects the work counter, so that two passes can run at the same time.
-int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
-                int work_slot = 0) {
+int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0) {
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;
     if ((rc = vpt::fill_trace_params(c, &tp))) return rc;
-    tp.work_counter = c->d_work + work_slot;
     // With sample-parallel render streams the training pass draws from its own per-pixel states.
     if (mode == vpt::kModeTrainNrc && c->frame.rng_stream_mode == 1) tp.rng = c->nrc->train_rng;
     tp.spp = spp;
@@ -150,7 +144,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc_buf = buf;
     tp.nrc_density_query = c->nrc_query_density;
     tp.nrc_termination = c->nrc_termination;
-    NRCP_CUDA(cudaMemsetAsync(tp.work_counter, 0, sizeof(unsigned int), s));
+    NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     const int threads = c->threads > 0 ? c->threads : 128;
     const bool grid_maj = c->frame.majorant_mode == 1;
     size_t smem = 0;
@@ -182,11 +176,6 @@ int nrc_reseed_train_rng(VptContextImpl* c) {
 }
 
 void VptContextImpl::release_nrc() {
-    if (nrc_aux) cudaStreamDestroy(nrc_aux);
-    if (nrc_ev_start) cudaEventDestroy(nrc_ev_start);
-    if (nrc_ev_render) cudaEventDestroy(nrc_ev_render);
-    nrc_aux = nullptr;
-    nrc_ev_start = nrc_ev_render = nullptr;
     if (!nrc) return;
     free_ptr(nrc->train_end_query);
     free_ptr(nrc->train_end_inferred);
@@ -334,22 +323,20 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t npix = static_cast<uint32_t>(c->width) * static_cast<uint32_t>(c->height);
     const bool batched = c->frame.rng_stream_mode == 1 && spp > 0;
-    if (batched) {
-        // The render pass traces on the second stream while the training iterations run: its
-        // paths need no network until their queries are inferred, after the training steps.
-        if ((rc = ensure_render_slots(c, spp))) return rc;
-        NRCP_CUDA(cudaEventRecord(c->nrc_ev_start, s));
-        NRCP_CUDA(cudaStreamWaitEvent(c->nrc_aux, c->nrc_ev_start, 0));
-        if ((rc = launch_pass(c, c->nrc_aux, vpt::kModeRenderNrc, 0, spp, 1, 1))) return rc;
-        NRCP_CUDA(cudaEventRecord(c->nrc_ev_render, c->nrc_aux));
-    }
+    if (batched && (rc = ensure_render_slots(c, spp))) return rc;
     vpt::NrcBuffers& b = *c->nrc;
     for (uint32_t it = 0; it < train_iterations; ++it) {
         c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
         const uint32_t buf = c->nrc_buf_index;
         const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
         if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
-        if ((rc = vpt_launch_generate_training(c, stream, buf))) return rc;
+        if (batched && it == 0) {
+            // The first training pass and the frame's render samples in one launch: the render
+            // paths need the network only at their inference, after the training steps below.
+            if ((rc = launch_pass(c, s, vpt::kModeComboNrc, buf, spp, 1))) return rc;
+        } else if ((rc = vpt_launch_generate_training(c, stream, buf))) {
+            return rc;
+        }
         // Predictions for the training suffixes' end queries (trainW * trainH of them).
         if (nrc_infer_device_count(net, stream, b.train_end_query, b.counters + 7, b.max_train_suffixes,
                                    b.train_end_inferred))
@@ -366,7 +353,7 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     }
     if (spp == 0) return VPT_OK;
     if (batched) {
-        NRCP_CUDA(cudaStreamWaitEvent(s, c->nrc_ev_render, 0));
+        if (train_iterations == 0 && (rc = launch_pass(c, s, vpt::kModeRenderNrc, 0, spp, 1))) return rc;
         if (nrc_infer(net, stream, b.infer_query, npix * spp, b.inferred))
             return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
         return vpt_accumulate_inferred_batch(c, stream, c->accum_samples, spp);

@@ -407,18 +407,10 @@ int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaS
         if (rc) return rc;
         c->jump_capacity = count;
     }
-    std::vector<ulonglong2> table(count);
-    uint64_t a, b, a1, b1;
-    lcg_jump(static_cast<uint64_t>(first) << kSampleStreamShift, &a, &b);
-    lcg_jump(1ULL << kSampleStreamShift, &a1, &b1);
-    for (uint32_t i = 0; i < count; ++i) {
-        table[i] = make_ulonglong2(a, b);
-        b = a1 * b + b1;  // compose with one more 2^40-draw jump
-        a = a1 * a;
-    }
-    // Ordered on the launch's stream; a copy from pageable memory has consumed the host buffer
-    // when the call returns.
-    VPT_CUDA(cudaMemcpyAsync(c->d_jumps, table.data(), count * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+    // Computed on the device, ordered on the launch's stream: no host copy (a copy from pageable
+    // memory can block the host until the stream reaches it).
+    launch_sample_jump_table(c->d_jumps, first, count, s);
+    VPT_CUDA(cudaGetLastError());
     return VPT_OK;
 }
 

@@ -64,9 +64,6 @@ struct VptContextImpl {
     float nrc_termination = 0.0f;          // 0 = the reference's pathTerminationFactor
     uint32_t nrc_buf_index = 1;            // the first training iteration uses buffer 0
     std::mt19937 nrc_offset_rng{72139121}; // perFrameRng (renderer_main.cpp:1500)
-    // Second stream and events of a frame whose render pass overlaps the training pass.
-    cudaStream_t nrc_aux = nullptr;
-    cudaEvent_t nrc_ev_start = nullptr, nrc_ev_render = nullptr;
     void release_nrc();
 };
 

@@ -32,25 +32,6 @@ constexpr size_t kScratchBytes = kScratchHeader + kNoAllocMaxSpp * sizeof(ulongl
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Entry i: LCG jump (multiplier, increment) advancing a pixel's seed state by (first + i) * 2^40
-// draws, the start of that sample's stream.
-__global__ void noalloc_jump_table_kernel(ulonglong2* out, uint32_t first, uint32_t count) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    uint64_t delta = static_cast<uint64_t>(first + i) << kSampleStreamShift;
-    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
-    while (delta > 0) {
-        if (delta & 1ULL) {
-            acc_mult *= cur_mult;
-            acc_plus = acc_plus * cur_mult + cur_plus;
-        }
-        cur_plus = (cur_mult + 1ULL) * cur_plus;
-        cur_mult *= cur_mult;
-        delta >>= 1;
-    }
-    out[i] = make_ulonglong2(acc_mult, acc_plus);
-}
-
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
@@ -187,7 +168,7 @@ extern "C" int vpt_launch_plain_noalloc(const VptNoAllocTrace* a, void* stream) 
     // The scratch keeps the previous call's contents: clear what must start at zero.
     if (cudaMemsetAsync(scratch, 0, kScratchHeader, s) != cudaSuccess)
         return ctx_set_error(VPT_ERR_CUDA, "vpt_launch_plain_noalloc: clearing the scratch failed");
-    if (tp.stream_mode == 1) noalloc_jump_table_kernel<<<(a->spp + 127) / 128, 128, 0, s>>>(jumps, a->stream_base, a->spp);
+    if (tp.stream_mode == 1) launch_sample_jump_table(jumps, a->stream_base, a->spp, s);
 
     const int threads = 128;
     const bool grid_maj = f.majorant_mode == 1;

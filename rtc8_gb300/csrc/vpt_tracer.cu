@@ -106,6 +106,31 @@ __device__ __forceinline__ void write_query(float* q, V3 pos, V3 vout, float rou
     p[6] = make_float2(0.0f, 0.0f);
 }
 
+// Work order of the training pass: item -> pixel of the training image, class by class, where
+// the class of a pixel is (its position in the 4x4 tile + offset) % 16 and class 0 holds the
+// unbiased suffixes (optix_pathtracing_kernels.cu:60-66). The long unbiased paths thus gather in
+// the first warps and CTAs, and the CTAs of the short biased suffixes retire early, freeing their
+// SM slots for the render pass that runs concurrently. Records stay at the reference's pixel
+// index; only the order in which the pixels are traced changes.
+__device__ __forceinline__ void train_item_to_pixel(uint32_t item, uint32_t w, uint32_t h, uint32_t offset,
+                                                    uint32_t* px, uint32_t* py) {
+    const uint32_t off = offset % 16;
+    for (uint32_t k = 0; k < 16; ++k) {
+        const uint32_t p = (k + 16 - off) % 16;  // tile position with (p + offset) % 16 == k
+        const uint32_t a = p % 4, b = p / 4;
+        const uint32_t cx = w > a ? (w - a + 3) / 4 : 0, cy = h > b ? (h - b + 3) / 4 : 0;
+        const uint32_t n = cx * cy;
+        if (item < n) {
+            *px = a + 4 * (item % cx);
+            *py = b + 4 * (item / cx);
+            return;
+        }
+        item -= n;
+    }
+    *px = 0;  // not reached for item < w * h
+    *py = 0;
+}
+
 // kMode: kModePlain (pathTrace), kModeRenderNrc (pathTraceWithNRC) or kModeTrainNrc
 // (generateTrainingData), optix_pathtracing_kernels.cu:438-448.
 template <bool kGridMajorant, bool kLog, int kMode>
@@ -160,19 +185,30 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
 
     // Radiance-cache passes: one sample per pixel of the pass image (the training image has the
     // adaptive size prepared on the device), RNG states of the full image's per-pixel buffer.
+    // kModeComboNrc runs one training pass and one batched render pass as ONE launch: work items
+    // [0, num_train) are the training pixels, the rest the render samples, so lanes that finish
+    // their training suffix go on with render samples and no SM slot idles behind the longest
+    // suffixes. is_train tells a lane which kind of item it traces.
     constexpr bool kNrc = kMode != kModePlain;
-    constexpr bool kTrain = kMode == kModeTrainNrc;
+    constexpr bool kCombo = kMode == kModeComboNrc;
+    constexpr bool kMayTrain = kMode == kModeTrainNrc || kCombo;
+    bool is_train = kMode == kModeTrainNrc;
     uint32_t img_w = static_cast<uint32_t>(P.width), img_h = static_cast<uint32_t>(P.height);
-    uint32_t num_items = num_pixels;
-    if constexpr (kTrain) {
-        img_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
-        img_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
-        num_items = min(img_w * img_h, num_pixels);
+    uint32_t num_items = num_pixels, num_train = 0, train_w = 0, train_h = 0;
+    if constexpr (kMayTrain) {
+        train_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
+        train_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
+        num_train = min(train_w * train_h, num_pixels);
+    }
+    if constexpr (kMode == kModeTrainNrc) {
+        num_items = num_train;
     } else if constexpr (kNrc) {
         // Sample-parallel streams: P.spp samples per pixel in one render pass, each its own
         // work item and record slot (sample-major: slot = sample * num_pixels + pixel).
         if (P.stream_mode == 1) num_items = num_pixels * P.spp;
+        if constexpr (kCombo) num_items += num_train;
     }
+    uint64_t* rng_buf = P.rng;  // per-pixel states the current sample continues (and writes back)
     uint32_t slot = 0;  // record index of the current sample in the pass buffers
     const float term_factor = P.nrc_termination > 0 ? P.nrc_termination : kPathTerminationFactor;
     const V3 wmin = bmin, wmax = bmax;
@@ -210,24 +246,38 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         st = ST_DONE;
                         break;
                     }
-                    slot = item;
-                    if (!kTrain && P.stream_mode == 1) {
-                        pixel = item % num_pixels;
-                        sample = item / num_pixels;
-                        const ulonglong2 jump = P.sample_jumps[sample];
-                        rng.state = jump.x * P.rng[pixel] + jump.y;
-                        st = ST_CAMERA;
-                        break;
-                    }
-                    pixel = item;  // linear index in the pass image
-                    const uint32_t px = item % img_w, py = item / img_w;
-                    rng_index = py * static_cast<uint32_t>(P.width) + px;
-                    rng.state = P.rng[rng_index];
+                    if constexpr (kCombo) is_train = item < num_train;
                     sample = 0;
-                    if constexpr (kTrain) {
+                    if (kMayTrain && is_train) {
+                        uint32_t px, py;
+                        train_item_to_pixel(item, train_w, train_h, P.nrc.counters[6], &px, &py);
+                        img_w = train_w;
+                        img_h = train_h;
+                        pixel = py * train_w + px;  // linear index in the training image
+                        slot = pixel;
+                        rng_index = py * static_cast<uint32_t>(P.width) + px;
+                        rng_buf = kCombo ? P.nrc.train_rng : P.rng;
+                        rng.state = rng_buf[rng_index];
                         // optix_pathtracing_kernels.cu:60-66: one unbiased suffix per 4x4 tile.
                         const uint32_t tile_index = (py % 4) * 4 + (px % 4);
                         unbiased = (tile_index + P.nrc.counters[6]) % 16 == 0;
+                        st = ST_CAMERA;
+                        break;
+                    }
+                    const uint32_t r = kCombo ? item - num_train : item;
+                    img_w = static_cast<uint32_t>(P.width);
+                    img_h = static_cast<uint32_t>(P.height);
+                    slot = r;
+                    rng_buf = P.rng;
+                    if (P.stream_mode == 1) {
+                        pixel = r % num_pixels;
+                        sample = r / num_pixels;
+                        const ulonglong2 jump = P.sample_jumps[sample];
+                        rng.state = jump.x * P.rng[pixel] + jump.y;
+                    } else {
+                        pixel = r;
+                        rng_index = r;
+                        rng.state = P.rng[rng_index];
                     }
                     st = ST_CAMERA;
                     break;
@@ -390,8 +440,8 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                     }
                     const RGB implicit = radiance * mis;
-                    if constexpr (!kTrain) contribution = contribution + throughput * implicit;
-                    if constexpr (kTrain) {
+                    if (!(kMayTrain && is_train)) contribution = contribution + throughput * implicit;
+                    if (kMayTrain && is_train) {
                         // :148-152: the environment hit completes the previous vertex's target.
                         if (prev_vertex != kInvalidVertex) {
                             float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(prev_vertex);
@@ -423,7 +473,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 float continue_prob = 1.0f;
                 bool rr_kill = false;
                 // Training suffixes apply Russian roulette from the third vertex (:256-257).
-                const int32_t rr_from = kTrain ? max(P.rr_start, 3) : P.rr_start;
+                const int32_t rr_from = (kMayTrain && is_train) ? max(P.rr_start, 3) : P.rr_start;
                 if (static_cast<int32_t>(path_length) >= rr_from) {
                     continue_prob = fminf(luminance(throughput) / init_importance, 1.0f);
                     if (rng.uniform() >= continue_prob) rr_kill = true;
@@ -439,17 +489,17 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     // spread exceeds the primary footprint (twice that for biased training suffixes).
                     bool ends_with_cache = rr_kill;
                     const float spread2 = sqrt_spread * sqrt_spread;
-                    if constexpr (kTrain) {
+                    if (kMayTrain && is_train) {
                         if (!unbiased) ends_with_cache |= spread2 > 2 * term_factor * primary_spread;
                     } else {
                         ends_with_cache |= spread2 > term_factor * primary_spread;
                     }
                     if (ends_with_cache) {
                         const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
-                        float* qdst = kTrain ? P.nrc.train_end_query : P.nrc.infer_query;
+                        float* qdst = (kMayTrain && is_train) ? P.nrc.train_end_query : P.nrc.infer_query;
                         write_query(qdst + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough, P.albedo, wmin,
                                     wmax);
-                        if constexpr (kTrain) {
+                        if (kMayTrain && is_train) {
                             P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         } else {
                             TerminalInfo ti;
@@ -554,7 +604,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         float gterm = lp_cos * 1.0f / 1.0f;
                         nee = fs * le * (vis * mis * gterm / area_pdf);
                     }
-                    if constexpr (!kTrain) contribution = contribution + throughput * nee;
+                    if (!(kMayTrain && is_train)) contribution = contribution + throughput * nee;
                     nee_value = nee;
                 }
                 if (P.max_bounces > 0 && static_cast<int32_t>(path_length) >= P.max_bounces) {
@@ -578,7 +628,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 RGB local_tp = fs * (fabsf(1.0f) / pdf);
                 throughput = throughput * local_tp;
                 dir_pdf = pdf;
-                if constexpr (kTrain) {
+                if (kMayTrain && is_train) {
                     // :358-409: record the training vertex (query, local throughput, link to the
                     // previous vertex, target initialised with the NEE estimate); a full buffer
                     // ends the suffix with a cache query.
@@ -617,7 +667,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 // optix_pathtracing_kernels.cu:413-432 (non-finite samples are dropped).
                 ++n_samples;
                 if constexpr (kNrc) {
-                    if constexpr (kTrain) {
+                    if (kMayTrain && is_train) {
                         if (!terminal_written)
                             P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
                     } else {
@@ -639,7 +689,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                         fc[1] = c.g;
                         fc[2] = c.b;
                     }
-                    if (kTrain || P.stream_mode != 1) P.rng[rng_index] = rng.state;
+                    if ((kMayTrain && is_train) || P.stream_mode != 1) rng_buf[rng_index] = rng.state;
                     st = ST_FETCH;
                     break;
                 }
@@ -756,7 +806,30 @@ __global__ void pool_majorants_kernel(const float* __restrict__ fine, int lx, in
     out[i] = m;
 }
 
+// Entry i: LCG jump (multiplier, increment) advancing a pixel's seed state by (first + i) * 2^40
+// draws, the start of that sample's stream (O(log) jump-ahead, Brown 1994).
+__global__ void sample_jump_table_kernel(ulonglong2* out, uint32_t first, uint32_t count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint64_t delta = static_cast<uint64_t>(first + i) << kSampleStreamShift;
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    out[i] = make_ulonglong2(acc_mult, acc_plus);
+}
+
 }  // namespace
+
+void launch_sample_jump_table(ulonglong2* out, uint32_t first, uint32_t count, cudaStream_t s) {
+    sample_jump_table_kernel<<<(count + 127) / 128, 128, 0, s>>>(out, first, count);
+}
 
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s) {
     finalize_mean_kernel<<<(n_values + 255) / 256, 256, 0, s>>>(sum, mean, n_values, 1.0 / samples);
@@ -794,6 +867,9 @@ const void* nrc_kernel_ptr(int mode, bool grid_majorant) {
     if (mode == kModeTrainNrc)
         return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeTrainNrc>)
                              : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeTrainNrc>);
+    if (mode == kModeComboNrc)
+        return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeComboNrc>)
+                             : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeComboNrc>);
     return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeRenderNrc>)
                          : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeRenderNrc>);
 }
@@ -801,16 +877,22 @@ const void* nrc_kernel_ptr(int mode, bool grid_majorant) {
 void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
                      cudaStream_t s) {
     dim3 grid(grid_ctas), block(threads);
+    const size_t sm = grid_majorant ? smem : 0;
     if (mode == kModeTrainNrc) {
         if (grid_majorant)
-            plain_trace_kernel<true, false, kModeTrainNrc><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, false, kModeTrainNrc><<<grid, block, sm, s>>>(p);
         else
-            plain_trace_kernel<false, false, kModeTrainNrc><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, false, kModeTrainNrc><<<grid, block, sm, s>>>(p);
+    } else if (mode == kModeComboNrc) {
+        if (grid_majorant)
+            plain_trace_kernel<true, false, kModeComboNrc><<<grid, block, sm, s>>>(p);
+        else
+            plain_trace_kernel<false, false, kModeComboNrc><<<grid, block, sm, s>>>(p);
     } else {
         if (grid_majorant)
-            plain_trace_kernel<true, false, kModeRenderNrc><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, false, kModeRenderNrc><<<grid, block, sm, s>>>(p);
         else
-            plain_trace_kernel<false, false, kModeRenderNrc><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, false, kModeRenderNrc><<<grid, block, sm, s>>>(p);
     }
 }
 

@@ -11,6 +11,7 @@ namespace vpt {
 constexpr int kModePlain = 0;      // pathTrace: accumulate full paths
 constexpr int kModeRenderNrc = 1;  // pathTraceWithNRC: short paths ending in a cache query
 constexpr int kModeTrainNrc = 2;   // generateTrainingData: training suffixes on the training image
+constexpr int kModeComboNrc = 3;   // a training pass and a batched render pass in one launch
 
 struct Sun {
     float dir[3];
@@ -69,6 +70,8 @@ void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int t
 void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
                      cudaStream_t s);
 const void* nrc_kernel_ptr(int mode, bool grid_majorant);
+// Jump table of sample-parallel streams first .. first + count - 1, computed on the device.
+void launch_sample_jump_table(ulonglong2* out, uint32_t first, uint32_t count, cudaStream_t s);
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
 void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int mx, int my, int mz, int factor,
                     cudaStream_t s);

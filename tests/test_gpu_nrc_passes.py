@@ -385,3 +385,54 @@ def test_training_pass_uses_its_own_states_with_sample_parallel_streams(cuda_dev
     assert same.mean() >= DECISION_PARITY
     assert r.device_errors() == 0
     r.close()
+
+
+def test_combined_training_and_render_launch_matches_separate_passes(cuda_device):
+    """The frame call's combined launch (training pixels, then render samples) gives the same
+    records as the separate training pass and batched render pass from the same states."""
+    import torch
+
+    cfg = small_config_mode(size=48, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=1)
+    vox, env = _scene(cfg)
+    spp = 2
+    a = _setup(cfg, vox, env)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=nrc.default_config(nrc.NRC_ENCODING_VOLUME))
+    trng0 = _np(a.nrc_views()["train_rng"]).view(np.uint64).copy()
+    a.nrc_frame(cache, 1, spp, True)
+    torch.cuda.synchronize()
+    va = a.nrc_views()
+    cnt = _np(va["counters"]).view(np.uint32).copy()
+    offset, tw, th = int(cnt[6]), int(cnt[2]), int(cnt[3])
+    ni = tw * th
+
+    b = _setup(cfg, vox, env)
+    vb = b.nrc_views()
+    assert np.array_equal(_np(vb["train_rng"]).view(np.uint64), trng0)
+    b.prepare_nrc(0, offset, True)
+    b.launch_generate_training(0)
+    b.launch_render_nrc_batch(spp)
+    torch.cuda.synchronize()
+    vb = b.nrc_views()
+    n = cfg.width * cfg.height * spp
+    for k in ("infer_terminal", "frame_contribution"):
+        np.testing.assert_array_equal(_np(va[k])[:n], _np(vb[k])[:n])
+    ta, tb = _np(va["infer_terminal"])[:n, 3].copy().view(np.uint32), _np(vb["infer_terminal"])[:n, 3].copy().view(np.uint32)
+    hq = (ta & 1) == 1
+    np.testing.assert_array_equal(_np(va["infer_query"])[:n][hq], _np(vb["infer_query"])[:n][hq])
+    assert np.array_equal(_np(va["train_rng"]).view(np.uint64), _np(vb["train_rng"]).view(np.uint64))
+    assert int(_np(vb["counters"]).view(np.uint32)[0]) == int(cnt[0])
+    sa = _np(va["train_suffix"]).view(np.uint32)[:ni]
+    sb = _np(vb["train_suffix"]).view(np.uint32)[:ni]
+    assert np.array_equal(sa >> 22, sb >> 22)
+    qa, qb = _np(va["train_query0"]), _np(vb["train_query0"])
+    ba = _np(va["train_vertex"])[:, 3].copy().view(np.uint32)
+    bb = _np(vb["train_vertex"])[:, 3].copy().view(np.uint32)
+    for ca, cb in zip(orc.suffix_chains(sa, ba, ni), orc.suffix_chains(sb, bb, ni)):
+        assert len(ca) == len(cb)
+        for ia, ib in zip(ca, cb):
+            np.testing.assert_array_equal(qa[ia], qb[ib])
+    assert a.device_errors() == 0 and b.device_errors() == 0 and cache.device_errors() == 0
+    cache.finalize()
+    a.close()
+    b.close()
