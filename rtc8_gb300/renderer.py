@@ -200,7 +200,7 @@ class Renderer:
         return {
             "infer_query": device_view(b.infer_query, (cap, 14), "<f4"),
             "infer_terminal": device_view(b.infer_terminal, (n, 4), "<f4"),
-            "train_suffix": device_view(b.train_suffix, (n,), "<i4"),
+            "train_suffix": device_view(b.train_suffix, (self.width * self.height,), "<i4"),
             "inferred": device_view(b.inferred, (cap, 3), "<f4"),
             "frame_contribution": device_view(b.frame_contribution, (n, 3), "<f4"),
             "train_query0": device_view(b.train_query[0], (tb, 14), "<f4"),
