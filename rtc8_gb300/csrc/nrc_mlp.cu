@@ -143,10 +143,16 @@ __device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* til
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int f = 0; f < 12; ++f) {
+                // sin / cos(pi v) with v = x 2^f exact: v = m + r (m integer, r in [0, 1)), so
+                // sin(pi v) = (-1)^m sin(pi r) and likewise cos; the hardware approximation on
+                // [0, pi) is accurate to ~4e-7, far below the FP16 rounding of the features.
+                const float v = q[a] * static_cast<float>(1 << f);
+                const float m = floorf(v);
                 float s, c;
-                sincospif(q[a] * static_cast<float>(1 << f), &s, &c);
-                w.push(s);
-                w.push(c);
+                __sincosf(kPiF * (v - m), &s, &c);
+                const float sign = (static_cast<int>(m) & 1) ? -1.0f : 1.0f;
+                w.push(sign * s);
+                w.push(sign * c);
             }
         const float scale[2] = {1.0f / 3.14159265f, 1.0f / 6.28318531f};
 #pragma unroll
@@ -219,50 +225,61 @@ constexpr uint32_t kErrTimeout = 1u;
 __host__ __device__ __forceinline__ uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
 // ------------------------------------------------------------------------------ inference
-template <int IN>
-__global__ void __launch_bounds__(kTile) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
-                                                          const float* __restrict__ in, const uint32_t* __restrict__ dev_n,
-                                                          uint32_t n_max, float* __restrict__ out,
-                                                          unsigned int* __restrict__ err) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    const int tid = threadIdx.x, warp = tid >> 5;
-    uint8_t* s_w = smem;
-    uint8_t* s_a0 = smem + align_up(ly.blob_bytes, 1024);
-    uint8_t* s_h = s_a0 + kTile * IN * 2;
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_h + kTile * kWidth * 2);
-    uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_bar + 1);
+// G independent groups of 128 threads per CTA, each with its own 128-row tile, mbarrier and 64
+// TMEM columns, share one copy of the weights in shared memory. The groups' per-layer chains
+// (MMA, then the TMEM -> ReLU -> FP16 epilogue) are not synchronised with each other, so while
+// one group runs its epilogue or encodes its next input, the tensor cores serve another: G tiles
+// in flight per SM instead of one per CTA. A group reuses its input tile's shared memory for the
+// hidden activations (a layer's MMA has completed before its epilogue overwrites the operand).
+__host__ __device__ constexpr uint32_t infer_tile_bytes(int in_dim) { return (kTile * in_dim * 2 + 1023) / 1024 * 1024; }
 
-    for (uint32_t i = tid; i < ly.blob_bytes / 16; i += kTile)
+template <int IN, int G>
+__global__ void __launch_bounds__(kTile* G) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+                                                             const float* __restrict__ in,
+                                                             const uint32_t* __restrict__ dev_n, uint32_t n_max,
+                                                             float* __restrict__ out, unsigned int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr uint32_t kTileBytes = infer_tile_bytes(IN);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int g = tid / kTile, gt = tid % kTile;  // group, row of the tile
+    const uint32_t bar_id = 1 + g;                // named barrier of the group (0 = whole CTA)
+    uint8_t* s_w = smem;
+    uint8_t* s_t = smem + align_up(ly.blob_bytes, 1024) + g * kTileBytes;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + align_up(ly.blob_bytes, 1024) + G * kTileBytes);
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_bar + G);
+
+    for (uint32_t i = tid; i < ly.blob_bytes / 16; i += kTile * G)
         reinterpret_cast<uint4*>(s_w)[i] = __ldg(reinterpret_cast<const uint4*>(blob) + i);
-    if (warp == 0) tmem_alloc(s_slot, 64);
-    if (tid == 0) {
-        mbar_init(s_bar, 1);
+    if (warp == 0) tmem_alloc(s_slot, 64 * G);
+    if (gt == 0) {
+        mbar_init(s_bar + g, 1);
         mbar_fence_init();
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *s_slot;
-    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const uint32_t tmem_base = *s_slot;
+    const uint32_t tmem = tmem_base + 64 * g;                        // the group's columns
+    const uint32_t lane_base = static_cast<uint32_t>((warp % 4) * 32) << 16;  // lanes = rows of the tile
     const uint32_t n = dev_n ? min(*dev_n, n_max) : n_max;
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     uint32_t phase = 0;
     bool ok = true;
-    for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const uint32_t row = tile * kTile + tid;
+    for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += gridDim.x * G) {
+        const uint32_t row = tile * kTile + gt;
         float q[14];
         load_query(in, row, n, q);
-        encode_row(ly.enc, q, s_a0, tid, IN);
+        encode_row(ly.enc, q, s_t, gt, IN);
         fence_async_smem();
-        __syncthreads();
+        named_sync(bar_id, kTile);
         for (int j = 0; j < ly.L && ok; ++j) {
-            if (tid == 0) {
+            if (gt == 0) {
                 tc_fence_after();
-                issue_layer(tmem, smem_u32(j == 0 ? s_a0 : s_h), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
-                mma_commit(s_bar);
+                issue_layer(tmem, smem_u32(s_t), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
+                mma_commit(s_bar + g);
             }
-            ok = __syncthreads_and(mbar_wait(s_bar, phase));  // block-uniform decision
+            ok = named_sync_and(bar_id, kTile, mbar_wait(s_bar + g, phase));  // group-uniform decision
             phase ^= 1;
             tc_fence_after();
             if (!ok) break;
@@ -274,11 +291,11 @@ __global__ void __launch_bounds__(kTile) mlp_infer_kernel(const NetLayout ly, co
                     tmem_wait_ld();
 #pragma unroll
                     for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
-                    store_row16(s_h, tid, c * 16, kWidth, v);
+                    store_row16(s_t, gt, c * 16, kWidth, v);
                 }
                 tc_fence_before();
                 fence_async_smem();
-                __syncthreads();
+                named_sync(bar_id, kTile);
             } else {
                 float v[16];
                 tmem_ld16(tmem + lane_base, v);
@@ -289,15 +306,15 @@ __global__ void __launch_bounds__(kTile) mlp_infer_kernel(const NetLayout ly, co
                     for (int c = 0; c < 3; ++c) o[c] = ly.out_act == NRC_OUTPUT_EXP ? __expf(v[c]) : v[c];
                 }
                 tc_fence_before();
-                __syncthreads();
+                named_sync(bar_id, kTile);
             }
         }
     }
-    if (!ok && tid == 0) atomicOr(err, kErrTimeout);
+    if (!ok && gt == 0) atomicOr(err, kErrTimeout);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (warp == 0) tmem_dealloc(tmem_base, 64 * G);
 }
 
 // ------------------------------------------------------------------------------ training
@@ -607,8 +624,26 @@ __global__ void selftest_kernel(const float* __restrict__ A, const float* __rest
 }
 
 // ------------------------------------------------------------------------------ host side
-uint32_t infer_smem(const NetLayout& l) {
-    return align_up(l.blob_bytes, 1024) + kTile * l.in_dim * 2 + kTile * kWidth * 2 + 16;
+uint32_t infer_smem(const NetLayout& l, int groups) {
+    return align_up(l.blob_bytes, 1024) + groups * infer_tile_bytes(l.in_dim) + groups * 8 + 16;
+}
+constexpr uint32_t kMaxSmemOptIn = 232448;  // 227 KB per CTA
+// Largest tile-group count (4, 2 or 1) whose shared memory fits one CTA.
+int infer_groups(const NetLayout& l) {
+    for (int g = 4; g > 1; g /= 2)
+        if (infer_smem(l, g) <= kMaxSmemOptIn) return g;
+    return 1;
+}
+const void* infer_kernel_ptr(int enc, int groups) {
+    const bool vol = enc == NRC_ENCODING_VOLUME;
+    switch (groups) {
+    case 4: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 4>)
+                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 4>);
+    case 2: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 2>)
+                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 2>);
+    default: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 1>)
+                        : reinterpret_cast<const void*>(mlp_infer_kernel<64, 1>);
+    }
 }
 uint32_t train_smem(const NetLayout& l) {
     return align_up(l.blob_bytes, 1024) + kTile * l.in_dim * 2 + (l.L - 1) * kTile * kWidth * 2 +
@@ -624,6 +659,7 @@ struct NrcHandle {
     NrcConfig cfg;
     NetLayout ly;
     int num_sms = 0;
+    int infer_groups = 1;  // 128-row tiles in flight per inference CTA
     float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *ema = nullptr, *loss = nullptr;
     uint8_t *blob_train = nullptr, *blob_infer = nullptr;
     unsigned int* err = nullptr;
@@ -731,9 +767,8 @@ int nrc_create(const NrcConfig* cfg, NrcHandle** out) {
         return rc;
     }
     const bool vol = cfg->encoding == NRC_ENCODING_VOLUME;
-    if ((rc = set_kernel_smem(vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144>)
-                                  : reinterpret_cast<const void*>(mlp_infer_kernel<64>),
-                              infer_smem(h->ly))) ||
+    h->infer_groups = infer_groups(h->ly);
+    if ((rc = set_kernel_smem(infer_kernel_ptr(cfg->encoding, h->infer_groups), infer_smem(h->ly, h->infer_groups))) ||
         (rc = set_kernel_smem(vol ? reinterpret_cast<const void*>(mlp_train_kernel<144>)
                                   : reinterpret_cast<const void*>(mlp_train_kernel<64>),
                               train_smem(h->ly)))) {
@@ -767,13 +802,28 @@ static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_
     if (!h || !in || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer: null argument");
     if (n == 0) return NRC_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    uint32_t tiles = (n + kTile - 1) / kTile;
-    uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(h->num_sms) * 2);
-    uint32_t smem = infer_smem(h->ly);
-    if (h->cfg.encoding == NRC_ENCODING_VOLUME)
-        mlp_infer_kernel<144><<<grid, kTile, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
-    else
-        mlp_infer_kernel<64><<<grid, kTile, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    const int G = h->infer_groups;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    const uint32_t grid = std::min<uint32_t>((tiles + G - 1) / G, static_cast<uint32_t>(h->num_sms));
+    const uint32_t smem = infer_smem(h->ly, G);
+    const bool vol = h->cfg.encoding == NRC_ENCODING_VOLUME;
+    const dim3 block(kTile * G);
+    if (G == 4) {
+        if (vol)
+            mlp_infer_kernel<144, 4><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+        else
+            mlp_infer_kernel<64, 4><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    } else if (G == 2) {
+        if (vol)
+            mlp_infer_kernel<144, 2><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+        else
+            mlp_infer_kernel<64, 2><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    } else {
+        if (vol)
+            mlp_infer_kernel<144, 1><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+        else
+            mlp_infer_kernel<64, 1><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+    }
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
 }
