@@ -83,88 +83,90 @@ NetLayout make_layout(int enc, int hidden, int out_act, float loss_scale) {
 }
 
 // ------------------------------------------------------------------------------ encodings
-// Writes the FP16 encoded input of one query into row `r` of a [128][in_dim] core-matrix tile.
-// Features are produced 8 at a time (one 16-byte store per core-matrix row).
-struct RowWriter {
-    uint8_t* base;
-    int r, K;
-    float buf[8];
-    int n = 0, chunk = 0;
-    __device__ __forceinline__ void push(float v) {
-        buf[n++] = v;
-        if (n == 8) flush();
-    }
-    __device__ __forceinline__ void flush() {
-        uint4 w;
-        w.x = pack_half2(buf[0], buf[1]);
-        w.y = pack_half2(buf[2], buf[3]);
-        w.z = pack_half2(buf[4], buf[5]);
-        w.w = pack_half2(buf[6], buf[7]);
-        *reinterpret_cast<uint4*>(base + cm_offset(r, chunk * 8, K)) = w;
-        ++chunk;
-        n = 0;
-    }
-    __device__ __forceinline__ void pad_to(int K_) {
-        while (chunk * 8 + n < K_) push(0.0f);
-    }
-};
+// The FP16 encoded input of one query goes into row `r` of a [128][K] core-matrix tile, eight
+// features (one 16-byte store) at a time. Every feature index is a compile-time constant after
+// unrolling, so the features stay in registers.
+__device__ __forceinline__ void store8(uint8_t* tile, int r, int chunk, int K, const float (&v)[8]) {
+    uint4 w;
+    w.x = pack_half2(v[0], v[1]);
+    w.y = pack_half2(v[2], v[3]);
+    w.z = pack_half2(v[4], v[5]);
+    w.w = pack_half2(v[6], v[7]);
+    *reinterpret_cast<uint4*>(tile + cm_offset(r, chunk * 8, K)) = w;
+}
 
 __device__ __forceinline__ float one_blob(float x, int b, int nbins) {
     float z = (x - (b + 0.5f) / nbins) * nbins;
     return __expf(-0.5f * z * z);
 }
 
-// NRC_ENCODING_REFERENCE: TriangleWave(12) x 3, OneBlob(4) x 5 (angles / pi, / 2pi), identity x 6.
-// NRC_ENCODING_VOLUME: sin/cos(pi 2^f x) x 12 x 3, OneBlob(32) on vOut theta / pi and phi / 2pi,
-// identity on the local density (roughness slot) and the albedo (diffuse.r).
+// NRC_ENCODING_REFERENCE (64 features): TriangleWave(12) on the 3 position coordinates
+// (feature 12a + f), OneBlob(4) on the 5 angle / roughness inputs, angles divided by pi or 2 pi
+// (feature 36 + 4a + b), identity on the 6 reflectance values (56..61), 2 zeros.
+__device__ __forceinline__ float reference_feature(int i, const float* q) {
+    if (i < 36) {
+        const float v = q[i / 12] * static_cast<float>(1 << (i % 12));
+        const float fr = v - floorf(v);
+        return 2.0f * fabsf(fr - 0.5f);
+    }
+    if (i < 56) {
+        const int a = (i - 36) / 4, b = (i - 36) % 4;
+        const float scale = a == 4 ? 1.0f : ((a & 1) ? 1.0f / 6.28318531f : 1.0f / 3.14159265f);
+        return one_blob(q[3 + a] * scale, b, 4);
+    }
+    if (i < 62) return q[8 + (i - 56)];
+    return 0.0f;
+}
+
+// NRC_ENCODING_VOLUME (144 features): sin and cos of pi 2^f x for the 3 position coordinates
+// (features 2(12a + f) and 2(12a + f) + 1), OneBlob(32) on vOut theta / pi and phi / 2 pi
+// (feature 72 + 32a + b), the local density (roughness slot) and the albedo (diffuse.r), 6 zeros.
+__device__ __forceinline__ void encode_row_volume(const float* q, uint8_t* tile, int r) {
+    constexpr int K = 144;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int p = 4 * k + i;  // = 12a + f
+            // sin / cos(pi v) with v = x 2^f exact: v = m + r (m integer, r in [0, 1)), so
+            // sin(pi v) = (-1)^m sin(pi r) and likewise cos; the hardware approximation on
+            // [0, pi) is accurate to ~4e-7, far below the FP16 rounding of the features.
+            const float x = q[p / 12] * static_cast<float>(1 << (p % 12));
+            const float m = floorf(x);
+            float sn, cs;
+            __sincosf(kPiF * (x - m), &sn, &cs);
+            const float sign = (static_cast<int>(m) & 1) ? -1.0f : 1.0f;
+            v[2 * i] = sign * sn;
+            v[2 * i + 1] = sign * cs;
+        }
+        store8(tile, r, k, K, v);
+    }
+    const float theta = q[5] * (1.0f / 3.14159265f), phi = q[6] * (1.0f / 6.28318531f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = one_blob(k < 4 ? theta : phi, 8 * (k % 4) + i, 32);
+        store8(tile, r, 9 + k, K, v);
+    }
+    const float last[8] = {q[7], q[8], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    store8(tile, r, 17, K, last);
+}
+
 __device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* tile, int r, int K) {
-    RowWriter w{tile, r, K};
     if (enc == NRC_ENCODING_REFERENCE) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < 8; ++k) {
+            float v[8];
 #pragma unroll
-            for (int f = 0; f < 12; ++f) {
-                float v = q[a] * static_cast<float>(1 << f);
-                float fr = v - floorf(v);
-                w.push(2.0f * fabsf(fr - 0.5f));
-            }
-        const float scale[5] = {1.0f / 3.14159265f, 1.0f / 6.28318531f, 1.0f / 3.14159265f, 1.0f / 6.28318531f, 1.0f};
-#pragma unroll
-        for (int a = 0; a < 5; ++a) {
-            float x = q[3 + a] * scale[a];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) w.push(one_blob(x, b, 4));
+            for (int i = 0; i < 8; ++i) v[i] = reference_feature(8 * k + i, q);
+            store8(tile, r, k, 64, v);
         }
-#pragma unroll
-        for (int a = 0; a < 6; ++a) w.push(q[8 + a]);
-        w.pad_to(64);
     } else {
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int f = 0; f < 12; ++f) {
-                // sin / cos(pi v) with v = x 2^f exact: v = m + r (m integer, r in [0, 1)), so
-                // sin(pi v) = (-1)^m sin(pi r) and likewise cos; the hardware approximation on
-                // [0, pi) is accurate to ~4e-7, far below the FP16 rounding of the features.
-                const float v = q[a] * static_cast<float>(1 << f);
-                const float m = floorf(v);
-                float s, c;
-                __sincosf(kPiF * (v - m), &s, &c);
-                const float sign = (static_cast<int>(m) & 1) ? -1.0f : 1.0f;
-                w.push(sign * s);
-                w.push(sign * c);
-            }
-        const float scale[2] = {1.0f / 3.14159265f, 1.0f / 6.28318531f};
-#pragma unroll
-        for (int a = 0; a < 2; ++a) {
-            float x = q[5 + a] * scale[a];
-#pragma unroll
-            for (int b = 0; b < 32; ++b) w.push(one_blob(x, b, 32));
-        }
-        w.push(q[7]);
-        w.push(q[8]);
-        w.pad_to(144);
+        encode_row_volume(q, tile, r);
     }
+    (void)K;
 }
 
 __device__ __forceinline__ void load_query(const float* __restrict__ in, uint32_t row, uint32_t n, float* q) {
@@ -234,7 +236,7 @@ __host__ __device__ __forceinline__ uint32_t align_up(uint32_t x, uint32_t a) { 
 __host__ __device__ constexpr uint32_t infer_tile_bytes(int in_dim) { return (kTile * in_dim * 2 + 1023) / 1024 * 1024; }
 
 template <int IN, int G>
-__global__ void __launch_bounds__(kTile* G) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+__global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
                                                              const float* __restrict__ in,
                                                              const uint32_t* __restrict__ dev_n, uint32_t n_max,
                                                              float* __restrict__ out, unsigned int* __restrict__ err) {
@@ -285,13 +287,18 @@ __global__ void __launch_bounds__(kTile* G) mlp_infer_kernel(const NetLayout ly,
             if (!ok) break;
             if (j < ly.L - 1) {
 #pragma unroll
-                for (int c = 0; c < kWidth / 16; ++c) {
-                    float v[16];
-                    tmem_ld16(tmem + lane_base + c * 16, v);
+                for (int c = 0; c < kWidth / 32; ++c) {  // two TMEM loads in flight per wait
+                    float v0[16], v1[16];
+                    tmem_ld16(tmem + lane_base + c * 32, v0);
+                    tmem_ld16(tmem + lane_base + c * 32 + 16, v1);
                     tmem_wait_ld();
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
-                    store_row16(s_t, gt, c * 16, kWidth, v);
+                    for (int i = 0; i < 16; ++i) {
+                        v0[i] = fmaxf(v0[i], 0.0f);
+                        v1[i] = fmaxf(v1[i], 0.0f);
+                    }
+                    store_row16(s_t, gt, c * 32, kWidth, v0);
+                    store_row16(s_t, gt, c * 32 + 16, kWidth, v1);
                 }
                 tc_fence_before();
                 fence_async_smem();
