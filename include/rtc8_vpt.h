@@ -256,10 +256,11 @@ int vpt_nrc_get_buffers(VptContext* ctx, VptNrcBuffers* out);
  * encoding of rtc8_nrc.h; the reference writes roughness 0 in a medium, 0 = that). The cache's
  * target scale is VptFrameParams.radiance_scale. */
 int vpt_nrc_set_query_density(VptContext* ctx, int32_t query_density);
-/* Path-spread termination factor c (pathTerminationFactor, renderer_shared.h:11): a render path
- * ends with a cache query once its spread exceeds c times the primary footprint, a biased
- * training suffix at 2c (optix_pathtracing_kernels.cu:282-289). 0 = the reference's 0.01. */
-int vpt_nrc_set_termination_factor(VptContext* ctx, float factor);
+/* Path-spread termination factors (pathTerminationFactor c, renderer_shared.h:11): a render path
+ * ends with a cache query once its spread exceeds render_factor times the primary footprint, a
+ * biased training suffix at train_factor (optix_pathtracing_kernels.cu:282-289 uses c and 2c).
+ * render_factor 0 = the reference's 0.01; train_factor 0 = 2 x render_factor. */
+int vpt_nrc_set_termination_factor(VptContext* ctx, float render_factor, float train_factor);
 /* prepareNRC(offsetToSelectUnbiasedPath, isNewSequence) on training buffer `buffer_index`
  * (nrc_set_up_kernels.cu:4-44). */
 int vpt_prepare_nrc(VptContext* ctx, void* stream, uint32_t buffer_index, uint32_t offset, int32_t new_sequence);

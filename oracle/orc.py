@@ -301,6 +301,7 @@ class OrcNrcSink(C.Structure):
         ("img_h", C.c_uint32),
         ("unbiased_offset", C.c_uint32),
         ("termination", C.c_float),
+        ("train_termination", C.c_float),
         ("infer_query", f32p),
         ("terminal_tp", f32p),
         ("terminal_bits", u32p),
@@ -338,7 +339,8 @@ def pass_lib():
 
 
 def nrc_pass(sc: OracleScene, rng: np.ndarray, mode: int, img_w: int, img_h: int, unbiased_offset: int = 0,
-             density_query: bool = False, log: bool = False, termination: float = 0.0) -> dict:
+             density_query: bool = False, log: bool = False, termination: float = 0.0,
+             train_termination: float = 0.0) -> dict:
     """One radiance-cache pass (mode 1 render, 2 training) on the pass image img_w x img_h;
     `rng` (the full image's per-pixel states) is advanced in place."""
     n = img_w * img_h
@@ -358,6 +360,7 @@ def nrc_pass(sc: OracleScene, rng: np.ndarray, mode: int, img_w: int, img_h: int
     k.mode, k.density_query, k.img_w, k.img_h = mode, int(density_query), img_w, img_h
     k.unbiased_offset = unbiased_offset & 0xFFFFFFFF
     k.termination = termination
+    k.train_termination = train_termination
     for name, t in (("infer_query", C.c_float), ("terminal_tp", C.c_float), ("terminal_bits", C.c_uint32),
                     ("frame_contribution", C.c_float), ("train_suffix", C.c_uint32), ("train_query", C.c_float),
                     ("train_target", C.c_float), ("train_local_tp", C.c_float), ("train_bits", C.c_uint32),

@@ -588,6 +588,7 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
     const bool with_nrc = nrc != nullptr;
     const bool train = with_nrc && nrc->mode == 2;
     const float term_factor = with_nrc && nrc->termination > 0 ? nrc->termination : ORC_NRC_TERMINATION_FACTOR;
+    const float train_term_factor = with_nrc && nrc->train_termination > 0 ? nrc->train_termination : 2 * term_factor;
     const float img_w = with_nrc ? static_cast<float>(nrc->img_w) : static_cast<float>(s.width);
     const float img_h = with_nrc ? static_cast<float>(nrc->img_h) : static_cast<float>(s.height);
     V3 origin, dir;
@@ -692,7 +693,7 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
             bool ends_with_cache = rr_kill;
             const float spread2 = sqrt_spread * sqrt_spread;
             if (train) {
-                if (!unbiased) ends_with_cache |= spread2 > 2 * term_factor * primary_spread;
+                if (!unbiased) ends_with_cache |= spread2 > train_term_factor * primary_spread;
             } else {
                 ends_with_cache |= spread2 > term_factor * primary_spread;
             }

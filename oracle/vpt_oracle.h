@@ -90,6 +90,7 @@ typedef struct OrcNrcSink {
     uint32_t img_w, img_h;     /* pass image (training image size in mode 2) */
     uint32_t unbiased_offset;  /* offsetToSelectUnbiasedPath */
     float termination;         /* path-spread termination factor (0 = 0.01) */
+    float train_termination;   /* biased training suffixes (0 = 2 x termination) */
     float* infer_query;        /* 14 per pass pixel */
     float* terminal_tp;        /* mode 1: 3 per pixel */
     uint32_t* terminal_bits;   /* mode 1: hasQuery | pathLength << 1 */

@@ -103,7 +103,7 @@ _VPT = {
     "vpt_nrc_enable": (C.c_int, [C.c_void_p]),
     "vpt_nrc_get_buffers": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_nrc_set_query_density": (C.c_int, [C.c_void_p, C.c_int32]),
-    "vpt_nrc_set_termination_factor": (C.c_int, [C.c_void_p, C.c_float]),
+    "vpt_nrc_set_termination_factor": (C.c_int, [C.c_void_p, C.c_float, C.c_float]),
     "vpt_prepare_nrc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]),
     "vpt_launch_generate_training": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vpt_propagate": (C.c_int, [C.c_void_p, C.c_void_p]),

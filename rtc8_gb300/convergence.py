@@ -85,7 +85,8 @@ def plain_curve(cfg: SceneConfig, ref: np.ndarray, target: float, chunk_spp: int
 
 def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None, spp_per_frame: int = 8,
               eval_every: int = 1, max_frames: int = 4096, time_budget: float = 60.0,
-              query_density: bool = True, termination: float = 0.0, warmup_frames: int = 0) -> dict:
+              query_density: bool = True, termination: float = 0.0, warmup_frames: int = 0,
+              train_termination: float = 0.0) -> dict:
     """relMSE of the radiance-cache renderer after every `eval_every` frames of `spp_per_frame`
     samples per pixel (the reference renders 8 samples per frame, renderer_main.cpp:359). The
     images of the first frame and of `warmup_frames` more frames (rendered while the cache is
@@ -98,7 +99,7 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg)
     r.nrc_set_query_density(query_density)
-    r.nrc_set_termination_factor(termination)
+    r.nrc_set_termination_factor(termination, train_termination)
     cache = nrc.NeuralRadianceCache()
     cache.initialize(config=net_config or nrc.default_config(nrc.NRC_ENCODING_VOLUME))
     curve, t, frames, reached = [], 0.0, 0, None

@@ -144,6 +144,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc_buf = buf;
     tp.nrc_density_query = c->nrc_query_density;
     tp.nrc_termination = c->nrc_termination;
+    tp.nrc_train_termination = c->nrc_train_termination;
     NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     const int threads = c->threads > 0 ? c->threads : 128;
     const bool grid_maj = c->frame.majorant_mode == 1;
@@ -238,10 +239,12 @@ int vpt_nrc_set_query_density(VptContext* c, int32_t query_density) {
     return VPT_OK;
 }
 
-int vpt_nrc_set_termination_factor(VptContext* c, float factor) {
-    if (!c || !(factor >= 0.0f) || !(factor < 1e30f))
+int vpt_nrc_set_termination_factor(VptContext* c, float render_factor, float train_factor) {
+    if (!c || !(render_factor >= 0.0f) || !(render_factor < 1e30f) || !(train_factor >= 0.0f) ||
+        !(train_factor < 1e30f))
         return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_set_termination_factor: bad arguments");
-    c->nrc_termination = factor;
+    c->nrc_termination = render_factor;
+    c->nrc_train_termination = train_factor;
     return VPT_OK;
 }
 

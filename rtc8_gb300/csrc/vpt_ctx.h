@@ -62,6 +62,7 @@ struct VptContextImpl {
     NrcBuffers* nrc = nullptr;
     int32_t nrc_query_density = 0;
     float nrc_termination = 0.0f;          // 0 = the reference's pathTerminationFactor
+    float nrc_train_termination = 0.0f;    // 0 = twice the render factor
     uint32_t nrc_buf_index = 1;            // the first training iteration uses buffer 0
     std::mt19937 nrc_offset_rng{72139121}; // perFrameRng (renderer_main.cpp:1500)
     void release_nrc();

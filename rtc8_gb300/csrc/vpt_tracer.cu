@@ -211,6 +211,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
     uint64_t* rng_buf = P.rng;  // per-pixel states the current sample continues (and writes back)
     uint32_t slot = 0;  // record index of the current sample in the pass buffers
     const float term_factor = P.nrc_termination > 0 ? P.nrc_termination : kPathTerminationFactor;
+    // Biased training suffixes end at twice the render factor (optix_pathtracing_kernels.cu:
+    // 284-285) unless a separate training factor is set.
+    const float train_term_factor = P.nrc_train_termination > 0 ? P.nrc_train_termination : 2 * term_factor;
     const V3 wmin = bmin, wmax = bmax;
     uint32_t rng_index = 0;
     float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
@@ -490,7 +493,7 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                     bool ends_with_cache = rr_kill;
                     const float spread2 = sqrt_spread * sqrt_spread;
                     if (kMayTrain && is_train) {
-                        if (!unbiased) ends_with_cache |= spread2 > 2 * term_factor * primary_spread;
+                        if (!unbiased) ends_with_cache |= spread2 > train_term_factor * primary_spread;
                     } else {
                         ends_with_cache |= spread2 > term_factor * primary_spread;
                     }

@@ -60,6 +60,7 @@ struct TraceParams {
     uint32_t nrc_buf;           // training buffer of this frame (nrcBufferIndex)
     int32_t nrc_density_query;  // 1: the query's roughness slot carries density / density_coeff
     float nrc_termination;      // path-spread termination factor c (0 = 0.01, renderer_shared.h:11)
+    float nrc_train_termination;  // factor of biased training suffixes (0 = 2c)
 };
 
 // Majorant grids up to this many cells are staged in shared memory (32 KB).

@@ -216,8 +216,9 @@ class Renderer:
             "stats": device_view(b.stats, (18,), "<f4"),
         }
 
-    def nrc_set_termination_factor(self, factor: float) -> None:
-        check(self.lib.vpt_nrc_set_termination_factor(self.ctx, factor), "vpt_nrc_set_termination_factor")
+    def nrc_set_termination_factor(self, render_factor: float, train_factor: float = 0.0) -> None:
+        check(self.lib.vpt_nrc_set_termination_factor(self.ctx, render_factor, train_factor),
+              "vpt_nrc_set_termination_factor")
 
     def nrc_set_query_density(self, on: bool) -> None:
         check(self.lib.vpt_nrc_set_query_density(self.ctx, int(on)), "vpt_nrc_set_query_density")

@@ -77,11 +77,12 @@ def test_render_pass_matches_oracle(cuda_device, density_query, termination):
     r.close()
 
 
-def _train_pass(cfg, vox, env, offset, density_query=False):
+def _train_pass(cfg, vox, env, offset, density_query=False, termination=0.0, train_termination=0.0):
     import torch
 
     r = _setup(cfg, vox, env)
     r.nrc_set_query_density(density_query)
+    r.nrc_set_termination_factor(termination, train_termination)
     rng0 = r.rng_states().copy()
     r.prepare_nrc(0, offset, True)
     r.launch_generate_training(0)
@@ -89,15 +90,15 @@ def _train_pass(cfg, vox, env, offset, density_query=False):
     return r, rng0
 
 
-@pytest.mark.parametrize("cfg_kind", ["reference", "config"])
-def test_training_pass_matches_oracle(cuda_device, cfg_kind):
+@pytest.mark.parametrize("cfg_kind,train_termination", [("reference", 0.0), ("config", 0.0), ("config", 0.05)])
+def test_training_pass_matches_oracle(cuda_device, cfg_kind, train_termination):
     if cfg_kind == "reference":
         cfg = small_reference_mode(size=64, n=32, sigma=60.0)
     else:
         cfg = small_config_mode(size=64, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=0)
     vox, env = _scene(cfg)
     offset = 2654435761
-    r, rng0 = _train_pass(cfg, vox, env, offset)
+    r, rng0 = _train_pass(cfg, vox, env, offset, termination=0.02, train_termination=train_termination)
     v = r.nrc_views()
     cnt = _np(v["counters"]).view(np.uint32)
     tw, th = int(cnt[2]), int(cnt[3])
@@ -115,7 +116,8 @@ def test_training_pass_matches_oracle(cuda_device, cfg_kind):
 
     sc = orc.scene_from_config(cfg, vox, env)
     o_rng = rng0.copy()
-    o = orc.nrc_pass(sc, o_rng, 2, tw, th, unbiased_offset=offset)
+    o = orc.nrc_pass(sc, o_rng, 2, tw, th, unbiased_offset=offset, termination=0.02,
+                     train_termination=train_termination)
     g_chains = orc.suffix_chains(g_suffix, g_vbits, ni)
     o_chains = orc.suffix_chains(o["train_suffix"], o["train_bits"], ni)
     # pixel (px, py) of the training image uses the full image's stream py * width + px
