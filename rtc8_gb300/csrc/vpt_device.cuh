@@ -232,74 +232,6 @@ __device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz, LeafCac
     return lerp(vx, vx1, wx);
 }
 
-// sample_trilinear for the first n of K points with the memory accesses of all points in flight
-// together: the leaf-table reads of every point are issued first, then the 8 voxel reads of every
-// point, then the interpolations (same operations and order per point as sample_trilinear, so the
-// results are identical). Points whose stencil leaves their leaf take the general path.
-template <int K>
-__device__ __forceinline__ void sample_trilinear_multi(const Grid& g, const V3 (&xyz)[K], int n, LeafCache& cache,
-                                                       float (&out)[K]) {
-    float wx[K], wy[K], wz[K];
-    int32_t slot[K], off[K];
-    bool fast[K];
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-        const float fi = floorf(xyz[q].x), fj = floorf(xyz[q].y), fk = floorf(xyz[q].z);
-        wx[q] = xyz[q].x - fi;
-        wy[q] = xyz[q].y - fj;
-        wz[q] = xyz[q].z - fk;
-        const int i = static_cast<int>(fi), j = static_cast<int>(fj), k = static_cast<int>(fk);
-        const bool inside = static_cast<uint32_t>(i) < static_cast<uint32_t>(g.nx - 1) &&
-                            static_cast<uint32_t>(j) < static_cast<uint32_t>(g.ny - 1) &&
-                            static_cast<uint32_t>(k) < static_cast<uint32_t>(g.nz - 1);
-        fast[q] = q < n && inside && (i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7;
-        slot[q] = -1;
-        off[q] = ((i & 7) << 6) | ((j & 7) << 3) | (k & 7);
-        if (fast[q]) {
-            const int32_t key = ((i >> 3) * g.ly + (j >> 3)) * g.lz + (k >> 3);
-            if (key == cache.key) {
-                slot[q] = cache.slot;
-            } else {
-                slot[q] = __ldg(g.leaf_table + key);
-                cache.key = key;
-                cache.slot = slot[q];
-            }
-        }
-    }
-    float v[K][8];
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-        if (fast[q] && slot[q] >= 0) {
-            const float* p = g.leaf_values + static_cast<int64_t>(slot[q]) * 512 + off[q];
-            v[q][0] = __ldg(p);
-            v[q][1] = __ldg(p + 1);
-            v[q][2] = __ldg(p + 8);
-            v[q][3] = __ldg(p + 9);
-            v[q][4] = __ldg(p + 64);
-            v[q][5] = __ldg(p + 65);
-            v[q][6] = __ldg(p + 72);
-            v[q][7] = __ldg(p + 73);
-        }
-    }
-    auto lerp = [](float a, float b, float w) { return a + w * (b - a); };
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-        out[q] = 0.0f;
-        if (q >= n) continue;
-        if (!fast[q]) {
-            out[q] = sample_trilinear(g, xyz[q], cache);
-        } else if (slot[q] >= 0) {
-            float vy = lerp(v[q][0], v[q][1], wz[q]);
-            float vy1 = lerp(v[q][2], v[q][3], wz[q]);
-            const float vx = lerp(vy, vy1, wy[q]);
-            vy1 = lerp(v[q][6], v[q][7], wz[q]);
-            vy = lerp(v[q][4], v[q][5], wz[q]);
-            const float vx1 = lerp(vy, vy1, wy[q]);
-            out[q] = lerp(vx, vx1, wx[q]);
-        }
-    }
-}
-
 // util/Ray.h:343-363 + :512-520 (slab test, clipped to the ray's [tmin, tmax]).
 __device__ __forceinline__ bool clip_ray(V3 bmin, V3 bmax, V3 eye, V3 dir, float tmin, float tmax, float* t0o,
                                          float* t1o) {

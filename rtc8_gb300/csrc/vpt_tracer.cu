@@ -43,24 +43,10 @@ enum : uint32_t {
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
+// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp.
+constexpr int kCellStepsPerPass = 1;
 // Parked lanes of a warp that trigger a joint event phase.
 constexpr int kParkThreshold = 24;
-// Tentative collision points a tracking lane prepares per lookup round. The distances of delta
-// and ratio tracking do not depend on the densities, so a lane draws the next points of its
-// current majorant segment ahead and the warp looks them all up with the memory accesses in
-// flight together; the points are then processed in order, and a collision (or the step cap)
-// rewinds the lane's PCG32 state to just after the draws of that point, so the random stream and
-// every decision are those of the one-point-at-a-time algorithm.
-#ifndef VPT_POINTS_PER_ROUND
-#define VPT_POINTS_PER_ROUND 2
-#endif
-constexpr int kPointsPerRound = VPT_POINTS_PER_ROUND;
-
-// PCG32 state after `n` more draws.
-__device__ __forceinline__ uint64_t pcg_skip(uint64_t state, int n) {
-    for (int i = 0; i < n; ++i) state = state * 6364136223846793005ULL + 1ULL;
-    return state;
-}
 
 struct DdaState {
     int cell[3];
@@ -147,13 +133,8 @@ __device__ __forceinline__ void train_item_to_pixel(uint32_t item, uint32_t w, u
 
 // kMode: kModePlain (pathTrace), kModeRenderNrc (pathTraceWithNRC) or kModeTrainNrc
 // (generateTrainingData), optix_pathtracing_kernels.cu:438-448.
-// Resident CTAs of 128 threads per SM that the register allocation is bounded for.
-#ifndef VPT_TRACER_MIN_CTAS
-#define VPT_TRACER_MIN_CTAS 5
-#endif
-
 template <bool kGridMajorant, bool kLog, int kMode>
-__global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(const TraceParams P) {
+__global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P) {
     extern __shared__ float s_maj[];
     const Grid& g = P.grid;
     const float* maj_grid = g.maj;
@@ -191,10 +172,6 @@ __global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(c
     float t = 0, t1 = 0, maj = global_maj, texit = 0;
     uint32_t seg_steps = 0;
     DdaState dda;
-    // tentative points of the current lookup round
-    float t_pt[kPointsPerRound] = {}, u_pt[kPointsPerRound] = {};
-    int n_pts = 0;
-    uint64_t rng_round = 0;  // PCG32 state before the round's draws
 
     // NEE in flight
     V3 light_dir = v3(0, 1, 0);
@@ -255,6 +232,7 @@ __global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(c
         if ((ev_mask | tr_mask) == 0) break;
         const bool event_phase = ev_mask != 0 && (tr_mask == 0 || __popc(ev_mask) >= park_threshold);
         bool need_lookup = false, yield = false;
+        V3 lookup_pos = v3(0, 0, 0);
         while (!need_lookup && !yield && st != ST_DONE && (event_phase ? st != ST_STEP : st == ST_STEP)) {
             switch (st) {
             case ST_FETCH: {
@@ -397,48 +375,34 @@ __global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(c
                 break;
             }
             case ST_STEP: {
-                // Tentative points of this round, all inside the current majorant segment (the
-                // whole clipped segment with the global majorant, the current cell with the grid):
-                // distance draw, then (delta tracking) the acceptance draw. A draw that leaves
-                // the segment is put back; it is drawn again as the segment's exit when the round
-                // has no point, so the random stream is consumed in the reference's order.
-                n_pts = 0;
-                rng_round = rng.state;
-                float tt_last = t;
-#pragma unroll
-                for (int i = 0; i < kPointsPerRound; ++i) {
-                    if (kGridMajorant && !(maj > 0)) break;
-                    const uint64_t s_before = rng.state;
-                    const float tt = tt_last + -logf(1.0f - rng.uniform()) / maj;
-                    const bool inside = kGridMajorant ? (tt < texit) : (tt <= t1);  // false on NaN
-                    if (!inside) {
-                        rng.state = s_before;
-                        break;
-                    }
-                    tt_last = tt;
-                    t_pt[i] = tt;
-                    if (!shadow) u_pt[i] = rng.uniform();
-                    ++n_pts;
-                }
-                if (n_pts > 0) {
-                    t = tt_last;
-                    need_lookup = true;
-                    break;
-                }
                 if constexpr (!kGridMajorant) {
-                    // optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378:
-                    // the distance draw that leaves the segment (also on a NaN distance).
+                    // optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378.
                     t += -logf(1.0f - rng.uniform()) / maj;
-                    st = shadow ? ST_NEE_DONE : ST_ESCAPE;
-                } else {
-                    // Majorant-grid DDA: overshooting the cell's exit restarts sampling at the
-                    // exit (memoryless); empty cells are skipped without draws.
-                    bool seg_end = false;
-                    if (maj > 0) rng.uniform();
-                    t = texit;
-                    if (texit >= t1) {
-                        seg_end = true;
+                    if (!(t <= t1)) {  // also ends the segment on a NaN distance
+                        st = shadow ? ST_NEE_DONE : ST_ESCAPE;
                     } else {
+                        lookup_pos = seg_eye + seg_dir * t;
+                        need_lookup = true;
+                    }
+                } else {
+                    // Majorant-grid DDA: sample within the current cell; overshooting its exit
+                    // restarts at the exit (memoryless); empty cells are skipped without draws.
+                    bool seg_end = false;
+                    for (int c = 0; c < kCellStepsPerPass; ++c) {
+                        if (maj > 0) {
+                            float tt = t + -logf(1.0f - rng.uniform()) / maj;
+                            if (tt < texit) {
+                                t = tt;
+                                lookup_pos = seg_eye + seg_dir * t;
+                                need_lookup = true;
+                                break;
+                            }
+                        }
+                        t = texit;
+                        if (texit >= t1) {
+                            seg_end = true;
+                            break;
+                        }
                         // Advance along the axis whose boundary comes first (x, then y, then z on
                         // ties); written with selects so the DDA state stays in registers.
                         bool ax0 = dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2];
@@ -452,17 +416,17 @@ __global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(c
                             dda.cell[2] < 0 || dda.cell[2] >= g.mz) {
                             t = t1;
                             seg_end = true;
-                        } else {
-                            if (ax0) dda.tnext[0] += dda.tdelta[0];
-                            if (ax1) dda.tnext[1] += dda.tdelta[1];
-                            if (ax2) dda.tnext[2] += dda.tdelta[2];
-                            texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
-                            maj = P.density_coeff * cell_maj(maj_grid, g, dda);
+                            break;
                         }
+                        if (ax0) dda.tnext[0] += dda.tdelta[0];
+                        if (ax1) dda.tnext[1] += dda.tdelta[1];
+                        if (ax2) dda.tnext[2] += dda.tdelta[2];
+                        texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+                        maj = P.density_coeff * cell_maj(maj_grid, g, dda);
                     }
                     if (seg_end)
                         st = shadow ? ST_NEE_DONE : ST_ESCAPE;
-                    else
+                    else if (!need_lookup)
                         yield = true;  // let the warp's lookups run before crossing more cells
                 }
                 break;
@@ -782,46 +746,27 @@ __global__ void __launch_bounds__(128, VPT_TRACER_MIN_CTAS) plain_trace_kernel(c
         if (event_phase || !__any_sync(0xffffffffu, need_lookup)) continue;
 
         // ---------------------------------------------------------------- converged lookups
-        // Every lane of the round looks up its n_pts points together; the points are then
-        // processed in order exactly as single steps would be.
-        float dens[kPointsPerRound];
-        {
-            V3 idx[kPointsPerRound];
-#pragma unroll
-            for (int i = 0; i < kPointsPerRound; ++i) idx[i] = world_to_index(g, seg_eye + seg_dir * t_pt[i]);
-            sample_trilinear_multi<kPointsPerRound>(g, idx, need_lookup ? n_pts : 0, leaf_cache, dens);
-        }
+        float density = 0.0f;
+        if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos), leaf_cache);
 
         if (need_lookup) {
-            int stop = -1;  // point after which the round ends early (collision or step cap)
-#pragma unroll
-            for (int i = 0; i < kPointsPerRound; ++i) {
-                if (i >= n_pts || stop >= 0) continue;
-                const float density = P.density_coeff * dens[i];
-                ++n_lookups;
-                ++seg_steps;
-                if (shadow) {
-                    ++rec_shadow;
-                    vis *= (1 - density / maj);
-                } else {
-                    ++rec_primary;
-                    if (u_pt[i] < density / maj) {
-                        st = ST_VERTEX;
-                        last_density = density;
-                        t = t_pt[i];
-                        stop = i;
-                    }
-                }
-                if (stop < 0 && seg_steps >= step_cap) {
-                    err |= VPT_DEVERR_STEP_CAP;
-                    end_code = END_STEP_CAP;
-                    st = ST_END_SAMPLE;
-                    t = t_pt[i];
-                    stop = i;
+            ++n_lookups;
+            ++seg_steps;
+            if (shadow) {
+                ++rec_shadow;
+                vis *= (1 - density / maj);
+            } else {
+                ++rec_primary;
+                if (rng.uniform() < density / maj) {
+                    st = ST_VERTEX;
+                    last_density = density;
                 }
             }
-            // Draws of the points after `stop` were never made by the one-step algorithm.
-            if (stop >= 0 && stop < n_pts - 1) rng.state = pcg_skip(rng_round, (stop + 1) * (shadow ? 1 : 2));
+            if (st == ST_STEP && seg_steps >= step_cap) {
+                err |= VPT_DEVERR_STEP_CAP;
+                end_code = END_STEP_CAP;
+                st = ST_END_SAMPLE;
+            }
         }
     }
 
