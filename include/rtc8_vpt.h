@@ -111,6 +111,11 @@ int vpt_set_volume_dense_device(VptContext* ctx, const float* dev_voxels, int32_
 int vpt_generate_fbm_volume(VptContext* ctx, int32_t n, uint32_t seed, int32_t octaves,
                             float lacunarity, float gain, float base_frequency, float threshold,
                             float voxel_size, const float origin[3]);
+/* Union of two such clouds (seeds seed_a and seed_b, each remapped and thresholded on its own):
+ * voxel = max of the two. */
+int vpt_generate_fbm_union(VptContext* ctx, int32_t n, uint32_t seed_a, uint32_t seed_b, int32_t octaves,
+                           float lacunarity, float gain, float base_frequency, float threshold,
+                           float voxel_size, const float origin[3]);
 /* Copies the dense voxel values of the last generated/uploaded volume to the host (n^3 floats);
  * only valid until the next volume call. */
 int vpt_download_volume_dense(VptContext* ctx, float* host_voxels);

@@ -100,6 +100,8 @@ _VPT = {
     "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
     "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "vpt_generate_fbm_union": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float,
+                                         C.c_float, C.c_float, C.c_float, c_float_p]),
     "vpt_nrc_enable": (C.c_int, [C.c_void_p]),
     "vpt_nrc_get_buffers": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_nrc_set_query_density": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -28,6 +28,7 @@ class VolumeSpec:
     base_frequency: float = 4.0  # lattice cells across the grid at the first octave
     threshold: float = 0.0       # > 0: sparse cloud, density = max(0, (r - t) / (1 - t))
     sigma_t_max: float = 20.0    # density coefficient (grid values lie in [0, 1])
+    union_seed: int | None = None  # a second cloud (same parameters, this seed) unioned by max
 
 
 @dataclass(frozen=True)

@@ -239,6 +239,26 @@ int vpt_generate_fbm_volume(VptContext* c, int32_t n, uint32_t seed, int32_t oct
     return build_grid_from_dense(c, c->d_dense, n, n, n, voxel_size, origin);
 }
 
+int vpt_generate_fbm_union(VptContext* c, int32_t n, uint32_t seed_a, uint32_t seed_b, int32_t octaves,
+                           float lacunarity, float gain, float base_frequency, float threshold, float voxel_size,
+                           const float origin[3]) {
+    if (!c || n <= 1 || n > 4096 || octaves <= 0 || octaves > 16 || !(voxel_size > 0) || !origin || threshold < 0 ||
+        threshold >= 1)
+        return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_generate_fbm_union: bad arguments");
+    int64_t total = static_cast<int64_t>(n) * n * n;
+    int rc;
+    if ((rc = dev_alloc(&c->d_dense, total))) return rc;
+    float* second = nullptr;
+    if ((rc = dev_alloc(&second, total))) return rc;
+    vpt::generate_fbm(c->d_dense, n, seed_a, octaves, lacunarity, gain, base_frequency, threshold, c->d_scratch_u32, 0);
+    vpt::generate_fbm(second, n, seed_b, octaves, lacunarity, gain, base_frequency, threshold, c->d_scratch_u32, 0);
+    vpt::max_into(c->d_dense, second, total, 0);
+    cudaError_t e = cudaGetLastError();
+    dev_free(&second);
+    if (e != cudaSuccess) return set_error(VPT_ERR_CUDA, std::string("vpt_generate_fbm_union: ") + cudaGetErrorString(e));
+    return build_grid_from_dense(c, c->d_dense, n, n, n, voxel_size, origin);
+}
+
 int vpt_download_volume_dense(VptContext* c, float* host) {
     if (!c || !host || !c->d_dense) return set_error(VPT_ERR_NOT_READY, "no dense volume resident");
     int64_t total = static_cast<int64_t>(c->nx) * c->ny * c->nz;

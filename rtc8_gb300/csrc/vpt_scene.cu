@@ -101,6 +101,12 @@ __global__ void remap_kernel(float* __restrict__ v, int64_t n, const unsigned in
     }
 }
 
+__global__ void max_into_kernel(float* __restrict__ a, const float* __restrict__ b, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        a[i] = fmaxf(a[i], b[i]);
+}
+
 // ------------------------------------------------------------------------------ sparse grid
 // One CTA per leaf cell: activity (any non-zero voxel), and the cell majorant = max over the
 // cell's voxels with a one-voxel apron below and a two-voxel apron above (the trilinear
@@ -220,6 +226,11 @@ void generate_fbm(float* dense, int n, uint32_t seed, int octaves, float lacunar
     cudaMemcpyAsync(d_minmax, init, sizeof(init), cudaMemcpyHostToDevice, s);
     minmax_kernel<<<blocks, 256, 0, s>>>(dense, total, d_minmax);
     remap_kernel<<<blocks, 256, 0, s>>>(dense, total, d_minmax, threshold);
+}
+
+void max_into(float* a, const float* b, int64_t n, cudaStream_t s) {
+    const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, 152 * 32));
+    max_into_kernel<<<blocks, 256, 0, s>>>(a, b, n);
 }
 
 void leaf_stats(const float* dense, int nx, int ny, int nz, int lx, int ly, int lz, int32_t* active, float* cell_maj,

@@ -9,6 +9,8 @@ namespace vpt {
 
 void generate_fbm(float* dense, int n, uint32_t seed, int octaves, float lacunarity, float gain, float base_frequency,
                   float threshold, unsigned int* d_minmax, cudaStream_t s);
+// a[i] = max(a[i], b[i]) (union of two clouds).
+void max_into(float* a, const float* b, int64_t n, cudaStream_t s);
 void leaf_stats(const float* dense, int nx, int ny, int nz, int lx, int ly, int lz, int32_t* active, float* cell_maj,
                 cudaStream_t s);
 void pack_leaves(const float* dense, int nx, int ny, int nz, int lx, int ly, int lz, const int32_t* table,

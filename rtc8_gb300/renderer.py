@@ -82,6 +82,11 @@ class Renderer:
 
     def generate_fbm_volume(self, spec, voxel_size: float, origin) -> None:
         o = np.ascontiguousarray(origin, dtype=np.float32)
+        if spec.union_seed is not None:
+            check(self.lib.vpt_generate_fbm_union(self.ctx, spec.n, spec.seed, spec.union_seed, spec.octaves,
+                                                  spec.lacunarity, spec.gain, spec.base_frequency, spec.threshold,
+                                                  voxel_size, ptr(o, C.c_float)), "vpt_generate_fbm_union")
+            return
         check(self.lib.vpt_generate_fbm_volume(self.ctx, spec.n, spec.seed, spec.octaves, spec.lacunarity, spec.gain,
                                                spec.base_frequency, spec.threshold, voxel_size, ptr(o, C.c_float)),
               "vpt_generate_fbm_volume")

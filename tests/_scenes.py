@@ -72,4 +72,7 @@ def small_config_mode(size: int = 32, n: int = 32, g: float = 0.8, majorant_mode
 
 def volume_for(cfg: SceneConfig) -> np.ndarray:
     v = cfg.volume
-    return fbm_numpy(v.n, v.seed, v.octaves, v.lacunarity, v.gain, v.base_frequency, v.threshold)
+    a = fbm_numpy(v.n, v.seed, v.octaves, v.lacunarity, v.gain, v.base_frequency, v.threshold)
+    if v.union_seed is None:
+        return a
+    return np.maximum(a, fbm_numpy(v.n, v.union_seed, v.octaves, v.lacunarity, v.gain, v.base_frequency, v.threshold))

@@ -158,6 +158,19 @@ def test_fbm_generator_matches_numpy_restatement(cuda_device):
     r.close()
 
 
+def test_fbm_union_matches_numpy_restatement(cuda_device):
+    spec = VolumeSpec(n=32, seed=9, octaves=5, threshold=0.5, union_seed=11)
+    r = Renderer(4, 4)
+    r.generate_fbm_volume(spec, 1.0 / 32, np.array([-0.5, -0.5, -0.5], np.float32))
+    r._dims = (32, 32, 32)
+    got = r.download_volume()
+    a = fbm_numpy(32, 9, 5, 2.0, 0.5, 4.0, 0.5)
+    b = fbm_numpy(32, 11, 5, 2.0, 0.5, 4.0, 0.5)
+    np.testing.assert_allclose(got, np.maximum(a, b), atol=2e-5)
+    assert (got > a).any() and (got > b).any()
+    r.close()
+
+
 def test_sparse_grid_majorants_match_oracle(cuda_device):
     vox = fbm_numpy(40, 4, 4, 2.0, 0.5, 4.0, 0.5)
     r = Renderer(4, 4)
