@@ -105,14 +105,15 @@ class ClockSampler:
 
 
 def _cfg(name):
-    from rtc8_gb300.configs import C1, C2
-    return {"c1": C1, "c2": C2}[name]
+    from rtc8_gb300.configs import C1, C2, C5
+    return {"c1": C1, "c2": C2, "c5": C5}[name]
 
 
 def _workload_name(cfg):
     v = cfg.volume
     return (f"{cfg.name}: plain volumetric path tracing, {cfg.width}x{cfg.height}, {STEP_SPP} spp per step, "
-            f"fBm {v.n}^3 ({'sparse, threshold ' + str(v.threshold) if v.threshold > 0 else 'dense'}), "
+            f"fBm {v.n}^3{' (two clouds unioned)' if v.union_seed is not None else ''} "
+            f"({'sparse, threshold ' + str(v.threshold) if v.threshold > 0 else 'dense'}), "
             f"sigma_t max {v.sigma_t_max}, albedo {cfg.albedo}, HG g {cfg.phase_param}, <= {cfg.max_bounces} bounces, "
             f"sun {cfg.sun_elevation_deg} deg + {'Hosek-Wilkie sky' if cfg.sky else 'constant env'}")
 
@@ -210,7 +211,7 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")

@@ -94,9 +94,11 @@ C2 = SceneConfig(name="c2_sparse512_1024px", width=1024, height=1024, spp=64,
                  sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=256, rr_start_vertex=9,
                  majorant_cell_log2=5)
 
-# BASELINE configuration 5 (stress): 2048^2, sparse 1024^3, sigma_t max 400, albedo 0.9995, g = 0.9.
+# BASELINE configuration 5 (stress): 2048^2, sparse 1024^3 made of two fBm clouds unioned
+# (threshold 0.78: about 8% of the leaves hold density), sigma_t max 400, albedo 0.9995, g = 0.9,
+# <= 1024 bounces.
 C5 = SceneConfig(name="c5_sparse1024_2048px", width=2048, height=2048, spp=16,
-                 volume=VolumeSpec(n=1024, seed=5, octaves=6, threshold=0.6, sigma_t_max=400.0),
+                 volume=VolumeSpec(n=1024, seed=5, octaves=6, threshold=0.78, sigma_t_max=400.0, union_seed=6),
                  albedo=0.9995, phase_kind=1, phase_param=0.9, sun_elevation_deg=20.0, env_constant=None,
                  sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=1024, rr_start_vertex=9,
                  majorant_cell_log2=6)
