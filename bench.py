@@ -204,6 +204,49 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
     return out
 
 
+def batch_bench(steps: int, warmup: int, spp: int = 4) -> dict:
+    """BASELINE configuration 4: 16 seeded scenes of uneven resolution and grid size, one batch
+    step = `spp` samples per pixel of every scene as one CUDA-graph launch, launch shapes picked by
+    the autotuner; the same step issued launch by launch is timed for comparison."""
+    import torch
+
+    from rtc8_gb300.batch import SceneBatch, make_c4_scenes
+
+    b = SceneBatch(make_c4_scenes(16, 4))
+    tuned = b.autotune(spp=2)
+    b.capture(spp)
+    s = torch.cuda.current_stream()
+
+    def timed(fn, n):
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(n):
+            fn()
+        e.record(s)
+        e.synchronize()
+        return a.elapsed_time(e) / n
+
+    for _ in range(warmup):
+        b.step()
+    graph_ms = timed(b.step, steps)
+    for _ in range(warmup):
+        b.step_uncaptured(spp)
+    plain_ms = timed(lambda: b.step_uncaptured(spp), steps)
+    paths = b.paths_per_step
+    errors = sum(r.device_errors() for r in b.renderers)
+    out = {"metric": "paths/s (16 batched scenes, one CUDA graph per step)", "value": paths / (graph_ms / 1e3),
+           "unit": "paths/s", "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": graph_ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded fBm volumes generated on the device)",
+           "config": {"workload": f"c4: 16 scenes, {spp} spp per scene per step, {paths} paths per step",
+                      "scenes": [{"name": c.name, "g": round(c.phase_param, 3), **{k: v for k, v in t.items()
+                                                                                   if k != "scene"}}
+                                 for c, t in zip(b.configs, tuned)]},
+           "uncaptured_ms_per_step": plain_ms, "device_errors": errors}
+    b.close()
+    return out
+
+
 # ------------------------------------------------------------------------------ main
 def main():
     ap = argparse.ArgumentParser()
@@ -211,7 +254,7 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4", "c5"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
@@ -262,6 +305,10 @@ def main():
     if args.nrc_frames:
         torch.cuda.set_device(local)
         print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup)), flush=True)
+        return
+    if args.config == "c4":
+        torch.cuda.set_device(local)
+        print(json.dumps(batch_bench(args.steps, warmup)), flush=True)
         return
 
     torch.cuda.set_device(local)

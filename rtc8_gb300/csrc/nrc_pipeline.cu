@@ -136,7 +136,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.accum_base = 0;
     tp.stream_mode = stream_mode;
     if (stream_mode == 1) {
-        if ((rc = vpt::upload_sample_jumps(c, c->stream_samples, spp, s))) return rc;
+        if ((rc = vpt::upload_sample_jumps(c, spp, s))) return rc;
         tp.sample_jumps = c->d_jumps;
     }
     tp.park_threshold = c->park_threshold;
@@ -156,7 +156,10 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj), smem);
     vpt::launch_nrc_pass(tp, mode, grid_maj, ctas, threads, smem, s);
     NRCP_CUDA(cudaGetLastError());
-    if (stream_mode == 1) c->stream_samples += spp;
+    if (stream_mode == 1) {
+        vpt::launch_frame_update(c->d_frame, spp, false, 0, s);
+        c->stream_samples += spp;
+    }
     return VPT_OK;
 }
 
@@ -293,6 +296,7 @@ int vpt_accumulate_inferred(VptContext* c, void* stream, uint32_t accum_frames) 
                         static_cast<cudaStream_t>(stream));
     NRCP_CUDA(cudaGetLastError());
     c->accum_samples = accum_frames + 1;
+    vpt::launch_frame_update(c->d_frame, 0, true, accum_frames + 1, static_cast<cudaStream_t>(stream));
     return VPT_OK;
 }
 
@@ -314,6 +318,7 @@ int vpt_accumulate_inferred_batch(VptContext* c, void* stream, uint32_t accum_fr
                         static_cast<cudaStream_t>(stream));
     NRCP_CUDA(cudaGetLastError());
     c->accum_samples = accum_frames + spp;
+    vpt::launch_frame_update(c->d_frame, 0, true, accum_frames + spp, static_cast<cudaStream_t>(stream));
     return VPT_OK;
 }
 

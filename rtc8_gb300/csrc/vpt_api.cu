@@ -71,7 +71,7 @@ int vpt_create(int32_t w, int32_t h, VptContext** out) {
     int rc;
     if ((rc = dev_alloc(&c->d_rng, npix)) || (rc = dev_alloc(&c->d_sum, 3 * npix)) ||
         (rc = dev_alloc(&c->d_mean, 3 * npix)) || (rc = dev_alloc(&c->d_work, 4)) ||
-        (rc = dev_alloc(&c->d_counters, 8)) || (rc = dev_alloc(&c->d_err, 1)) || (rc = dev_alloc(&c->d_scratch_u32, 4)) ||
+        (rc = dev_alloc(&c->d_counters, 8)) || (rc = dev_alloc(&c->d_frame, 2)) || (rc = dev_alloc(&c->d_err, 1)) || (rc = dev_alloc(&c->d_scratch_u32, 4)) ||
         (rc = dev_alloc(&c->d_integral, 1))) {
         vpt_destroy(c);
         return rc;
@@ -79,6 +79,7 @@ int vpt_create(int32_t w, int32_t h, VptContext** out) {
     VPT_CUDA(cudaMemset(c->d_sum, 0, 3 * npix * sizeof(double)));
     VPT_CUDA(cudaMemset(c->d_mean, 0, 3 * npix * sizeof(float)));
     VPT_CUDA(cudaMemset(c->d_counters, 0, 8 * sizeof(unsigned long long)));
+    VPT_CUDA(cudaMemset(c->d_frame, 0, 2 * sizeof(uint32_t)));
     VPT_CUDA(cudaMemset(c->d_err, 0, sizeof(unsigned int)));
     // A constant 1x1 environment so that a context is always renderable.
     float one[3] = {1.0f, 1.0f, 1.0f};
@@ -102,6 +103,7 @@ int vpt_destroy(VptContext* c) {
     dev_free(&c->d_mean);
     dev_free(&c->d_work);
     dev_free(&c->d_counters);
+    dev_free(&c->d_frame);
     dev_free(&c->d_err);
     dev_free(&c->d_scratch_u32);
     dev_free(&c->d_integral);
@@ -125,6 +127,7 @@ int vpt_seed_rng(VptContext* c, uint64_t seed) {
     for (int64_t i = 0; i < npix; ++i) states[i] = gen();
     VPT_CUDA(cudaMemcpy(c->d_rng, states.data(), npix * sizeof(uint64_t), cudaMemcpyHostToDevice));
     c->stream_samples = 0;
+    VPT_CUDA(cudaMemset(c->d_frame, 0, sizeof(uint32_t)));
     if (int rc = vpt::nrc_reseed_train_rng(c)) return rc;
     return vpt_reset_accumulation(c);
 }
@@ -150,6 +153,7 @@ int vpt_reset_accumulation(VptContext* c) {
     VPT_CUDA(cudaMemset(c->d_sum, 0, 3 * npix * sizeof(double)));
     VPT_CUDA(cudaMemset(c->d_mean, 0, 3 * npix * sizeof(float)));
     c->accum_samples = 0;
+    VPT_CUDA(cudaMemset(c->d_frame + 1, 0, sizeof(uint32_t)));
     return VPT_OK;
 }
 
@@ -420,7 +424,7 @@ void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus) {
 
 // Jump table of a sample-parallel launch: entry i advances a pixel's seed state to the start
 // of sample (first + i), i.e. by (first + i) * 2^40 draws.
-int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaStream_t s) {
+int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s) {
     if (count > (1u << 20)) return set_error(VPT_ERR_INVALID_ARGUMENT, "at most 2^20 samples per pixel and launch");
     if (c->jump_capacity < count) {
         int rc = dev_alloc(&c->d_jumps, count);
@@ -429,7 +433,7 @@ int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaS
     }
     // Computed on the device, ordered on the launch's stream: no host copy (a copy from pageable
     // memory can block the host until the stream reaches it).
-    launch_sample_jump_table(c->d_jumps, first, count, s);
+    launch_sample_jump_table_dev(c->d_jumps, c->d_frame, count, s);
     VPT_CUDA(cudaGetLastError());
     return VPT_OK;
 }
@@ -548,7 +552,7 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     if (npix * spp >= (1ull << 31)) return set_error(VPT_ERR_INVALID_ARGUMENT, "too many samples in one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (tp.stream_mode == 1) {
-        int rc2 = vpt::upload_sample_jumps(c, c->stream_samples, spp, s);
+        int rc2 = vpt::upload_sample_jumps(c, spp, s);
         if (rc2) return rc2;
         tp.sample_jumps = c->d_jumps;
     }
@@ -562,10 +566,11 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     }
     int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr), smem);
     vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
+    if (tp.stream_mode == 1)
+        vpt::launch_finalize_mean_dev(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->d_frame, spp, s);
+    vpt::launch_frame_update(c->d_frame, spp, false, spp, s);
     c->accum_samples += spp;
     c->stream_samples += spp;
-    if (tp.stream_mode == 1)
-        vpt::launch_finalize_mean(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->accum_samples, s);
     VPT_CUDA(cudaGetLastError());
     return VPT_OK;
 }
@@ -582,7 +587,11 @@ int vpt_download_sum(VptContext* c, double* host, uint32_t* n) {
     int64_t npix = static_cast<int64_t>(c->width) * c->height;
     VPT_CUDA(cudaDeviceSynchronize());
     VPT_CUDA(cudaMemcpy(host, c->d_sum, 3 * npix * sizeof(double), cudaMemcpyDeviceToHost));
-    if (n) *n = c->accum_samples;
+    if (n) {
+        uint32_t frame[2];
+        VPT_CUDA(cudaMemcpy(frame, c->d_frame, sizeof(frame), cudaMemcpyDeviceToHost));
+        *n = frame[1];  // advanced on the device, also by replays of captured launches
+    }
     return VPT_OK;
 }
 

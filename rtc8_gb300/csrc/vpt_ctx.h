@@ -24,6 +24,7 @@ struct VptContextImpl {
     float* d_mean = nullptr;
     uint32_t accum_samples = 0;
     uint32_t stream_samples = 0;   // samples ever traced since seeding (sample-parallel streams)
+    uint32_t* d_frame = nullptr;   // device copy of {stream_samples, accum_samples} (authoritative)
     ulonglong2* d_jumps = nullptr; // per-launch PCG jump table of the sample-parallel streams
     uint32_t jump_capacity = 0;
 
@@ -75,8 +76,9 @@ int persistent_grid(VptContextImpl* c, int threads, const void* kernel, size_t s
 void lcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus);
 // Training-pass RNG states derived from the context's per-pixel states (no-op without cache buffers).
 int nrc_reseed_train_rng(VptContextImpl* c);
-// Jump table (A, C) of sample-parallel streams first .. first + count - 1, enqueued on `s`.
-int upload_sample_jumps(VptContextImpl* c, uint32_t first, uint32_t count, cudaStream_t s);
+// Jump table (A, C) of the next `count` sample-parallel streams (first = the device frame
+// counter), enqueued on `s`; the caller advances the counter after its launch.
+int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);

@@ -828,7 +828,51 @@ __global__ void sample_jump_table_kernel(ulonglong2* out, uint32_t first, uint32
     out[i] = make_ulonglong2(acc_mult, acc_plus);
 }
 
+// As sample_jump_table_kernel, with the first sample index read from the context's device
+// frame counters (so that a launch captured in a CUDA graph continues the streams on replay).
+__global__ void sample_jump_table_dev_kernel(ulonglong2* out, const uint32_t* __restrict__ frame, uint32_t count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint64_t delta = static_cast<uint64_t>(frame[0] + i) << kSampleStreamShift;
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1ULL, acc_mult = 1ULL, acc_plus = 0ULL;
+    while (delta > 0) {
+        if (delta & 1ULL) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ULL) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    out[i] = make_ulonglong2(acc_mult, acc_plus);
+}
+
+// mean = sum / (accumulated samples + spp), the count read from the device frame counters.
+__global__ void finalize_mean_dev_kernel(const double* __restrict__ sum, float* __restrict__ mean, uint32_t n,
+                                         const uint32_t* __restrict__ frame, uint32_t spp) {
+    const double inv = 1.0 / (static_cast<double>(frame[1]) + spp);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mean[i] = static_cast<float>(sum[i] * inv);
+}
+
+// frame[0] += add_stream; frame[1] = set ? value : frame[1] + value.
+__global__ void frame_update_kernel(uint32_t* frame, uint32_t add_stream, int set_accum, uint32_t value) {
+    frame[0] += add_stream;
+    frame[1] = set_accum ? value : frame[1] + value;
+}
+
 }  // namespace
+
+void launch_sample_jump_table_dev(ulonglong2* out, const uint32_t* frame, uint32_t count, cudaStream_t s) {
+    sample_jump_table_dev_kernel<<<(count + 127) / 128, 128, 0, s>>>(out, frame, count);
+}
+void launch_finalize_mean_dev(const double* sum, float* mean, uint32_t n_values, const uint32_t* frame, uint32_t spp,
+                              cudaStream_t s) {
+    finalize_mean_dev_kernel<<<(n_values + 255) / 256, 256, 0, s>>>(sum, mean, n_values, frame, spp);
+}
+void launch_frame_update(uint32_t* frame, uint32_t add_stream, bool set_accum, uint32_t value, cudaStream_t s) {
+    frame_update_kernel<<<1, 1, 0, s>>>(frame, add_stream, set_accum ? 1 : 0, value);
+}
 
 void launch_sample_jump_table(ulonglong2* out, uint32_t first, uint32_t count, cudaStream_t s) {
     sample_jump_table_kernel<<<(count + 127) / 128, 128, 0, s>>>(out, first, count);

@@ -74,6 +74,13 @@ const void* nrc_kernel_ptr(int mode, bool grid_majorant);
 // Jump table of sample-parallel streams first .. first + count - 1, computed on the device.
 void launch_sample_jump_table(ulonglong2* out, uint32_t first, uint32_t count, cudaStream_t s);
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
+// Device frame counters of a context: [0] sample-parallel streams used since seeding, [1] samples
+// in the accumulation. The launches of the plain and render paths read and advance them on the
+// device, so a sequence of launches captured once in a CUDA graph renders new samples on replay.
+void launch_sample_jump_table_dev(ulonglong2* out, const uint32_t* frame, uint32_t count, cudaStream_t s);
+void launch_finalize_mean_dev(const double* sum, float* mean, uint32_t n_values, const uint32_t* frame, uint32_t spp,
+                              cudaStream_t s);
+void launch_frame_update(uint32_t* frame, uint32_t add_stream, bool set_accum, uint32_t value, cudaStream_t s);
 void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int mx, int my, int mz, int factor,
                     cudaStream_t s);
 
