@@ -272,7 +272,12 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    cfg = _cfg(args.config)
+    if args.config == "c4" and args.impl == "ours":
+        if rank == 0:
+            torch.cuda.set_device(local)
+            print(json.dumps(batch_bench(args.steps, warmup)), flush=True)
+        return
+    cfg = _cfg(args.config if args.config != "c4" else "c1")
     if args.image:
         cfg = cfg.replace(width=args.image, height=args.image)
     workload = _workload_name(cfg)
@@ -305,10 +310,6 @@ def main():
     if args.nrc_frames:
         torch.cuda.set_device(local)
         print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup)), flush=True)
-        return
-    if args.config == "c4":
-        torch.cuda.set_device(local)
-        print(json.dumps(batch_bench(args.steps, warmup)), flush=True)
         return
 
     torch.cuda.set_device(local)
