@@ -169,8 +169,9 @@ def scene_host_inputs(cfg):
 
 
 def nrc_frame_loop(frames: int, warmup: int) -> dict:
-    """The radiance-cache frame loop (1 training iteration + 8 spp per frame, settings of the
-    equal-error comparison) on the 256x256 dense 64^3 scene; returns the mean frame time."""
+    """The radiance-cache frame loop (1 training iteration + spp_per_frame samples per frame, the
+    settings of the equal-error comparison) on the 256x256 dense 64^3 scene; returns the mean
+    frame time."""
     import torch
 
     from rtc8_gb300 import convergence, nrc
@@ -181,7 +182,7 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
     r = Renderer(C1.width, C1.height)
     setup_scene(r, C1)
     r.nrc_set_query_density(True)
-    r.nrc_set_termination_factor(st["termination"])
+    r.nrc_set_termination_factor(st["termination"], st.get("train_termination", 0.0))
     net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
     net.ema_decay, net.learning_rate = st["ema_decay"], st["learning_rate"]
     cache = nrc.NeuralRadianceCache()
