@@ -69,18 +69,19 @@ def plain_curve(cfg: SceneConfig, ref: np.ndarray, target: float, chunk_spp: int
     s = torch.cuda.Stream()
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg)
-    curve, t, spp, reached = [], 0.0, 0, None
+    curve, t, spp, reached, img = [], 0.0, 0, None, None
     wall0 = time.perf_counter()
     while spp < max_spp and time.perf_counter() - wall0 < time_budget:
         t += _timed(s, lambda: r.launch_plain(chunk_spp, s.cuda_stream))
         spp += chunk_spp
-        e = rel_mse(r.image(), ref)
+        img = r.image()
+        e = rel_mse(img, ref)
         curve.append((spp, t, e))
         if e <= target and reached is None:
             reached = {"spp": spp, "seconds": t}
             break
     r.close()
-    return {"curve": curve, "reached": reached}
+    return {"curve": curve, "reached": reached, "image": img}
 
 
 def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None, spp_per_frame: int = 8,
@@ -102,7 +103,7 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
     r.nrc_set_termination_factor(termination, train_termination)
     cache = nrc.NeuralRadianceCache()
     cache.initialize(config=net_config or nrc.default_config(nrc.NRC_ENCODING_VOLUME))
-    curve, t, frames, reached = [], 0.0, 0, None
+    curve, t, frames, reached, img = [], 0.0, 0, None, None
     t += _timed(s, lambda: r.nrc_frame(cache, 8, spp_per_frame, True, s.cuda_stream))
     for _ in range(warmup_frames):
         t += _timed(s, lambda: r.nrc_frame(cache, 1, spp_per_frame, False, s.cuda_stream))
@@ -116,7 +117,8 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
                 r.nrc_frame(cache, 1, spp_per_frame, False, s.cuda_stream)
         t += _timed(s, run)
         frames += eval_every
-        e = rel_mse(r.image(), ref)
+        img = r.image()
+        e = rel_mse(img, ref)
         curve.append((frames * spp_per_frame, t, e))
         if e <= target and reached is None:
             reached = {"frames": frames, "spp": frames * spp_per_frame, "seconds": t}
@@ -125,7 +127,7 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
     best = min(c[2] for c in curve) if curve else math.inf
     r.close()
     cache.finalize()
-    return {"curve": curve, "reached": reached, "best_rel_mse": best, "device_errors": errors}
+    return {"curve": curve, "reached": reached, "best_rel_mse": best, "device_errors": errors, "image": img}
 
 
 # Radiance-cache settings of the equal-error comparison, from a sweep on the 64^3 cloud: the
@@ -155,6 +157,10 @@ def compare(cfg: SceneConfig, target: float = 1e-3, oracle_spp: int = 16384, tim
            "plain": {"reached": plain["reached"], "last": plain["curve"][-1] if plain["curve"] else None},
            "nrc": {"reached": cache["reached"], "last": cache["curve"][-1] if cache["curve"] else None,
                    "best_rel_mse": cache["best_rel_mse"], "device_errors": cache["device_errors"]}}
+    # MLP error: relMSE of the radiance-cache estimate against the plain estimate, both at the
+    # point where they stopped.
+    if cache["image"] is not None and plain["image"] is not None:
+        out["nrc"]["mlp_error_vs_plain"] = rel_mse(cache["image"], plain["image"])
     if plain["reached"] and cache["reached"]:
         out["speedup"] = plain["reached"]["seconds"] / cache["reached"]["seconds"]
     else:
