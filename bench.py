@@ -6,7 +6,11 @@ bounces, sun at 20 degrees + Hosek-Wilkie sky). Metric: paths/s = pixels * spp /
 The line also carries `nrc_vs_plain`: GPU time for the radiance-cache renderer and for the plain
 tracer to reach relMSE 1e-3 against a 16384-spp FP64 image on the 256x256 dense 64^3 scene.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2|c1]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2|c1|c4|c5]
+                  [--no-nrc] [--no-cpu-baseline] [--nrc-frames N]
+
+`--config c4` times the 16-scene batch (one CUDA graph per step), `--config c5` the 2048^2 /
+1024^3 stress scene; `--nrc-frames N` runs only the radiance-cache frame loop (profiling).
 
 `--impl reference` times the reference's per-path CPU algorithm on the host cores. The reference's
 own implementation (OptiX raygen + tiny-cuda-nn) cannot be built on this platform, so the arm runs
@@ -120,34 +124,36 @@ def _workload_name(cfg):
 
 # ------------------------------------------------------------------------------ CPU legs
 def cpu_sample(cfg, vox: np.ndarray, env_rgb: np.ndarray | None, target_seconds: float = 12.0, threads: int = 0):
-    """Times the oracle (all host threads) on a bounded sample of the workload: whole image rows
-    spread over the frame, 1 sample per pixel, sized to about `target_seconds`."""
+    """Times the oracle (all host threads) on a bounded sample of the workload: bands of image rows
+    spread over the frame, one sample per pixel per pass, passes repeated (sample 0, 1, ...) until
+    about `target_seconds` of CPU work."""
     from oracle import orc
 
     threads = threads or (os.cpu_count() or 1)
     sc = orc.scene_from_config(cfg, vox, env_rgb)
     rng = orc.seed_states(cfg.width, cfg.height, cfg.rng_seed)
-    # Bands of `threads` rows (one row per OpenMP thread) at positions spread over the frame
-    # in bit-reversed order, until the time budget is spent.
+    # Bands of `threads` rows (one row per OpenMP thread) in bit-reversed order over the frame.
     band = threads
     nbands = max(1, cfg.height // band)
     bits = max(1, (nbands - 1).bit_length())
     order = sorted(range(nbands), key=lambda b: int(format(b, f"0{bits}b")[::-1], 2))
-    rows = 0
+    paths = 0
     elapsed = 0.0
-    for b in order:
-        if elapsed >= target_seconds:
-            break
-        y0 = b * band
-        y1 = min(cfg.height, y0 + band)
-        t0 = time.perf_counter()
-        orc.render_plain(sc, rng, 1, rows=(y0, y1), threads=threads)
-        elapsed += time.perf_counter() - t0
-        rows += y1 - y0
-    paths = rows * cfg.width
+    passes = 0
+    while elapsed < target_seconds:
+        for b in order:
+            if elapsed >= target_seconds:
+                break
+            y0 = b * band
+            y1 = min(cfg.height, y0 + band)
+            t0 = time.perf_counter()
+            orc.render_plain(sc, rng, 1, accum_base=passes, rows=(y0, y1), threads=threads)
+            elapsed += time.perf_counter() - t0
+            paths += (y1 - y0) * cfg.width
+        passes += 1
     return {"value": paths / elapsed, "unit": "paths/s", "cores": threads, "kind": "port",
-            "sample": f"{rows} rows x {cfg.width} px x 1 spp of {cfg.name} ({paths} paths, {elapsed:.1f} s), "
-                      f"oracle restatement with OpenMP, rows in bands spread over the frame"}
+            "sample": f"{paths} paths of {cfg.name} ({passes} pass(es) of 1 spp over row bands spread over the "
+                      f"frame, {elapsed:.1f} s), oracle restatement with OpenMP"}
 
 
 def scene_host_inputs(cfg):
