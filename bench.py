@@ -174,6 +174,53 @@ def scene_host_inputs(cfg):
     return vox, env
 
 
+def mlp_bench(steps: int, warmup: int) -> dict:
+    """The cache's MLP kernels alone at the sizes of a radiance-cache frame of the equal-error
+    comparison: inference over 2^21 queries (256^2 pixels x 32 samples) and training steps of 16384
+    records, volume encoding, 5 hidden layers of 64. FLOPs are those of the padded network
+    (144x64 + 4x64x64 + 64x16 multiply-adds per record forward, 3x that per training record)."""
+    import torch
+
+    from rtc8_gb300 import nrc
+
+    cfg = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    n_inf, n_tr = 1 << 21, 16384
+    q = torch.rand((n_inf, 14), device="cuda", generator=gen)
+    q[:, 3:7] *= 3.0
+    out = torch.empty((n_inf, 3), device="cuda")
+    tgt = torch.rand((n_tr, 3), device="cuda", generator=gen)
+    s = torch.cuda.current_stream()
+
+    def timed(fn, n):
+        for _ in range(warmup):
+            fn()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(n):
+            fn()
+        e.record(s)
+        e.synchronize()
+        return a.elapsed_time(e) / n / 1e3
+
+    flop_fwd = 2 * (144 * 64 + 4 * 64 * 64 + 64 * 16)
+    t_inf = timed(lambda: cache.infer(s.cuda_stream, q, n_inf, out), max(steps, 10))
+    t_tr = timed(lambda: cache.train(s.cuda_stream, q, tgt, n_tr), max(steps, 10))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    inf_tf = n_inf * flop_fwd / t_inf / 1e12
+    tr_tf = n_tr * 3 * flop_fwd / t_tr / 1e12
+    errors = cache.device_errors()
+    cache.finalize()
+    return {"metric": "MLP TFLOP/s (padded FP16 network, FP32 accumulation)", "infer_ms": t_inf * 1e3,
+            "infer_tflops": inf_tf, "infer_frac_of_peak": inf_tf / peak, "train_step_ms": t_tr * 1e3,
+            "train_tflops": tr_tf, "train_frac_of_peak": tr_tf / peak,
+            "peak_tflops": peak, "peak_source": "measured bf16_tflops (dense FP16 has the same rate)",
+            "infer_records": n_inf, "train_records": n_tr, "device_errors": errors}
+
+
 def nrc_frame_loop(frames: int, warmup: int) -> dict:
     """The radiance-cache frame loop (1 training iteration + spp_per_frame samples per frame, the
     settings of the equal-error comparison) on the 256x256 dense 64^3 scene; returns the mean
@@ -266,6 +313,8 @@ def main():
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
     ap.add_argument("--no-nrc", action="store_true", help="skip the NRC-vs-plain equal-error comparison")
+    ap.add_argument("--mlp", action="store_true",
+                    help="profiling run: only the cache's MLP kernels (inference and training steps)")
     ap.add_argument("--nrc-frames", type=int, default=0,
                     help="profiling run: only the radiance-cache frame loop on the 256x256 scene, N timed frames")
     args = ap.parse_args()
@@ -314,6 +363,10 @@ def main():
 
     from rtc8_gb300.renderer import Renderer, setup_scene
 
+    if args.mlp:
+        torch.cuda.set_device(local)
+        print(json.dumps(mlp_bench(args.steps, warmup)), flush=True)
+        return
     if args.nrc_frames:
         torch.cuda.set_device(local)
         print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup)), flush=True)

@@ -118,36 +118,70 @@ __device__ __forceinline__ float reference_feature(int i, const float* q) {
     return 0.0f;
 }
 
+// Eight consecutive one-blob bins b0 .. b0 + 7 of x (already scaled by the bin count):
+// g_b = exp(-z_b^2 / 2), z_b = x - (b + 0.5). From the exact value at bin b0 + 4, the neighbours
+// follow by the ratios g_{b+1} / g_b = exp(z_b - 1/2) and g_{b-1} / g_b = exp(-z_b - 1/2), each
+// ratio shrinking by e^-1 per step: three special-function evaluations for eight bins instead of
+// eight (the relative error of the products stays near 1e-6, far below the FP16 rounding).
+// For |z| up to the bin count no intermediate overflows; where the centre value underflows to 0
+// every bin of the group is below e^-40 and encodes as 0 in FP16.
+__device__ __forceinline__ void one_blob8(float x, int b0, float (&v)[8]) {
+    constexpr float kInvE = 0.36787944117144233f;
+    const float z = x - (static_cast<float>(b0 + 4) + 0.5f);
+    const float g = __expf(-0.5f * z * z);
+    float up = __expf(z - 0.5f);   // g_{c+1} / g_c
+    float dn = __expf(-z - 0.5f);  // g_{c-1} / g_c
+    v[4] = g;
+    float gu = g, gd = g;
+#pragma unroll
+    for (int j = 1; j <= 3; ++j) {
+        gu *= up;
+        up *= kInvE;
+        v[4 + j] = gu;
+        gd *= dn;
+        dn *= kInvE;
+        v[4 - j] = gd;
+    }
+    gd *= dn;
+    v[0] = gd;
+}
+
 // NRC_ENCODING_VOLUME (144 features): sin and cos of pi 2^f x for the 3 position coordinates
 // (features 2(12a + f) and 2(12a + f) + 1), OneBlob(32) on vOut theta / pi and phi / 2 pi
 // (feature 72 + 32a + b), the local density (roughness slot) and the albedo (diffuse.r), 6 zeros.
 __device__ __forceinline__ void encode_row_volume(const float* q, uint8_t* tile, int r) {
     constexpr int K = 144;
+    // Chunk k holds frequencies f0 .. f0 + 3 (f0 = 4 (k % 3)) of coordinate k / 3.
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
+        // sin / cos(pi v) with v = x 2^f0 exact: v = m + r (m integer, r in [0, 1)), so
+        // sin(pi v) = (-1)^m sin(pi r) and likewise cos; the hardware approximation on [0, pi)
+        // is accurate to ~4e-7. The next three frequencies follow by angle doubling,
+        // sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a), which at most
+        // multiplies that error by 8 (~3e-6, far below the FP16 rounding of the features).
+        const float x = q[k / 3] * static_cast<float>(1 << (4 * (k % 3)));
+        const float m = floorf(x);
+        float sn, cs;
+        __sincosf(kPiF * (x - m), &sn, &cs);
+        const float sign = (static_cast<int>(m) & 1) ? -1.0f : 1.0f;
+        sn *= sign;
+        cs *= sign;
         float v[8];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int p = 4 * k + i;  // = 12a + f
-            // sin / cos(pi v) with v = x 2^f exact: v = m + r (m integer, r in [0, 1)), so
-            // sin(pi v) = (-1)^m sin(pi r) and likewise cos; the hardware approximation on
-            // [0, pi) is accurate to ~4e-7, far below the FP16 rounding of the features.
-            const float x = q[p / 12] * static_cast<float>(1 << (p % 12));
-            const float m = floorf(x);
-            float sn, cs;
-            __sincosf(kPiF * (x - m), &sn, &cs);
-            const float sign = (static_cast<int>(m) & 1) ? -1.0f : 1.0f;
-            v[2 * i] = sign * sn;
-            v[2 * i + 1] = sign * cs;
+            v[2 * i] = sn;
+            v[2 * i + 1] = cs;
+            const float s2 = 2.0f * sn * cs;
+            cs = (cs - sn) * (cs + sn);
+            sn = s2;
         }
         store8(tile, r, k, K, v);
     }
-    const float theta = q[5] * (1.0f / 3.14159265f), phi = q[6] * (1.0f / 6.28318531f);
+    const float theta = q[5] * (32.0f / 3.14159265f), phi = q[6] * (32.0f / 6.28318531f);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         float v[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = one_blob(k < 4 ? theta : phi, 8 * (k % 4) + i, 32);
+        one_blob8(k < 4 ? theta : phi, 8 * (k % 4), v);
         store8(tile, r, 9 + k, K, v);
     }
     const float last[8] = {q[7], q[8], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -204,6 +238,18 @@ __device__ __forceinline__ void store_row16(uint8_t* tile, int r, int c0, int K,
         w.y = pack_half2(v[8 * h + 2], v[8 * h + 3]);
         w.z = pack_half2(v[8 * h + 4], v[8 * h + 5]);
         w.w = pack_half2(v[8 * h + 6], v[8 * h + 7]);
+        *reinterpret_cast<uint4*>(tile + cm_offset(r, c0 + 8 * h, K)) = w;
+    }
+}
+// As store_row16 with ReLU fused into the FP16 conversion.
+__device__ __forceinline__ void store_row16_relu(uint8_t* tile, int r, int c0, int K, const float (&v)[16]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        uint4 w;
+        w.x = pack_half2_relu(v[8 * h + 0], v[8 * h + 1]);
+        w.y = pack_half2_relu(v[8 * h + 2], v[8 * h + 3]);
+        w.z = pack_half2_relu(v[8 * h + 4], v[8 * h + 5]);
+        w.w = pack_half2_relu(v[8 * h + 6], v[8 * h + 7]);
         *reinterpret_cast<uint4*>(tile + cm_offset(r, c0 + 8 * h, K)) = w;
     }
 }
@@ -292,13 +338,8 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
                     tmem_ld16(tmem + lane_base + c * 32, v0);
                     tmem_ld16(tmem + lane_base + c * 32 + 16, v1);
                     tmem_wait_ld();
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        v0[i] = fmaxf(v0[i], 0.0f);
-                        v1[i] = fmaxf(v1[i], 0.0f);
-                    }
-                    store_row16(s_t, gt, c * 32, kWidth, v0);
-                    store_row16(s_t, gt, c * 32 + 16, kWidth, v1);
+                    store_row16_relu(s_t, gt, c * 32, kWidth, v0);
+                    store_row16_relu(s_t, gt, c * 32 + 16, kWidth, v1);
                 }
                 tc_fence_before();
                 fence_async_smem();
@@ -385,9 +426,7 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, co
                 float v[16];
                 tmem_ld16(tmem + lane_base + c * 16, v);
                 tmem_wait_ld();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
-                store_row16(act(j + 1), tid, c * 16, kWidth, v);
+                store_row16_relu(act(j + 1), tid, c * 16, kWidth, v);
             }
         } else {
             // output, loss and its gradient (rows beyond n contribute nothing)

@@ -135,5 +135,11 @@ __device__ __forceinline__ uint32_t pack_half2(float a, float b) {
     __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
+// max(a, 0) and max(b, 0) rounded to FP16 (a in the low half) in one conversion instruction.
+__device__ __forceinline__ uint32_t pack_half2_relu(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
 
 }  // namespace nrc
