@@ -314,11 +314,13 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     uint32_t phase = 0;
     bool ok = true;
+    float q[14];
+    load_query(in, (blockIdx.x * G + g) * kTile + gt, n, q);
     for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += gridDim.x * G) {
         const uint32_t row = tile * kTile + gt;
-        float q[14];
-        load_query(in, row, n, q);
         encode_row(ly.enc, q, s_t, gt, IN);
+        // The next tile's queries load while this tile runs through the layers.
+        load_query(in, (tile + gridDim.x * G) * kTile + gt, n, q);
         fence_async_smem();
         named_sync(bar_id, kTile);
         for (int j = 0; j < ly.L && ok; ++j) {
