@@ -126,6 +126,59 @@ int vpt_get_volume_info(VptContext* ctx, int64_t* active_leaves, int64_t* total_
  * apron on every side) as a host copy of cx*cy*cz floats. */
 int vpt_download_cell_majorants(VptContext* ctx, float* host_cells);
 
+/* ---- NanoVDB grids ------------------------------------------------------------------- */
+/* Description of one NanoVDB grid (format version 32.x). Filled from a file's metadata record
+ * by vpt_nvdb_file_info (io::GridMetaData, ext/nanovdb/nanovdb/util/IO.h:144-158) or from an
+ * in-memory grid by vpt_nanovdb_grid_info (GridData / TreeData / RootData, NanoVDB.h:2185-2205,
+ * 2501-2507, 2687-2725); fields a source does not hold stay zero. */
+typedef struct VptNanoVdbInfo {
+    char name[256];
+    uint32_t grid_type;           /* NanoVDB GridType; 1 = float, the only type a volume accepts */
+    uint32_t grid_class;          /* 1 = level set, 2 = fog volume, ... */
+    uint64_t grid_bytes;          /* bytes of the in-memory grid */
+    uint64_t file_bytes;          /* bytes of the payload in the file (compressed size) */
+    uint64_t active_voxels;
+    int32_t index_min[3], index_max[3];  /* inclusive index box of the active values */
+    double world_min[3], world_max[3];   /* world box: the clip box of the volume */
+    double voxel_size[3];
+    float map_mat_f[9], map_inv_mat_f[9], map_vec_f[3];  /* index-to-world map, float copy */
+    double map_mat_d[9], map_vec_d[3];                    /* index-to-world map, double copy */
+    float background;
+    uint32_t node_count[3];       /* leaf, lower and upper internal nodes */
+    uint32_t tile_count[3];       /* active tiles of those levels */
+    /* file only */
+    uint32_t codec;               /* 0 = none, 1 = ZIP, 2 = BLOSC */
+    uint32_t grid_count;          /* grids in the file */
+    uint64_t payload_offset;      /* absolute byte offset of the grid's payload */
+    /* in-memory only: the leaf cells a volume built from this grid holds */
+    int32_t extent_min[3], extent_max[3];  /* leaf-aligned index box [min, max) */
+    int64_t flat_leaves;
+} VptNanoVdbInfo;
+
+/* Metadata of grid number `grid_index` (counted over all segments) of an .nvdb file. Host only. */
+int vpt_nvdb_file_info(const char* path, uint64_t grid_index, VptNanoVdbInfo* info);
+/* Metadata of a NanoVDB grid held in host memory (the buffer of a nanovdb::GridHandle). Host only. */
+int vpt_nanovdb_grid_info(const void* grid, uint64_t bytes, VptNanoVdbInfo* info);
+/* The leaves a volume built from this float grid holds, decoded on the host: every leaf of the
+ * tree inside the extent, then one constant 8^3 leaf per cell of each non-zero tile, then (for
+ * a non-zero background) one leaf per cell no root entry covers. leaf_origins gets 3 index
+ * coordinates per leaf, leaf_values 512 values per leaf (order x<<6 | y<<3 | z). With both
+ * pointers NULL only *count is set; otherwise capacity must be >= the count. Host only. */
+int vpt_nanovdb_decode_leaves(const void* grid, uint64_t bytes, int64_t capacity, int32_t* leaf_origins,
+                              float* leaf_values, int64_t* count);
+/* Density volume from a NanoVDB float grid in host memory: replaces Scene::allocateVolumeGrid
+ * (renderer/renderer_scene.cpp:491-537). The clip box is the grid's world box converted to
+ * float (:517-519); the global majorant is the maximum over index coordinates [min, max) of
+ * the index box (:498-509); lookups follow the grid's map (uniform scale + translation only;
+ * other maps are rejected). The tree is flattened into the tracer's 8^3 leaves over the
+ * leaf-aligned extent [index_min - 2, index_max + 2]. */
+int vpt_set_volume_nanovdb(VptContext* ctx, const void* grid, uint64_t bytes);
+/* The same from grid number `grid_index` of an uncompressed .nvdb file: replaces
+ * nanovdb::io::readGrid (ext/nanovdb/nanovdb/util/IO.h:576-606) as called at
+ * renderer/renderer_scene.cpp:2468. A ZIP or BLOSC grid is refused with an error naming the
+ * codec: inflate its payload on the host and call vpt_set_volume_nanovdb. */
+int vpt_set_volume_nvdb_file(VptContext* ctx, const char* path, uint64_t grid_index);
+
 /* Image-based environment from an RGB float image (row-major, rows = polar angle from +y).
  * Builds the hierarchical importance map on the device (compute_light_probs.cu:161-211). */
 int vpt_set_environment_rgb(VptContext* ctx, const float* host_rgb, int32_t width, int32_t height);

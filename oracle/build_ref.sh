@@ -23,6 +23,10 @@ gcc -O2 -std=gnu99 -I "$REF/ext/hosek_wilkie_2013" "$HERE/ref_hosek_dump.c" "$OU
 # NanoVDB 32.3 grid builder, first-order sampler and ray clip.
 g++ -O2 -std=c++17 -w -I "$REF/ext/nanovdb" "$HERE/ref_kat_nanovdb.cpp" -o "$OUT/ref_kat_nanovdb" -lpthread
 
+# NanoVDB 32.3 file writer/reader fixtures (io::writeGrid(s), with the ZIP codec through zlib).
+g++ -O2 -std=c++17 -w -DNANOVDB_USE_ZIP -I "$REF/ext/nanovdb" "$HERE/ref_nvdb_files.cpp" -o "$OUT/ref_nvdb_files" \
+    -lpthread -lz
+
 # common/basic_types.{h,cpp} host math (needs CUDA vector types, hence nvcc in host mode).
 NVCC="${NVCC:-nvcc}"
 "$NVCC" -std=c++17 -O2 -w -x cu -DCUDA_UTIL_DONT_USE_GL_INTEROP -I "$REF/common" "$HERE/ref_kat_basic.cu" "$REF/common/basic_types.cpp" \

@@ -65,6 +65,24 @@ class VptNoAllocTrace(C.Structure):
     ]
 
 
+class VptNanoVdbInfo(C.Structure):
+    """Mirror of ``VptNanoVdbInfo`` (include/rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("name", C.c_char * 256),
+        ("grid_type", C.c_uint32), ("grid_class", C.c_uint32),
+        ("grid_bytes", C.c_uint64), ("file_bytes", C.c_uint64), ("active_voxels", C.c_uint64),
+        ("index_min", C.c_int32 * 3), ("index_max", C.c_int32 * 3),
+        ("world_min", C.c_double * 3), ("world_max", C.c_double * 3), ("voxel_size", C.c_double * 3),
+        ("map_mat_f", C.c_float * 9), ("map_inv_mat_f", C.c_float * 9), ("map_vec_f", C.c_float * 3),
+        ("map_mat_d", C.c_double * 9), ("map_vec_d", C.c_double * 3),
+        ("background", C.c_float),
+        ("node_count", C.c_uint32 * 3), ("tile_count", C.c_uint32 * 3),
+        ("codec", C.c_uint32), ("grid_count", C.c_uint32), ("payload_offset", C.c_uint64),
+        ("extent_min", C.c_int32 * 3), ("extent_max", C.c_int32 * 3), ("flat_leaves", C.c_int64),
+    ]
+
+
 # name -> (restype, argtypes)
 _VPT = {
     "vpt_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -81,6 +99,11 @@ _VPT = {
     "vpt_download_volume_dense": (C.c_int, [C.c_void_p, c_float_p]),
     "vpt_get_volume_info": (C.c_int, [C.c_void_p, c_i64_p, c_i64_p, c_float_p, c_i64_p]),
     "vpt_download_cell_majorants": (C.c_int, [C.c_void_p, c_float_p]),
+    "vpt_nvdb_file_info": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(VptNanoVdbInfo)]),
+    "vpt_nanovdb_grid_info": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(VptNanoVdbInfo)]),
+    "vpt_nanovdb_decode_leaves": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64, c_i32_p, c_float_p, c_i64_p]),
+    "vpt_set_volume_nanovdb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "vpt_set_volume_nvdb_file": (C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64]),
     "vpt_set_environment_rgb": (C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32]),
     "vpt_get_importance_map_info": (C.c_int, [C.c_void_p, c_i32_p, c_i32_p, c_i32_p, c_i64_p, c_float_p]),
     "vpt_download_importance_map": (C.c_int, [C.c_void_p, c_float_p]),

@@ -644,3 +644,71 @@ int vpt_synchronize(VptContext* c, void* stream) {
 }
 
 }  // extern "C"
+
+namespace vpt {
+
+// Device side of vpt_set_volume_nanovdb: the flattened leaves (slot order), their table over the
+// leaf-aligned extent starting at index `lo`, and the grid's map and boxes. Cell majorants use
+// the same apron as the dense build; the global majorant scans [index_min, index_max) of the
+// grid's index box (renderer/renderer_scene.cpp:498-509).
+int upload_sparse_grid(VptContextImpl* c, const std::vector<int32_t>& table, int32_t lx, int32_t ly, int32_t lz,
+                       const std::vector<int32_t>& origins, const float* values, int64_t slots, const int32_t lo[3],
+                       const VptNanoVdbInfo& info) {
+    const int64_t cells = static_cast<int64_t>(lx) * ly * lz;
+    dev_free(&c->d_dense);
+    c->has_volume = false;
+    int32_t* d_origins = nullptr;
+    int rc;
+    if ((rc = dev_alloc(&c->d_cell_maj, cells)) || (rc = dev_alloc(&c->d_leaf_table, cells)) ||
+        (rc = dev_alloc(&c->d_leaf_values, std::max<int64_t>(slots, 1) * 512)) ||
+        (rc = dev_alloc(&d_origins, std::max<int64_t>(slots, 1) * 3)))
+        return rc;
+    VPT_CUDA(cudaMemcpy(c->d_leaf_table, table.data(), cells * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (slots > 0) {
+        VPT_CUDA(cudaMemcpy(c->d_leaf_values, values, slots * 512 * sizeof(float), cudaMemcpyHostToDevice));
+        VPT_CUDA(cudaMemcpy(d_origins, origins.data(), slots * 3 * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
+    c->lx = lx;
+    c->ly = ly;
+    c->lz = lz;
+    c->nx = 8 * lx;
+    c->ny = 8 * ly;
+    c->nz = 8 * lz;
+    vpt::sparse_leaf_stats(c->d_leaf_table, c->d_leaf_values, lx, ly, lz, c->d_cell_maj, 0);
+    int32_t box_lo[3], box_hi[3];
+    for (int a = 0; a < 3; ++a) {
+        box_lo[a] = info.index_min[a] - lo[a];
+        box_hi[a] = info.index_max[a] - lo[a];
+    }
+    vpt::leaf_box_max(c->d_leaf_values, d_origins, slots, box_lo, box_hi, c->d_scratch_u32, 0);
+    cudaError_t e = cudaGetLastError();
+    unsigned int gmax_bits = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&gmax_bits, c->d_scratch_u32, sizeof(unsigned int), cudaMemcpyDeviceToHost);
+    dev_free(&d_origins);
+    if (e != cudaSuccess) return set_error(VPT_ERR_CUDA, std::string("vpt_set_volume_nanovdb: ") + cudaGetErrorString(e));
+    std::memcpy(&c->global_majorant, &gmax_bits, sizeof(float));
+    c->active_leaves = slots;
+    c->total_leaves = cells;
+    // Lookups map world p to index (p - origin) * inv_voxel_size, origin being the world position
+    // of the extent's first voxel; for an extent starting at index 0 that is the grid's own
+    // float map (NanoVDB.h:2029-2032, applyInverseMapF).
+    c->voxel_size = info.map_mat_f[0];
+    c->inv_voxel_size = info.map_inv_mat_f[0];
+    float center[3];
+    float r2 = 0;
+    for (int a = 0; a < 3; ++a) {
+        c->origin[a] = static_cast<float>(info.map_vec_d[a] + static_cast<double>(lo[a]) * info.map_mat_d[4 * a]);
+        c->bbox_min[a] = static_cast<float>(info.world_min[a]);
+        c->bbox_max[a] = static_cast<float>(info.world_max[a]);
+        center[a] = (c->bbox_min[a] + c->bbox_max[a]) * 0.5f;
+        float d = c->bbox_max[a] - center[a];
+        r2 += d * d;
+    }
+    c->world_radius = std::sqrt(r2);
+    c->has_volume = true;
+    c->maj_shift = 0;  // the pooled majorant grid is rebuilt at the next launch
+    VPT_CUDA(cudaDeviceSynchronize());
+    return VPT_OK;
+}
+
+}  // namespace vpt

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <random>
+#include <vector>
 
 #include "../../include/rtc8_vpt.h"
 
@@ -82,6 +83,11 @@ int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);
+// Uploads a flattened sparse grid (leaf table over the extent starting at index `lo`, leaves in
+// slot order with their extent-relative origins) and derives its majorants (vpt_nvdb.cu).
+int upload_sparse_grid(VptContextImpl* c, const std::vector<int32_t>& table, int32_t lx, int32_t ly, int32_t lz,
+                       const std::vector<int32_t>& origins, const float* values, int64_t slots, const int32_t lo[3],
+                       const VptNanoVdbInfo& info);
 
 }  // namespace vpt
 

@@ -165,6 +165,69 @@ __global__ void pack_leaves_kernel(const float* __restrict__ dense, int nx, int 
     }
 }
 
+// leaf_stats_kernel for a grid held as leaves behind a table (absent leaves read 0): a cell
+// whose 3x3x3 neighbourhood of cells holds no leaf gets majorant 0 without reading voxels.
+__global__ void sparse_leaf_stats_kernel(const int32_t* __restrict__ table, const float* __restrict__ values, int lx,
+                                         int ly, int lz, float* __restrict__ cell_maj) {
+    const int64_t cell = blockIdx.x;
+    const int cz = static_cast<int>(cell % lz);
+    const int cy = static_cast<int>((cell / lz) % ly);
+    const int cx = static_cast<int>(cell / (static_cast<int64_t>(lz) * ly));
+    __shared__ int s_near;
+    __shared__ float s_mx[32];
+    if (threadIdx.x == 0) s_near = 0;
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        const int x = cx + static_cast<int>(threadIdx.x / 9) - 1, y = cy + static_cast<int>((threadIdx.x / 3) % 3) - 1,
+                  z = cz + static_cast<int>(threadIdx.x % 3) - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < lx && y < ly && z < lz &&
+            table[(static_cast<int64_t>(x) * ly + y) * lz + z] >= 0)
+            s_near = 1;
+    }
+    __syncthreads();
+    if (!s_near) {
+        if (threadIdx.x == 0) cell_maj[cell] = 0.0f;
+        return;
+    }
+    const int nx = 8 * lx, ny = 8 * ly, nz = 8 * lz;
+    float mx = 0.0f;
+    for (int q = threadIdx.x; q < 11 * 11 * 11; q += blockDim.x) {
+        const int dz = q % 11, dy = (q / 11) % 11, dx = q / 121;
+        const int x = cx * 8 - 1 + dx, y = cy * 8 - 1 + dy, z = cz * 8 - 1 + dz;
+        if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
+        const int32_t slot = table[(static_cast<int64_t>(x >> 3) * ly + (y >> 3)) * lz + (z >> 3)];
+        if (slot < 0) continue;
+        mx = fmaxf(mx, values[static_cast<int64_t>(slot) * 512 + (((x & 7) << 6) | ((y & 7) << 3) | (z & 7))]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_mx[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.0f;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) m = fmaxf(m, s_mx[w]);
+        cell_maj[cell] = m;
+    }
+}
+
+// Maximum of the leaf voxels inside [lo, hi) (non-negative start, so the float bits order like
+// unsigned integers).
+__global__ void leaf_box_max_kernel(const float* __restrict__ values, const int32_t* __restrict__ origins,
+                                    int64_t total, int3 lo, int3 hi, unsigned int* out) {
+    float mx = 0.0f;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t slot = i >> 9;
+        const int q = static_cast<int>(i & 511);
+        const int x = origins[3 * slot] + (q >> 6), y = origins[3 * slot + 1] + ((q >> 3) & 7),
+                  z = origins[3 * slot + 2] + (q & 7);
+        if (x >= lo.x && x < hi.x && y >= lo.y && y < hi.y && z >= lo.z && z < hi.z) mx = fmaxf(mx, values[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
+}
+
 // renderer_scene.cpp:498-509: the reference scans index coordinates [min, max) of the
 // inclusive index box, i.e. every voxel but the last plane along each axis.
 __global__ void global_max_kernel(const float* __restrict__ dense, int nx, int ny, int nz, unsigned int* out) {
@@ -243,6 +306,23 @@ void pack_leaves(const float* dense, int nx, int ny, int nz, int lx, int ly, int
                  float* values, cudaStream_t s) {
     int64_t cells = static_cast<int64_t>(lx) * ly * lz;
     pack_leaves_kernel<<<static_cast<unsigned int>(cells), 256, 0, s>>>(dense, nx, ny, nz, lx, ly, lz, table, values);
+}
+
+void sparse_leaf_stats(const int32_t* table, const float* values, int lx, int ly, int lz, float* cell_maj,
+                       cudaStream_t s) {
+    const int64_t cells = static_cast<int64_t>(lx) * ly * lz;
+    if (cells > 0)
+        sparse_leaf_stats_kernel<<<static_cast<unsigned int>(cells), 128, 0, s>>>(table, values, lx, ly, lz, cell_maj);
+}
+
+void leaf_box_max(const float* values, const int32_t* origins, int64_t slots, const int32_t box_lo[3],
+                  const int32_t box_hi[3], unsigned int* out, cudaStream_t s) {
+    cudaMemsetAsync(out, 0, sizeof(unsigned int), s);
+    if (slots <= 0) return;
+    const int64_t total = slots * 512;
+    const int blocks = static_cast<int>(std::min<int64_t>((total + 255) / 256, 152 * 16));
+    leaf_box_max_kernel<<<blocks, 256, 0, s>>>(values, origins, total, make_int3(box_lo[0], box_lo[1], box_lo[2]),
+                                               make_int3(box_hi[0], box_hi[1], box_hi[2]), out);
 }
 
 void global_max(const float* dense, int nx, int ny, int nz, unsigned int* out, cudaStream_t s) {

@@ -91,6 +91,24 @@ class Renderer:
                                                spec.base_frequency, spec.threshold, voxel_size, ptr(o, C.c_float)),
               "vpt_generate_fbm_volume")
 
+    def set_volume_nanovdb(self, grid: bytes) -> dict:
+        """Density volume from an in-memory NanoVDB float grid (Scene::allocateVolumeGrid,
+        renderer/renderer_scene.cpp:491-537); returns the grid's metadata."""
+        from . import nvdb
+
+        info = nvdb.grid_info(grid)
+        check(self.lib.vpt_set_volume_nanovdb(self.ctx, grid, len(grid)), "vpt_set_volume_nanovdb")
+        self._dims = tuple(8 * (hi - lo) // 8 for lo, hi in zip(info["extent_min"], info["extent_max"]))
+        return info
+
+    def load_nvdb(self, path, grid: int | str = 0) -> dict:
+        """Density volume from grid `grid` (index or name) of an .nvdb file (nanovdb::io::readGrid +
+        allocateVolumeGrid, renderer/renderer_scene.cpp:2468-2469); ZIP-coded grids are inflated
+        on the host first."""
+        from . import nvdb
+
+        return self.set_volume_nanovdb(nvdb.read_grid(path, grid))
+
     def download_volume(self) -> np.ndarray:
         info = self.volume_info()
         n = info["dims"]

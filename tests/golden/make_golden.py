@@ -9,15 +9,21 @@ It builds oracle/_ref/ with oracle/build_ref.sh and writes
                                       quaternion matrices, 16-band CIE CMF integrals)
   tests/golden/ref_nanovdb.json       NanoVDB 32.3 GridBuilder / SampleFromVoxels<1> / Ray::clip
   tests/golden/ref_hosek_kat.json     Hosek-Wilkie radiance at fixed angles (first sky entry)
+  tests/golden/nvdb/                  .nvdb files written by NanoVDB 32.3 io::writeGrid(s)
+                                      (gzip-compressed when uncoded) and ref_nvdb_files.json,
+                                      the reference's own reading of them
   rtc8_gb300/data/hosek_sky.json      per-band sky states used by the sky configurations
 The fixtures are committed; the GPU host never reads the reference.
 """
 from __future__ import annotations
 
+import gzip
 import json
 import os
+import shutil
 import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[2]
@@ -48,6 +54,17 @@ def main() -> int:
     (GOLDEN / "ref_hosek_kat.json").write_text(json.dumps({
         "elevation_deg": first["elevation_deg"], "turbidity": first["turbidity"], "albedo": first["albedo"],
         "band_theta_gamma_radiance": kat}))
+    nvdb_dir = GOLDEN / "nvdb"
+    nvdb_dir.mkdir(exist_ok=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        out = subprocess.run([str(REF_BIN / "ref_nvdb_files"), tmp], check=True, capture_output=True,
+                             text=True).stdout
+        (nvdb_dir / "ref_nvdb_files.json").write_text(json.dumps(json.loads(out)))
+        for name in ("multi.nvdb", "sphere_fog.nvdb"):
+            with open(Path(tmp) / name, "rb") as src, gzip.GzipFile(nvdb_dir / (name + ".gz"), "wb", 9,
+                                                                     mtime=0) as dst:
+                shutil.copyfileobj(src, dst)
+        shutil.copy(Path(tmp) / "sphere_zip.nvdb", nvdb_dir / "sphere_zip.nvdb")
     DATA.mkdir(exist_ok=True)
     sky["cmf"] = basic["cmf_xs_ys_zs_centers_integral"]
     sky["source"] = ("Hosek-Wilkie 2013 v1.4a model states (arhosekskymodelstate_alloc_init) per renderer band, "
