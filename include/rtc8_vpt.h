@@ -249,6 +249,22 @@ typedef struct VptNoAllocTrace {
     float* mean_rgb;            /* 3 per pixel */
 } VptNoAllocTrace;
 int vpt_launch_plain_noalloc(const VptNoAllocTrace* args, void* stream);
+/* ---- image output -------------------------------------------------------------------- */
+#define VPT_SDR_SRGB 0x1u     /* sRGB gamma before the 8-bit conversion (the headless default) */
+#define VPT_SDR_FLIP_Y 0x2u   /* write rows bottom-up */
+/* Tone map of the accumulated mean image, replacing the applyToneMap kernel
+ * (renderer/gpu_kernels/post_process_kernels.cu:10-41: per channel x^(1/0.6), then the colour
+ * scaled by (1 - exp(-brightness * lum)) / lum; the reference's brightness is 1), fused with the
+ * 8-bit conversion of saveImage (common/common_host.cpp:517-568) as the headless loop sets it
+ * up (renderer/renderer_main.cpp:1490-1495: no second tone map, negatives clamped to 0, sRGB
+ * gamma, min(uint(v * 255), 255) per channel, alpha 255). dev_rgba32 receives width*height
+ * float4 (the reference's outputBuffer, alpha 1), dev_rgba8 width*height 32-bit RGBA words
+ * (R in the low byte); either may be NULL. Asynchronous on `stream`. */
+int vpt_tonemap(VptContext* ctx, void* stream, float brightness, uint32_t sdr_flags, float* dev_rgba32,
+                uint32_t* dev_rgba8);
+/* The same into a context-owned device image, copied to host_rgba8 (width*height words):
+ * the frame enqueueSaveImage writes to "%03u.png" (renderer_main.cpp:1646-1655). Synchronous. */
+int vpt_download_image_rgba8(VptContext* ctx, float brightness, uint32_t sdr_flags, uint32_t* host_rgba8);
 int vpt_reset_accumulation(VptContext* ctx);
 
 /* Reads back the accumulation: FP64 per-pixel RGB sums and sample count, FP32 running mean. */

@@ -48,6 +48,8 @@ _FUNCS = {
     "orc_build_imp_map": (C.c_float, [f32p, C.c_int32, C.c_int32, f32p]),
     "orc_majorants": (C.c_float, [f32p, C.c_int32, C.c_int32, C.c_int32, f32p]),
     "orc_sample_density": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p]),
+    "orc_srgb_gamma": (None, [f32p, C.c_int32, f32p]),
+    "orc_tonemap": (None, [f32p, C.c_int32, C.c_float, C.c_int32, f32p, C.POINTER(C.c_uint8)]),
     "orc_clip_rays": (None, [C.POINTER(OrcScene), f32p, f32p, C.c_int32, f32p, f32p, i32p]),
     "orc_env_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p, f32p]),
     "orc_env_evaluate": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p]),
@@ -112,6 +114,23 @@ def majorants(vox: np.ndarray) -> tuple[np.ndarray, float]:
     cells = np.zeros(((nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8), dtype=np.float32)
     g = lib().orc_majorants(p(v, C.c_float), nx, ny, nz, p(cells, C.c_float))
     return cells, float(g)
+
+
+def srgb_gamma(v: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(v, dtype=np.float32)
+    out = np.zeros_like(a)
+    lib().orc_srgb_gamma(p(a, C.c_float), a.size, p(out, C.c_float))
+    return out
+
+
+def tonemap(mean_rgb: np.ndarray, brightness: float = 1.0, srgb: bool = True) -> tuple[np.ndarray, np.ndarray]:
+    """Tone-mapped float RGB and 8-bit RGBA of a mean image (..., 3)."""
+    m = np.ascontiguousarray(mean_rgb, dtype=np.float32)
+    n = m.size // 3
+    out = np.zeros(m.shape, dtype=np.float32)
+    rgba = np.zeros(m.shape[:-1] + (4,), dtype=np.uint8)
+    lib().orc_tonemap(p(m, C.c_float), n, brightness, int(srgb), p(out, C.c_float), p(rgba, C.c_uint8))
+    return out, rgba
 
 
 def pool_cells(cells: np.ndarray, factor: int) -> np.ndarray:

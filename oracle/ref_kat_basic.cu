@@ -1,6 +1,8 @@
 // Known-answer generator built from the reference's own common/basic_types.{h,cpp} (host code
 // only, compiled by oracle/build_ref.sh into oracle/_ref/). Prints JSON with the outputs of the
 // reference's math helpers on fixed inputs; tests/golden/make_golden.py stores them as fixtures.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <random>
 
@@ -65,6 +67,52 @@ int main() {
     float lum_in[3] = {0.25f, 0.5f, 0.75f};
     float lum = RGBSpectrum(lum_in[0], lum_in[1], lum_in[2]).luminance();
 
+    // sRGB_gamma_s (basic_types.h:3181-3188) on fixed inputs, and the output path of the
+    // headless loop: applyToneMap (renderer/gpu_kernels/post_process_kernels.cu:10-41, device code
+    // there, evaluated here on the host with the same RGBSpectrum and std functions) followed by
+    // saveImage's 8-bit conversion (common/common_host.cpp:517-568, applyToneMap off, sRGB on).
+    const int NS = 40;
+    float srgb_in[NS], srgb_out[NS];
+    for (int i = 0; i < NS; ++i) {
+        float v = 0.5f * (u(gen) + 1.0f) * 1.25f;
+        if (i == 0) v = 0.0f;
+        if (i == 1) v = 0.0031308f;
+        if (i == 2) v = std::nextafter(0.0031308f, 1.0f);
+        if (i == 3) v = 1.0f;
+        if (i == 4) v = 1e-4f;
+        srgb_in[i] = v;
+        srgb_out[i] = sRGB_gamma_s(v);
+    }
+    const int NT = 96;
+    float tm_in[3 * NT], tm_out[3 * NT], tm_bytes[3 * NT];
+    for (int i = 0; i < NT; ++i) {
+        RGBSpectrum c((u(gen) + 1.0f) * 1.5f, (u(gen) + 1.0f) * 1.5f, (u(gen) + 1.0f) * 1.5f);
+        if (i == 0) c = RGBSpectrum(0.0f, 0.0f, 0.0f);
+        if (i == 1) c = RGBSpectrum(0.0f, 0.25f, 0.0f);
+        if (i == 2) c = RGBSpectrum(40.0f, 0.001f, 0.5f);
+        tm_in[3 * i] = c.r;
+        tm_in[3 * i + 1] = c.g;
+        tm_in[3 * i + 2] = c.b;
+        constexpr float gamma = 1.0f / 0.6f;
+        c.r = std::pow(c.r, gamma);
+        c.g = std::pow(c.g, gamma);
+        c.b = std::pow(c.b, gamma);
+        float lum = c.luminance();
+        if (lum > 0.0f) {
+            float lumT = 1 - std::exp(-1.0f * lum);
+            c *= lumT / lum;
+        }
+        tm_out[3 * i] = c.r;
+        tm_out[3 * i + 1] = c.g;
+        tm_out[3 * i + 2] = c.b;
+        RGBSpectrum v = c;
+        if (v.hasNegative()) v = max(v, RGBSpectrum::Zero());
+        v = sRGB_gamma(v);
+        tm_bytes[3 * i] = static_cast<float>(std::min<uint32_t>(static_cast<uint32_t>(v.r * 255), 255));
+        tm_bytes[3 * i + 1] = static_cast<float>(std::min<uint32_t>(static_cast<uint32_t>(v.g * 255), 255));
+        tm_bytes[3 * i + 2] = static_cast<float>(std::min<uint32_t>(static_cast<uint32_t>(v.b * 255), 255));
+    }
+
     std::printf("{\n");
     print_floats("dirs", vin, 3 * N);
     print_floats("polar_yup_theta_phi", polar, 2 * N);
@@ -74,7 +122,12 @@ int main() {
     print_floats("quats", qin, 32);
     print_floats("quat_matrices_colmajor", mats, 72);
     print_floats("cmf_xs_ys_zs_centers_integral", cmf, 65);
-    print_floats("luminance_of_0.25_0.5_0.75", &lum, 1, true);
+    print_floats("luminance_of_0.25_0.5_0.75", &lum, 1);
+    print_floats("srgb_gamma_in", srgb_in, NS);
+    print_floats("srgb_gamma_out", srgb_out, NS);
+    print_floats("tonemap_mean_rgb", tm_in, 3 * NT);
+    print_floats("tonemap_out_rgb", tm_out, 3 * NT);
+    print_floats("tonemap_srgb_bytes", tm_bytes, 3 * NT, true);
     std::printf("}\n");
     return 0;
 }

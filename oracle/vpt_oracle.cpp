@@ -897,6 +897,50 @@ float orc_majorants(const float* v, int32_t nx, int32_t ny, int32_t nz, float* c
     return g;
 }
 
+// sRGB_gamma_s (basic_types.h:3181-3188).
+void orc_srgb_gamma(const float* in, int32_t n, float* out) {
+    for (int32_t i = 0; i < n; ++i) {
+        const float v = in[i];
+        out[i] = v <= 0.0031308f ? 12.92f * v : 1.055f * std::pow(v, static_cast<float>(1 / 2.4)) - 0.055f;
+    }
+}
+
+// applyToneMap (renderer/gpu_kernels/post_process_kernels.cu:10-41) and the 8-bit conversion of
+// saveImage (common/common_host.cpp:517-568) with the headless loop's settings
+// (renderer_main.cpp:1490-1495): x^(1/0.6) per channel, colour * (1 - exp(-b * lum)) / lum,
+// negatives clamped to 0, sRGB_gamma_s (basic_types.h:3181-3188) when srgb is set,
+// min(uint(v * 255), 255) per channel (NaN -> 0), alpha 255.
+void orc_tonemap(const float* mean, int32_t n, float brightness, int32_t srgb, float* out_rgb, uint8_t* out_rgba) {
+    auto gamma_s = [](float v) {
+        if (v <= 0.0031308f) return 12.92f * v;
+        return 1.055f * std::pow(v, static_cast<float>(1 / 2.4)) - 0.055f;
+    };
+    auto to_byte = [](float v) -> uint8_t {
+        const float x = v * 255.0f;
+        if (!(x > 0.0f)) return 0;
+        if (x >= 255.0f) return 255;
+        return static_cast<uint8_t>(static_cast<uint32_t>(x));
+    };
+    for (int32_t i = 0; i < n; ++i) {
+        constexpr float kGamma = 1.0f / 0.6f;
+        float c[3] = {std::pow(mean[3 * i], kGamma), std::pow(mean[3 * i + 1], kGamma),
+                      std::pow(mean[3 * i + 2], kGamma)};
+        const float lum = 0.2126729f * c[0] + 0.7151522f * c[1] + 0.0721750f * c[2];
+        if (lum > 0.0f) {
+            const float lum_t = 1 - std::exp(-brightness * lum);
+            const float sc = lum_t / lum;
+            for (float& v : c) v *= sc;
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (out_rgb) out_rgb[3 * i + k] = c[k];
+            float v = std::fmax(c[k], 0.0f);
+            if (srgb) v = gamma_s(v);
+            if (out_rgba) out_rgba[4 * i + k] = to_byte(v);
+        }
+        if (out_rgba) out_rgba[4 * i + 3] = 255;
+    }
+}
+
 void orc_sample_density(const OrcScene* sc, const float* idx, int32_t n, float* out) {
     for (int i = 0; i < n; ++i) out[i] = sample_trilinear(*sc, v3(idx[3 * i], idx[3 * i + 1], idx[3 * i + 2]));
 }

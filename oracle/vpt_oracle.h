@@ -121,6 +121,10 @@ float orc_majorants(const float* voxels, int32_t nx, int32_t ny, int32_t nz, flo
 
 /* Component batch entry points used by the known-answer tests. */
 void orc_sample_density(const OrcScene* sc, const float* idx_xyz, int32_t n, float* out);
+void orc_srgb_gamma(const float* in, int32_t n, float* out);
+/* Tone map + 8-bit sRGB conversion of a mean image (n RGB pixels) into out_rgb (3 floats per
+ * pixel) and out_rgba (4 bytes per pixel); either may be NULL. */
+void orc_tonemap(const float* mean, int32_t n, float brightness, int32_t srgb, float* out_rgb, uint8_t* out_rgba);
 void orc_clip_rays(const OrcScene* sc, const float* org, const float* dir, int32_t n,
                    float* t0, float* t1, int32_t* hit);
 void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, float* pdf,

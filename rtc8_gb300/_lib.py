@@ -10,6 +10,9 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "librtc8_gb300.so"
 
+VPT_SDR_SRGB = 0x1  # include/rtc8_vpt.h
+VPT_SDR_FLIP_Y = 0x2
+
 c_float_p = C.POINTER(C.c_float)
 c_double_p = C.POINTER(C.c_double)
 c_u32_p = C.POINTER(C.c_uint32)
@@ -114,6 +117,8 @@ _VPT = {
     "vpt_launch_plain": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vpt_launch_plain_logged": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vpt_launch_plain_noalloc": (C.c_int, [C.POINTER(VptNoAllocTrace), C.c_void_p]),
+    "vpt_tonemap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "vpt_download_image_rgba8": (C.c_int, [C.c_void_p, C.c_float, C.c_uint32, c_u32_p]),
     "vpt_reset_accumulation": (C.c_int, [C.c_void_p]),
     "vpt_download_sum": (C.c_int, [C.c_void_p, c_double_p, c_u32_p]),
     "vpt_download_mean": (C.c_int, [C.c_void_p, c_float_p]),

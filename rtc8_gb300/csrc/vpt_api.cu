@@ -113,6 +113,7 @@ int vpt_destroy(VptContext* c) {
     dev_free(&c->d_maj);
     dev_free(&c->d_jumps);
     dev_free(&c->d_dense);
+    dev_free(&c->d_rgba8);
     dev_free(&c->d_env);
     dev_free(&c->d_mips);
     delete c;

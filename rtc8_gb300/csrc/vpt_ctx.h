@@ -23,6 +23,7 @@ struct VptContextImpl {
     uint64_t* d_rng = nullptr;
     double* d_sum = nullptr;
     float* d_mean = nullptr;
+    uint32_t* d_rgba8 = nullptr;   // 8-bit output image of vpt_download_image_rgba8 (allocated on first use)
     uint32_t accum_samples = 0;
     uint32_t stream_samples = 0;   // samples ever traced since seeding (sample-parallel streams)
     uint32_t* d_frame = nullptr;   // device copy of {stream_samples, accum_samples} (authoritative)
@@ -83,6 +84,8 @@ int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);
+// Tone map + 8-bit conversion of the mean image (vpt_post.cu).
+int launch_tonemap(VptContextImpl* c, cudaStream_t s, float brightness, uint32_t flags, float* rgba32, uint32_t* rgba8);
 // Uploads a flattened sparse grid (leaf table over the extent starting at index `lo`, leaves in
 // slot order with their extent-relative origins) and derives its majorants (vpt_nvdb.cu).
 int upload_sparse_grid(VptContextImpl* c, const std::vector<int32_t>& table, int32_t lx, int32_t ly, int32_t lz,

@@ -196,6 +196,27 @@ class Renderer:
         s, n = self.download_sum()
         return s / max(n, 1)
 
+    def image_rgba8(self, brightness: float = 1.0, srgb: bool = True, flip_y: bool = False) -> np.ndarray:
+        """The frame the headless loop saves: tone map + sRGB + 8-bit conversion on the device
+        (vpt_download_image_rgba8), as an (h, w, 4) uint8 array."""
+        out = np.empty((self.height, self.width), dtype=np.uint32)
+        flags = (_lib.VPT_SDR_SRGB if srgb else 0) | (_lib.VPT_SDR_FLIP_Y if flip_y else 0)
+        check(self.lib.vpt_download_image_rgba8(self.ctx, brightness, flags, ptr(out, C.c_uint32)),
+              "vpt_download_image_rgba8")
+        return out.view(np.uint8).reshape(self.height, self.width, 4)
+
+    def save_png(self, path, brightness: float = 1.0) -> None:
+        """Writes the current frame as the reference's headless loop does ("%03u.png")."""
+        from . import image
+
+        image.write_png(path, self.image_rgba8(brightness))
+
+    def save_exr(self, path, brightness: float = 1.0, flip_y: bool = False) -> None:
+        """Writes the mean image as saveImageHDR does (half-float A, B, G, R channels)."""
+        from . import image
+
+        image.write_exr(path, self.download_mean().reshape(self.height, self.width, 3), brightness, flip_y)
+
     def counters(self) -> dict:
         a, b, c, d = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
         check(self.lib.vpt_get_counters(self.ctx, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "vpt_get_counters")
