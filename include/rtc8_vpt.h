@@ -80,6 +80,11 @@ typedef struct VptFrameParams {
     /* log2 of the majorant-grid cell size in voxels (>= 3; 3 = one cell per 8^3 leaf). Larger
      * cells mean fewer DDA steps per ray and looser majorants. */
     int32_t majorant_cell_log2;
+    /* Russian roulette on the transmittance of NEE shadow rays (configuration mode; 0 = off, the
+     * reference's plain ratio tracking): once a shadow ray's visibility drops below this
+     * threshold it survives with probability vis / threshold and continues with visibility
+     * = threshold (unbiased); the extra random number is drawn from the path's stream. */
+    float shadow_rr_threshold;
 } VptFrameParams;
 
 /* ---- context ------------------------------------------------------------------------ */
@@ -281,6 +286,15 @@ int vpt_reset_counters(VptContext* ctx);
 uint32_t vpt_get_device_errors(VptContext* ctx);
 int vpt_synchronize(VptContext* ctx, void* stream);
 
+/* Tracker of vpt_launch_plain: kind 0 = persistent megakernel (the default: one launch,
+ * asynchronous, capturable in a CUDA graph), 1 = wavefront: an event kernel and a persistent
+ * tracking kernel alternate in passes over per-slot path state, the host issuing passes until
+ * every slot retired, so the call returns once the launch's work is nearly done; a stream under
+ * graph capture always gets the megakernel. slots_per_sm (paths in flight per SM, 0 = 3072),
+ * pass_steps (lookups a segment may take per pass, 0 = 64) and track_ctas_per_sm (0 = as many
+ * as fit) tune the wavefront. Both trackers draw each path's random numbers in the same order. */
+int vpt_set_tracker(VptContext* ctx, int32_t kind, int32_t slots_per_sm, int32_t pass_steps,
+                    int32_t track_ctas_per_sm);
 /* Launch shape of the persistent tracker (CTAs per SM, threads per CTA) and the number of
  * parked lanes of a warp that triggers its joint event phase; 0 = defaults. */
 int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,

@@ -36,7 +36,7 @@ class OrcScene(C.Structure):
         ("cam_aspect", C.c_float), ("cam_fovy", C.c_float), ("cam_pos", C.c_float * 3), ("cam_quat", C.c_float * 4),
         ("width", C.c_int32), ("height", C.c_int32),
         ("max_bounces", C.c_int32), ("rr_start", C.c_int32), ("majorant_mode", C.c_int32), ("max_steps", C.c_int32),
-        ("stream_mode", C.c_int32), ("maj_shift", C.c_int32),
+        ("stream_mode", C.c_int32), ("maj_shift", C.c_int32), ("shadow_rr", C.c_float),
     ]
 
 
@@ -158,7 +158,8 @@ def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: 
                cam_aspect: float, cam_fovy: float, cam_pos, cam_quat, sun_dir=None, sun_irradiance=0.0,
                sun_prob=0.5, max_bounces=0, rr_start=1, majorant_mode=0, max_steps=0, stream_mode=0, maj_shift=3,
                env_power=1.0,
-               env_rotation=0.0, cells: np.ndarray | None = None, global_majorant: float | None = None) -> OracleScene:
+               env_rotation=0.0, cells: np.ndarray | None = None, global_majorant: float | None = None,
+               shadow_rr: float = 0.0) -> OracleScene:
     s = OrcScene()
     v = np.ascontiguousarray(voxels, dtype=np.float32)
     keep = [v]
@@ -219,6 +220,7 @@ def make_scene(*, voxels: np.ndarray, voxel_size: float, origin, density_coeff: 
     s.width, s.height = width, height
     s.max_bounces, s.rr_start, s.majorant_mode, s.max_steps = max_bounces, rr_start, majorant_mode, max_steps
     s.stream_mode = stream_mode
+    s.shadow_rr = shadow_rr if 0.0 < shadow_rr < 1.0 else 0.0
     return OracleScene(s, keep)
 
 
@@ -235,7 +237,8 @@ def scene_from_config(cfg, voxels: np.ndarray, env_rgb: np.ndarray | None, **ove
               sun_dir=None if sun is None else sun.astype(np.float32), sun_irradiance=cfg.sun_irradiance,
               sun_prob=cfg.sun_select_prob, max_bounces=cfg.max_bounces, rr_start=cfg.rr_start_vertex,
               majorant_mode=cfg.majorant_mode, max_steps=cfg.max_steps_per_segment,
-              stream_mode=cfg.rng_stream_mode, maj_shift=cfg.majorant_cell_log2)
+              stream_mode=cfg.rng_stream_mode, maj_shift=cfg.majorant_cell_log2,
+              shadow_rr=cfg.shadow_rr_threshold)
     kw.update(over)
     return make_scene(**kw)
 

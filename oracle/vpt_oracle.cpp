@@ -418,6 +418,19 @@ inline void dda_init(const OrcScene& s, V3 eye, V3 dir, float t, Dda* d) {
     }
 }
 
+// Russian roulette on a shadow ray's visibility once it drops below s.shadow_rr (configuration
+// mode; an extra draw from the path's stream). Returns true when the ray is terminated (vis = 0).
+inline bool shadow_roulette(const OrcScene& s, Pcg32& rng, float* vis) {
+    if (!(*vis < s.shadow_rr)) return false;
+    const float q = *vis / s.shadow_rr;
+    if (rng.uniform() >= q) {
+        *vis = 0.0f;
+        return true;
+    }
+    *vis = s.shadow_rr;
+    return false;
+}
+
 // Tracks [t, t1] along (eye, dir). Delta tracking (shadow = false) returns SEG_COLLIDE with
 // *t at the collision; ratio tracking (shadow = true) multiplies *vis.
 inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, float t1, bool shadow,
@@ -436,6 +449,10 @@ inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, f
             ++seg_steps;
             if (shadow) {
                 *vis *= (1 - density / maj);
+                if (shadow_roulette(s, rng, vis)) {
+                    *tio = t;
+                    return SEG_EXIT;
+                }
             } else if (rng.uniform() < density / maj) {
                 *tio = t;
                 return SEG_COLLIDE;
@@ -462,6 +479,10 @@ inline SegEnd track(const OrcScene& s, Pcg32& rng, V3 eye, V3 dir, float* tio, f
                 ++seg_steps;
                 if (shadow) {
                     *vis *= (1 - density / maj);
+                    if (shadow_roulette(s, rng, vis)) {
+                        *tio = t1;
+                        return SEG_EXIT;
+                    }
                 } else if (rng.uniform() < density / maj) {
                     *tio = t;
                     return SEG_COLLIDE;

@@ -66,6 +66,7 @@ typedef struct OrcScene {
     int32_t max_steps;         /* safety cap on density lookups per segment, 0 = none */
     int32_t stream_mode;       /* 0 = per-pixel sequential streams, 1 = sample s jumped by s * 2^40 */
     int32_t maj_shift;         /* majorant cells of 2^maj_shift voxels (cell_majorant has cx*cy*cz) */
+    float shadow_rr;           /* Russian-roulette threshold of shadow-ray visibility, 0 = off */
 } OrcScene;
 
 /* Per-sample decision record: vertices, primary lookups, shadow lookups, end code. */

@@ -47,6 +47,7 @@ class VptFrameParams(C.Structure):
         ("max_steps_per_segment", C.c_int32),
         ("rng_stream_mode", C.c_int32),
         ("majorant_cell_log2", C.c_int32),
+        ("shadow_rr_threshold", C.c_float),
     ]
 
 
@@ -128,6 +129,7 @@ _VPT = {
     "vpt_get_device_errors": (C.c_uint32, [C.c_void_p]),
     "vpt_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vpt_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "vpt_set_tracker": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "vpt_generate_fbm_union": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float,
                                          C.c_float, C.c_float, C.c_float, c_float_p]),
     "vpt_nrc_enable": (C.c_int, [C.c_void_p]),

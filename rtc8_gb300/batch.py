@@ -54,6 +54,9 @@ class SceneBatch:
         for cfg in self.configs:
             r = Renderer(cfg.width, cfg.height)
             setup_scene(r, cfg)
+            # The batch step is one CUDA graph: its launches are the persistent megakernel (the
+            # wavefront tracer issues its passes from the host and cannot be captured).
+            r.set_tracker(0)
             self.renderers.append(r)
         self.streams = [torch.cuda.Stream() for _ in self.renderers]
         self.graph = None

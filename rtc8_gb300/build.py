@@ -23,7 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
 # Units whose float arithmetic must follow the reference's operation order.
-NO_FMA_UNITS = {"vpt_tracer.cu", "nrc_tracer.cu", "vpt_post.cu"}
+NO_FMA_UNITS = {"vpt_tracer.cu", "nrc_tracer.cu", "vpt_post.cu", "vpt_wavefront.cu"}
 
 
 def nvcc() -> str:

@@ -62,6 +62,10 @@ class SceneConfig:
     max_steps_per_segment: int = 1 << 20
     rng_stream_mode: int = 1       # 0 = reference per-pixel sequential streams, 1 = sample-parallel
     majorant_cell_log2: int = 3    # majorant-grid cell = 2^k voxels (3: one cell per 8^3 leaf)
+    # Russian roulette on NEE shadow-ray visibility below this threshold (unbiased; 0 = off, the
+    # reference's plain ratio tracking). About 85% of the density lookups of these scenes are
+    # shadow-ray steps, most of them where the visibility is already near zero.
+    shadow_rr_threshold: float = 0.1
     fov_deg: float = 40.0
     cam_distance_diagonals: float = 2.5
     cam_direction: tuple = (0.55, 0.3, 1.0)   # from the grid centre towards the camera
@@ -84,7 +88,8 @@ C1 = SceneConfig(name="c1_dense64_256px", width=256, height=256, spp=16,
 # The same scene rendered with the reference's own path rules: single global majorant,
 # Schlick phase function, no bounce cap, Russian roulette at every vertex, environment only.
 C1_REFERENCE_MODE = C1.replace(name="c1_reference_mode", phase_kind=0, phase_param=0.0, sun_elevation_deg=None,
-                               max_bounces=0, rr_start_vertex=1, majorant_mode=0, rng_stream_mode=0)
+                               max_bounces=0, rr_start_vertex=1, majorant_mode=0, rng_stream_mode=0,
+                               shadow_rr_threshold=0.0)
 
 # BASELINE configuration 2: 1024^2 x 64 spp, sparse 512^3 fBm (6 octaves, threshold 0.55),
 # sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256 bounces, sun at 20 degrees + Hosek sky.

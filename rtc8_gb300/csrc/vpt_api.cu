@@ -98,6 +98,7 @@ int vpt_create(int32_t w, int32_t h, VptContext** out) {
 int vpt_destroy(VptContext* c) {
     if (!c) return VPT_OK;
     c->release_nrc();
+    c->release_wf();
     dev_free(&c->d_rng);
     dev_free(&c->d_sum);
     dev_free(&c->d_mean);
@@ -516,6 +517,7 @@ int fill_trace_params(VptContextImpl* c, TraceParams* tp) {
     tp->max_bounces = f.max_bounces;
     tp->rr_start = f.rr_start_vertex;
     tp->max_steps = f.max_steps_per_segment;
+    tp->shadow_rr = f.shadow_rr_threshold > 0.0f && f.shadow_rr_threshold < 1.0f ? f.shadow_rr_threshold : 0.0f;
     tp->rng = c->d_rng;
     tp->sum_rgb = c->d_sum;
     tp->mean_rgb = c->d_mean;
@@ -565,8 +567,22 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         tp.maj_in_smem = 1;
         smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
     }
-    int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr), smem);
-    vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
+    if (c->tracker == 1 && capture == cudaStreamCaptureStatusNone) {
+        // Wavefront tracer: its passes are issued from the host until every slot retired (not
+        // capturable; a stream being captured gets the persistent megakernel below).
+        const uint64_t items = tp.stream_mode == 1 ? npix * spp : npix;
+        const uint64_t per_sm = c->wf_slots_per_sm > 0 ? static_cast<uint64_t>(c->wf_slots_per_sm) : 3072u;
+        const uint32_t slots = static_cast<uint32_t>(std::min<uint64_t>(items, per_sm * c->num_sms));
+        int rc3 = vpt::wf_ensure(c, slots);
+        if (rc3) return rc3;
+        rc3 = vpt::wf_run(c, tp, grid_maj, smem, s);
+        if (rc3) return rc3;
+    } else {
+        int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr), smem);
+        vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
+    }
     if (tp.stream_mode == 1)
         vpt::launch_finalize_mean_dev(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->d_frame, spp, s);
     vpt::launch_frame_update(c->d_frame, spp, false, spp, s);

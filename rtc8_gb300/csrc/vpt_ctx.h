@@ -14,6 +14,32 @@ namespace vpt {
 struct TraceParams;
 struct NrcBuffers;
 
+// Per-slot path state of the wavefront tracer (vpt_wavefront.cu), structure of arrays.
+struct WfBuffers {
+    uint32_t slots = 0;                // slots of the current launch (queue stride)
+    uint32_t capacity = 0;             // allocated slots
+    uint64_t* rng = nullptr;
+    uint32_t* pixel = nullptr;
+    uint32_t* sample = nullptr;
+    uint32_t* path_length = nullptr;
+    uint32_t* flags = nullptr;         // state | end code << 8 | segment flags
+    uint2* rec = nullptr;              // primary / shadow lookups of the sample (decision log)
+    float4* org = nullptr;             // vertex position, direction pdf
+    float4* dir = nullptr;             // direction, initial importance
+    float4* tp = nullptr;              // throughput, NEE area pdf
+    float4* contrib = nullptr;         // contribution, NEE visibility
+    float4* emit = nullptr;            // NEE emittance
+    float4* seg0 = nullptr;            // segment eye, t
+    float4* seg1 = nullptr;            // segment direction, t1
+    int4* dda_i = nullptr;             // suspended segment: DDA cell, lookups so far
+    float4* dda_f = nullptr;           // suspended segment: DDA tnext
+    double* sum = nullptr;             // per-pixel streams: the pixel's sums (3 per slot)
+    float4* mean = nullptr;            // per-pixel streams: the pixel's running mean
+    uint32_t* track_queue = nullptr;   // 2 x slots
+    uint32_t* event_queue = nullptr;   // 2 x slots
+    uint32_t* count = nullptr;         // [0,1] tracking queues, [2,3] event queues, [4] tracking fetch
+};
+
 struct VptContextImpl {
     int32_t width = 0, height = 0;
     int device = 0, num_sms = 0;
@@ -62,6 +88,14 @@ struct VptContextImpl {
     bool has_frame = false;
 
     // neural-radiance-cache render/training buffers (allocated on first use)
+    // wavefront tracer of the plain path (allocated on first use)
+    int32_t tracker = 0;                // 0 = persistent megakernel, 1 = wavefront
+    int32_t wf_slots_per_sm = 0, wf_pass_steps = 0, wf_track_ctas_per_sm = 0;
+    WfBuffers wf;
+    uint32_t* wf_pinned = nullptr;
+    cudaEvent_t wf_events[8] = {};
+    void release_wf();
+
     NrcBuffers* nrc = nullptr;
     int32_t nrc_query_density = 0;
     float nrc_termination = 0.0f;          // 0 = the reference's pathTerminationFactor
@@ -84,6 +118,10 @@ int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged);
+// Wavefront plain tracer: runs the passes of one launch on `s` (vpt_wavefront.cu).
+int wf_run(VptContextImpl* c, const TraceParams& tp, bool grid_majorant, size_t smem, cudaStream_t s);
+int wf_ensure(VptContextImpl* c, uint32_t slots);
+const void* wf_track_kernel_ptr(bool grid_majorant);
 // Tone map + 8-bit conversion of the mean image (vpt_post.cu).
 int launch_tonemap(VptContextImpl* c, cudaStream_t s, float brightness, uint32_t flags, float* rgba32, uint32_t* rgba8);
 // Uploads a flattened sparse grid (leaf table over the extent starting at index `lo`, leaves in

@@ -152,6 +152,7 @@ extern "C" int vpt_launch_plain_noalloc(const VptNoAllocTrace* a, void* stream) 
     tp.max_bounces = f.max_bounces;
     tp.rr_start = f.rr_start_vertex;
     tp.max_steps = f.max_steps_per_segment;
+    tp.shadow_rr = f.shadow_rr_threshold > 0.0f && f.shadow_rr_threshold < 1.0f ? f.shadow_rr_threshold : 0.0f;
     tp.spp = a->spp;
     tp.accum_base = a->accum_base;
     tp.stream_mode = f.rng_stream_mode;

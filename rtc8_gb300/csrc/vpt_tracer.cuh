@@ -61,6 +61,7 @@ struct TraceParams {
     int32_t nrc_density_query;  // 1: the query's roughness slot carries density / density_coeff
     float nrc_termination;      // path-spread termination factor c (0 = 0.01, renderer_shared.h:11)
     float nrc_train_termination;  // factor of biased training suffixes (0 = 2c)
+    float shadow_rr;              // Russian-roulette threshold of shadow-ray visibility (0 = off)
 };
 
 // Majorant grids up to this many cells are staged in shared memory (32 KB).

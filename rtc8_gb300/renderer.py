@@ -165,6 +165,10 @@ class Renderer:
         self.params = p
         check(self.lib.vpt_set_frame_params(self.ctx, C.byref(p)), "vpt_set_frame_params")
 
+    def set_tracker(self, kind: int = 0, slots_per_sm: int = 0, pass_steps: int = 0, track_ctas_per_sm: int = 0) -> None:
+        """0 = persistent megakernel (default), 1 = wavefront; see vpt_set_tracker."""
+        check(self.lib.vpt_set_tracker(self.ctx, kind, slots_per_sm, pass_steps, track_ctas_per_sm), "vpt_set_tracker")
+
     def set_launch_shape(self, ctas_per_sm: int = 0, threads: int = 0, park_threshold: int = 0) -> None:
         check(self.lib.vpt_set_launch_shape(self.ctx, ctas_per_sm, threads, park_threshold), "vpt_set_launch_shape")
 
@@ -333,6 +337,7 @@ def frame_params(cfg: SceneConfig, env_enabled: bool = True) -> VptFrameParams:
     p.max_steps_per_segment = cfg.max_steps_per_segment
     p.rng_stream_mode = cfg.rng_stream_mode
     p.majorant_cell_log2 = cfg.majorant_cell_log2
+    p.shadow_rr_threshold = cfg.shadow_rr_threshold
     return p
 
 

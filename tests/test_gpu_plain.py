@@ -20,11 +20,12 @@ pytestmark = pytest.mark.gpu
 DECISION_PARITY = 0.999
 
 
-def _gpu_logged(cfg, vox, env, spp):
+def _gpu_logged(cfg, vox, env, spp, tracker=0, **tracker_kw):
     import torch
 
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg, volume=vox)
+    r.set_tracker(tracker, **tracker_kw)
     if env is not None and cfg.sky is None:
         r.set_environment_rgb(env)
     log = torch.zeros(cfg.width * cfg.height * spp * 4, dtype=torch.int32, device="cuda")
@@ -191,3 +192,23 @@ def test_step_cap_sets_error_flag_and_matches_oracle(cuda_device):
     assert same.mean() >= DECISION_PARITY
     assert (g["log"][..., 3] == 5).any()
     assert g["errors"] & 0x1
+
+
+@pytest.mark.parametrize("kind", ["reference", "config", "config_global"])
+def test_wavefront_tracker_matches_megakernel(cuda_device, kind):
+    """The wavefront tracker (event and tracking kernels alternating over per-slot state) draws
+    every path's random numbers in the megakernel's order: identical decision logs, RNG states
+    and sums, also when segments are suspended after a few lookups per pass."""
+    if kind == "reference":
+        cfg = small_reference_mode(size=40, n=32)
+    else:
+        cfg = small_config_mode(size=40, n=40, g=0.8, majorant_mode=1 if kind == "config" else 0)
+    vox = volume_for(cfg)
+    env = constant_environment(cfg.env_constant if cfg.env_constant is not None else 0.5)
+    a = _gpu_logged(cfg, vox, env, 3, tracker=0)
+    b = _gpu_logged(cfg, vox, env, 3, tracker=1, slots_per_sm=4, pass_steps=3)
+    np.testing.assert_array_equal(a["log"], b["log"])
+    np.testing.assert_array_equal(a["rng"], b["rng"])
+    np.testing.assert_array_equal(a["sum"], b["sum"])
+    np.testing.assert_array_equal(a["mean"], b["mean"])
+    assert a["counters"] == b["counters"] and a["errors"] == b["errors"] == 0

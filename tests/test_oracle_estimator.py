@@ -75,3 +75,32 @@ def test_pure_absorber_transmittance(mode):
     expect = sensor * math.exp(-tau)
     se = math.sqrt(expect * (sensor - expect) / spp)
     assert abs(est - expect) < 4 * se + 1e-4 * expect
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_shadow_roulette_is_unbiased(mode):
+    """Russian roulette on shadow-ray visibility (configuration mode) leaves the expectation of
+    the image unchanged: the same scene with and without it, from independent streams, agrees
+    within 4 standard errors of the difference of the two means (batch means estimate them)."""
+    n = 8
+    rng0 = np.random.default_rng(3)
+    vox = (0.3 + rng0.random((n, n, n))).astype(np.float32)
+    env = np.full((16, 32, 3), 0.3, np.float32)
+    W = H = 4
+    def render(thr, seed):
+        sc = orc.make_scene(voxels=vox, voxel_size=1.0 / n, origin=[-0.5, -0.5, -0.5], density_coeff=6.0,
+                            albedo=0.9, phase_kind=1, phase_param=0.6, env_rgb=env, width=W, height=H,
+                            sun_dir=np.float32([0.3, 0.8, 0.52]) / np.linalg.norm([0.3, 0.8, 0.52]),
+                            sun_irradiance=3.0, sun_prob=0.5, max_bounces=32, rr_start=4, majorant_mode=mode,
+                            stream_mode=1, shadow_rr=thr, **CAM)
+        rng = orc.seed_states(W, H, seed)
+        means = []
+        for b in range(24):
+            res = orc.render_plain(sc, rng, 64, accum_base=64 * b)
+            means.append(res["sum"].mean() / 64)
+        return np.array(means), res
+    a, _ = render(0.0, 21)
+    b, _ = render(0.3, 22)
+    se = math.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+    assert abs(a.mean() - b.mean()) < 4 * se, (a.mean(), b.mean(), se)
+    assert se < 0.05 * a.mean()
