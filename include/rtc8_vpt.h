@@ -83,7 +83,8 @@ typedef struct VptFrameParams {
     /* Russian roulette on the transmittance of NEE shadow rays (configuration mode; 0 = off, the
      * reference's plain ratio tracking): once a shadow ray's visibility drops below this
      * threshold it survives with probability vis / threshold and continues with visibility
-     * = threshold (unbiased); the extra random number is drawn from the path's stream. */
+     * = threshold (unbiased); the extra random number is drawn from the path's stream. The
+     * radiance-cache training passes ignore it (their NEE estimates are training targets). */
     float shadow_rr_threshold;
 } VptFrameParams;
 

@@ -740,7 +740,11 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
 
         float vis;
         bool capped = false;
-        RGB nee = next_event(s, rng, pos, fr, &vis, &rec[2], lookups, &capped);
+        // Training suffixes keep plain ratio tracking (no roulette): their NEE estimates are the
+        // cache's targets.
+        OrcScene s_nee = s;
+        if (train) s_nee.shadow_rr = 0.0f;
+        RGB nee = next_event(s_nee, rng, pos, fr, &vis, &rec[2], lookups, &capped);
         if (capped) {
             end_code = ORC_END_STEP_CAP;
             break;

@@ -755,14 +755,16 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
             if (shadow) {
                 ++rec_shadow;
                 vis *= (1 - density / maj);
-                if (vis < P.shadow_rr) {
-                    // Russian roulette on the remaining visibility (configuration mode).
-                    const float q = vis / P.shadow_rr;
+                // Russian roulette on the remaining visibility (configuration mode). Training
+                // suffixes keep plain ratio tracking: their NEE estimates are the cache's targets.
+                const float rr_thr = (kMayTrain && is_train) ? 0.0f : P.shadow_rr;
+                if (vis < rr_thr) {
+                    const float q = vis / rr_thr;
                     if (rng.uniform() >= q) {
                         vis = 0.0f;
                         st = ST_NEE_DONE;
                     } else {
-                        vis = P.shadow_rr;
+                        vis = rr_thr;
                     }
                 }
             } else {
