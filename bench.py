@@ -7,10 +7,12 @@ The line also carries `nrc_vs_plain`: GPU time for the radiance-cache renderer a
 tracer to reach relMSE 1e-3 against a 16384-spp FP64 image on the 256x256 dense 64^3 scene.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2|c1|c4|c5]
-                  [--no-nrc] [--no-cpu-baseline] [--nrc-frames N]
+                  [--no-nrc] [--no-cpu-baseline] [--nrc-frames N] [--mlp] [--tracker megakernel|wavefront]
 
 `--config c4` times the 16-scene batch (one CUDA graph per step), `--config c5` the 2048^2 /
-1024^3 stress scene; `--nrc-frames N` runs only the radiance-cache frame loop (profiling).
+1024^3 stress scene; `--nrc-frames N` runs only the radiance-cache frame loop and `--mlp` only
+the cache's MLP kernels (profiling); `--tracker wavefront` times the wavefront form of the plain
+tracker instead of the persistent megakernel.
 
 `--impl reference` times the reference's per-path CPU algorithm on the host cores. The reference's
 own implementation (OptiX raygen + tiny-cuda-nn) cannot be built on this platform, so the arm runs
@@ -313,6 +315,8 @@ def main():
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
     ap.add_argument("--no-nrc", action="store_true", help="skip the NRC-vs-plain equal-error comparison")
+    ap.add_argument("--tracker", default="megakernel", choices=["megakernel", "wavefront"],
+                    help="plain tracker: the persistent megakernel (default) or the wavefront form")
     ap.add_argument("--mlp", action="store_true",
                     help="profiling run: only the cache's MLP kernels (inference and training steps)")
     ap.add_argument("--nrc-frames", type=int, default=0,
@@ -376,6 +380,7 @@ def main():
     dev = torch.device("cuda", local)
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg)
+    r.set_tracker(1 if args.tracker == "wavefront" else 0)
     info = r.volume_info()
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
