@@ -178,18 +178,19 @@ def scene_host_inputs(cfg):
 
 def mlp_bench(steps: int, warmup: int) -> dict:
     """The cache's MLP kernels alone at the sizes of a radiance-cache frame of the equal-error
-    comparison: inference over 2^21 queries (256^2 pixels x 32 samples) and training steps of 16384
-    records, volume encoding, 5 hidden layers of 64. FLOPs are those of the padded network
-    (144x64 + 4x64x64 + 64x16 multiply-adds per record forward, 3x that per training record)."""
+    comparison: inference over 256^2 pixels x spp_per_frame queries (2^22 at 64 samples per frame)
+    and training steps of 16384 records, volume encoding, 5 hidden layers of 64. FLOPs are those of
+    the padded network (144x64 + 4x64x64 + 64x16 multiply-adds per record forward, 3x that per
+    training record)."""
     import torch
 
-    from rtc8_gb300 import nrc
+    from rtc8_gb300 import convergence, nrc
 
     cfg = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
     cache = nrc.NeuralRadianceCache()
     cache.initialize(config=cfg)
     gen = torch.Generator(device="cuda").manual_seed(0)
-    n_inf, n_tr = 1 << 21, 16384
+    n_inf, n_tr = 65536 * convergence.NRC_SETTINGS["spp_per_frame"], 16384
     q = torch.rand((n_inf, 14), device="cuda", generator=gen)
     q[:, 3:7] *= 3.0
     out = torch.empty((n_inf, 3), device="cuda")
