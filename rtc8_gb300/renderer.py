@@ -131,6 +131,16 @@ class Renderer:
         check(self.lib.vpt_download_cell_majorants(self.ctx, ptr(out, C.c_float)), "vpt_download_cell_majorants")
         return out
 
+    def load_environment_exr(self, path) -> np.ndarray:
+        """Image-based environment from an OpenEXR file (the scene's `envmap`,
+        renderer/renderer_scene.cpp:1140-1165, 1765-1790): rows are the polar angle from +y.
+        Returns the RGB image that was uploaded."""
+        from . import image
+
+        rgb = np.ascontiguousarray(image.read_exr(path)[..., :3])
+        self.set_environment_rgb(rgb)
+        return rgb
+
     def set_environment_rgb(self, rgb: np.ndarray) -> None:
         img = np.ascontiguousarray(rgb, dtype=np.float32)
         h, w, _ = img.shape

@@ -68,3 +68,28 @@ def test_png_frame_of_a_render(cuda_device, tmp_path):
     r.save_exr(e)
     assert e.read_bytes() == image.encode_exr(r.download_mean())
     r.close()
+
+
+def test_environment_from_exr(cuda_device, tmp_path):
+    """An EXR environment map uploads the same texels and importance map as the float array it
+    was written from (half precision)."""
+    from ._scenes import small_config_mode
+
+    rng = np.random.default_rng(5)
+    env = (rng.random((32, 64, 3)) * 3).astype(np.float32)
+    p = image.write_exr(tmp_path / "env.exr", env, compression=image.EXR_ZIP)
+    cfg = small_config_mode(size=16, n=16)
+    a = Renderer(cfg.width, cfg.height)
+    setup_scene(a, cfg)
+    rgb = a.load_environment_exr(p)
+    np.testing.assert_array_equal(rgb, env.astype(np.float16).astype(np.float32))
+    b = Renderer(cfg.width, cfg.height)
+    setup_scene(b, cfg)
+    b.set_environment_rgb(env.astype(np.float16).astype(np.float32))
+    ma, ia = a.importance_map()
+    mb, ib = b.importance_map()
+    np.testing.assert_array_equal(ma, mb)
+    assert ia == ib
+    np.testing.assert_array_equal(a.download_environment(64, 32), b.download_environment(64, 32))
+    a.close()
+    b.close()

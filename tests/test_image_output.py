@@ -101,3 +101,50 @@ def test_exr_layout_and_values():
     expect = (2.0 * rgb)[::-1].astype(np.float16).astype(np.float32)
     np.testing.assert_array_equal(got, expect)
     assert np.all(np.array(planes["A"]) == 0)
+
+
+@pytest.mark.parametrize("compression", [image.EXR_NONE, image.EXR_RLE, image.EXR_ZIPS, image.EXR_ZIP])
+@pytest.mark.parametrize("pixel_type", [1, 2])
+def test_exr_reader_round_trip(compression, pixel_type):
+    rng = np.random.default_rng(4)
+    rgb = (rng.random((37, 29, 3)) * 8).astype(np.float32)
+    rgb[:5, :5] = 0.25  # runs for the RLE codec
+    out = image.decode_exr(image.encode_exr(rgb, compression=compression, pixel_type=pixel_type))
+    expect = rgb.astype(np.float16 if pixel_type == 1 else np.float32).astype(np.float32)
+    np.testing.assert_array_equal(out[..., :3], expect)
+    assert np.all(out[..., 3] == 0)  # the writer stores A = 0 where the image has no alpha
+
+
+def _y_only_exr(y: np.ndarray) -> bytes:
+    """A one-channel (Y, FLOAT) uncompressed scan-line file, built field by field."""
+    h, w = y.shape
+    chlist = b"Y\0" + struct.pack("<iB3xii", 2, 0, 1, 1) + b"\0"
+    header = (struct.pack("<ii", 20000630, 2) + image._attr("channels", "chlist", chlist) +
+              image._attr("compression", "compression", b"\0") +
+              image._attr("dataWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1)) +
+              image._attr("displayWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1)) +
+              image._attr("lineOrder", "lineOrder", b"\0") + b"\0")
+    first = len(header) + 8 * h
+    offs = np.arange(h, dtype="<u8") * np.uint64(8 + 4 * w) + np.uint64(first)
+    body = b"".join(struct.pack("<ii", r, 4 * w) + y[r].astype("<f4").tobytes() for r in range(h))
+    return header + offs.tobytes() + body
+
+
+def test_exr_reader_gray_and_refusals():
+    y = np.linspace(0, 2, 6 * 4, dtype=np.float32).reshape(6, 4)
+    rgba = image.decode_exr(_y_only_exr(y))
+    for k in range(3):
+        np.testing.assert_array_equal(rgba[..., k], y)
+    assert np.all(rgba[..., 3] == 1.0)  # no alpha channel: opaque
+    data = bytearray(image.encode_exr(y[..., None], pixel_type=2))
+    with pytest.raises(ValueError, match="magic"):
+        image.decode_exr(b"\x00" * 16)
+    tiled = bytearray(data)
+    tiled[4:8] = struct.pack("<i", 2 | 0x200)
+    with pytest.raises(ValueError, match="scan-line"):
+        image.decode_exr(bytes(tiled))
+    piz = bytearray(data)
+    i = piz.index(b"compression\0compression\0") + len(b"compression\0compression\0") + 4
+    piz[i] = 4  # PIZ
+    with pytest.raises(ValueError, match="compression 4"):
+        image.decode_exr(bytes(piz))
