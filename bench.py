@@ -1,4 +1,4 @@
-"""Benchmark of the GB300 volumetric path tracer (plain path, BASELINE configuration 2).
+"""Benchmark of the GB300 volumetric path tracer (plain path, 1024^2 sparse 512^3 workload).
 
 One step = one launch of the plain tracer over the whole 1024x1024 image at STEP_SPP samples
 per pixel on the sparse 512^3 fBm cloud (sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256
@@ -262,7 +262,7 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
 
 
 def batch_bench(steps: int, warmup: int, spp: int = 4) -> dict:
-    """BASELINE configuration 4: 16 seeded scenes of uneven resolution and grid size, one batch
+    """The batched workload: 16 seeded scenes of uneven resolution and grid size, one batch
     step = `spp` samples per pixel of every scene as one CUDA-graph launch, launch shapes picked by
     the autotuner; the same step issued launch by launch is timed for comparison."""
     import torch

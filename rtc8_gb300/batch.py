@@ -1,4 +1,4 @@
-"""Batched rendering of many independent scenes (BASELINE configuration 4).
+"""Batched rendering of many independent scenes (16 scenes of uneven resolution and grid size).
 
 Every scene keeps its own context (volume, environment, camera, image size, RNG streams and,
 for the radiance-cache form, its own cache). One batch step renders `spp` samples per pixel of
@@ -26,7 +26,7 @@ LAUNCH_CANDIDATES = [(0, 0), (4, 16), (5, 16), (5, 28), (4, 24)]
 
 
 def make_c4_scenes(count: int = 16, seed: int = 4) -> list[SceneConfig]:
-    """Scenes of BASELINE configuration 4: resolution from {256, 512, 768, 1024}^2, fBm grid from
+    """The batched workload's scenes: resolution from {256, 512, 768, 1024}^2, fBm grid from
     {64, 128, 256, 512}^3 (sparse above 64^3), HG g uniform in [0.3, 0.9], drawn from `seed`."""
     rng = np.random.default_rng(seed)
     out = []

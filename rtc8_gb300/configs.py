@@ -79,7 +79,7 @@ class SceneConfig:
         return self.width * self.height
 
 
-# BASELINE configuration 1: plain tracer, 256^2 x 16 spp, dense 64^3 fBm, sigma_t max 20.
+# Dense workload: plain tracer, 256^2 x 16 spp, dense 64^3 fBm, sigma_t max 20.
 C1 = SceneConfig(name="c1_dense64_256px", width=256, height=256, spp=16,
                  volume=VolumeSpec(n=64, seed=1, octaves=4, sigma_t_max=20.0),
                  albedo=0.99, phase_kind=1, phase_param=0.8, sun_elevation_deg=30.0, env_constant=0.5,
@@ -91,7 +91,7 @@ C1_REFERENCE_MODE = C1.replace(name="c1_reference_mode", phase_kind=0, phase_par
                                max_bounces=0, rr_start_vertex=1, majorant_mode=0, rng_stream_mode=0,
                                shadow_rr_threshold=0.0)
 
-# BASELINE configuration 2: 1024^2 x 64 spp, sparse 512^3 fBm (6 octaves, threshold 0.55),
+# Sparse workload at scale: 1024^2 x 64 spp, sparse 512^3 fBm (6 octaves, threshold 0.55),
 # sigma_t max 200, albedo 0.999, HG g = 0.85, <= 256 bounces, sun at 20 degrees + Hosek sky.
 C2 = SceneConfig(name="c2_sparse512_1024px", width=1024, height=1024, spp=64,
                  volume=VolumeSpec(n=512, seed=2, octaves=6, threshold=0.55, sigma_t_max=200.0),
@@ -99,7 +99,7 @@ C2 = SceneConfig(name="c2_sparse512_1024px", width=1024, height=1024, spp=64,
                  sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=256, rr_start_vertex=9,
                  majorant_cell_log2=5)
 
-# BASELINE configuration 5 (stress): 2048^2, sparse 1024^3 made of two fBm clouds unioned
+# Stress workload: 2048^2, sparse 1024^3 made of two fBm clouds unioned
 # (threshold 0.78: about 8% of the leaves hold density), sigma_t max 400, albedo 0.9995, g = 0.9,
 # <= 1024 bounces.
 C5 = SceneConfig(name="c5_sparse1024_2048px", width=2048, height=2048, spp=16,

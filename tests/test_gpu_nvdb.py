@@ -131,7 +131,7 @@ def _render_pair(cfg, buf, spp):
 @pytest.mark.parametrize("mode", ["reference", "config"])
 def test_render_through_nvdb_volume_matches_oracle(cuda_device, files, mode):
     """Reference mode (one global majorant, the reference's tracking): >= 99.9% identical path
-    decisions. Configuration mode (majorant-grid DDA, no counterpart in the reference, judged
+    decisions. Configuration mode (majorant-grid DDA, no counterpart in the reference, compared
     statistically): the fog sphere's lower y face lies on a majorant-cell boundary, so the cell
     a ray entering through it starts in is decided by the last bit of the entry point, where
     the GPU's and the host's sin/cos differ by an ulp for some scattered directions; the bar
