@@ -229,6 +229,16 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem_d, uint32_t a_addr, ui
     }
 }
 
+// As issue_layer with A read from tensor memory: a_tmem holds the 128 x K FP16 activations
+// (row = lane, K elements packed two per 32-bit column).
+__device__ __forceinline__ void issue_layer_ts(uint32_t tmem_d, uint32_t a_tmem, uint32_t w_addr, int K, int N) {
+    const uint32_t idesc = idesc_f16(kTile, N, 0, 0);
+    for (int ks = 0; ks < K / 16; ++ks) {
+        uint64_t bd = smem_desc(w_addr + ks * 256, 128, static_cast<uint32_t>(K * 16));
+        mma_f16_ts(tmem_d, a_tmem + ks * 8, bd, idesc, ks > 0 ? 1u : 0u);
+    }
+}
+
 // Writes 16 FP32 values (columns c0..c0+15 of row r) as FP16 into a [128][K] core-matrix tile.
 __device__ __forceinline__ void store_row16(uint8_t* tile, int r, int c0, int K, const float (&v)[16]) {
 #pragma unroll
@@ -281,7 +291,10 @@ __host__ __device__ __forceinline__ uint32_t align_up(uint32_t x, uint32_t a) { 
 // hidden activations (a layer's MMA has completed before its epilogue overwrites the operand).
 __host__ __device__ constexpr uint32_t infer_tile_bytes(int in_dim) { return (kTile * in_dim * 2 + 1023) / 1024 * 1024; }
 
-template <int IN, int G>
+// TA: the hidden activations stay in tensor memory (32 packed FP16 columns per group next to the
+// group's 64 accumulator columns) and feed the next layer's MMA as its A operand; only the encoded
+// input tile goes through shared memory.
+template <int IN, int G, bool TA>
 __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
                                                              const float* __restrict__ in,
                                                              const uint32_t* __restrict__ dev_n, uint32_t n_max,
@@ -298,7 +311,8 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
 
     for (uint32_t i = tid; i < ly.blob_bytes / 16; i += kTile * G)
         reinterpret_cast<uint4*>(s_w)[i] = __ldg(reinterpret_cast<const uint4*>(blob) + i);
-    if (warp == 0) tmem_alloc(s_slot, 64 * G);
+    constexpr uint32_t kCols = TA ? 128 : 64;  // TMEM columns per group
+    if (warp == 0) tmem_alloc(s_slot, kCols * G);
     if (gt == 0) {
         mbar_init(s_bar + g, 1);
         mbar_fence_init();
@@ -308,32 +322,59 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *s_slot;
-    const uint32_t tmem = tmem_base + 64 * g;                        // the group's columns
+    const uint32_t tmem = tmem_base + kCols * g;                     // the group's accumulator columns
+    const uint32_t tmem_a = tmem + 64;                               // TA: the group's activation columns
     const uint32_t lane_base = static_cast<uint32_t>((warp % 4) * 32) << 16;  // lanes = rows of the tile
     const uint32_t n = dev_n ? min(*dev_n, n_max) : n_max;
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     uint32_t phase = 0;
     bool ok = true;
     float q[14];
+    const uint32_t stride = gridDim.x * G;
     load_query(in, (blockIdx.x * G + g) * kTile + gt, n, q);
-    for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += gridDim.x * G) {
+    for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += stride) {
         const uint32_t row = tile * kTile + gt;
         encode_row(ly.enc, q, s_t, gt, IN);
-        // The next tile's queries load while this tile runs through the layers.
-        load_query(in, (tile + gridDim.x * G) * kTile + gt, n, q);
+        // The next tile's queries load while this tile runs through the layers. (Encoding it
+        // during layer 1, when the input tile is already free in the TA form, measured slower:
+        // the group's next epilogue waits for the encoder.)
+        load_query(in, (tile + stride) * kTile + gt, n, q);
         fence_async_smem();
         named_sync(bar_id, kTile);
         for (int j = 0; j < ly.L && ok; ++j) {
             if (gt == 0) {
                 tc_fence_after();
-                issue_layer(tmem, smem_u32(s_t), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
+                if (TA && j > 0)
+                    issue_layer_ts(tmem, tmem_a, smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
+                else
+                    issue_layer(tmem, smem_u32(s_t), smem_u32(s_w + ly.boff[j]), ly.in[j], ly.out[j]);
                 mma_commit(s_bar + g);
             }
+
             ok = named_sync_and(bar_id, kTile, mbar_wait(s_bar + g, phase));  // group-uniform decision
             phase ^= 1;
             tc_fence_after();
             if (!ok) break;
-            if (j < ly.L - 1) {
+            if (j < ly.L - 1 && TA) {
+                // ReLU + FP16 pack of the accumulator straight back into tensor memory.
+#pragma unroll
+                for (int c = 0; c < kWidth / 32; ++c) {
+                    float v0[16], v1[16];
+                    tmem_ld16(tmem + lane_base + c * 32, v0);
+                    tmem_ld16(tmem + lane_base + c * 32 + 16, v1);
+                    tmem_wait_ld();
+                    uint32_t w[16];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        w[i] = pack_half2_relu(v0[2 * i], v0[2 * i + 1]);
+                        w[8 + i] = pack_half2_relu(v1[2 * i], v1[2 * i + 1]);
+                    }
+                    tmem_st16(tmem_a + lane_base + c * 16, w);
+                }
+                tmem_wait_st();
+                tc_fence_before();
+                named_sync(bar_id, kTile);
+            } else if (j < ly.L - 1) {
 #pragma unroll
                 for (int c = 0; c < kWidth / 32; ++c) {  // two TMEM loads in flight per wait
                     float v0[16], v1[16];
@@ -364,7 +405,7 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem_base, 64 * G);
+    if (warp == 0) tmem_dealloc(tmem_base, kCols * G);
 }
 
 // ------------------------------------------------------------------------------ training
@@ -672,10 +713,15 @@ __global__ void selftest_kernel(const float* __restrict__ A, const float* __rest
 }
 
 // ------------------------------------------------------------------------------ host side
-uint32_t infer_smem(const NetLayout& l, int groups) {
-    return align_up(l.blob_bytes, 1024) + groups * infer_tile_bytes(l.in_dim) + groups * 8 + 16;
-}
+// Hidden activations in tensor memory (the TA form of the inference kernel).
+constexpr bool kInferTmemActivations = true;
 constexpr uint32_t kMaxSmemOptIn = 232448;  // 227 KB per CTA
+uint32_t infer_smem(const NetLayout& l, int groups) {
+    const uint32_t s = align_up(l.blob_bytes, 1024) + groups * infer_tile_bytes(l.in_dim) + groups * 8 + 16;
+    // The TA form allocates 128 TMEM columns per group, all 512 of an SM at four groups: the
+    // shared-memory request keeps a second CTA off the SM so that its allocation never waits.
+    return kInferTmemActivations ? std::max<uint32_t>(s, kMaxSmemOptIn / 2 + 1024) : s;
+}
 // Largest tile-group count (4, 2 or 1) whose shared memory fits one CTA.
 int infer_groups(const NetLayout& l) {
     for (int g = 4; g > 1; g /= 2)
@@ -685,12 +731,12 @@ int infer_groups(const NetLayout& l) {
 const void* infer_kernel_ptr(int enc, int groups) {
     const bool vol = enc == NRC_ENCODING_VOLUME;
     switch (groups) {
-    case 4: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 4>)
-                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 4>);
-    case 2: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 2>)
-                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 2>);
-    default: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 1>)
-                        : reinterpret_cast<const void*>(mlp_infer_kernel<64, 1>);
+    case 4: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 4, kInferTmemActivations>)
+                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 4, kInferTmemActivations>);
+    case 2: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 2, kInferTmemActivations>)
+                       : reinterpret_cast<const void*>(mlp_infer_kernel<64, 2, kInferTmemActivations>);
+    default: return vol ? reinterpret_cast<const void*>(mlp_infer_kernel<144, 1, kInferTmemActivations>)
+                        : reinterpret_cast<const void*>(mlp_infer_kernel<64, 1, kInferTmemActivations>);
     }
 }
 uint32_t train_smem(const NetLayout& l) {
@@ -858,19 +904,19 @@ static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_
     const dim3 block(kTile * G);
     if (G == 4) {
         if (vol)
-            mlp_infer_kernel<144, 4><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 4><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
     } else if (G == 2) {
         if (vol)
-            mlp_infer_kernel<144, 2><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 2><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
     } else {
         if (vol)
-            mlp_infer_kernel<144, 1><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 1><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
     }
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
