@@ -51,3 +51,30 @@ def test_library_built_for_sm_103a():
     from rtc8_gb300 import build
 
     assert "arch=compute_103a,code=sm_103a" in build.ARCH
+
+
+def test_cpp_shim_compiles_links_and_refuses_hashgrid(lib, tmp_path):
+    """include/rtc8_nrc.hpp: the reference's rtc8::NeuralRadianceCache interface over the C ABI
+    compiles and links as the renderer would use it; the unimplemented HashGrid encoding throws
+    (no device work, so this runs without a GPU)."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "shim.cpp"
+    src.write_text(
+        '#include "rtc8_nrc.hpp"\n#include <cstdio>\n'
+        "int main() {\n  rtc8::NeuralRadianceCache cache;\n"
+        "  try { cache.initialize(rtc8::PositionEncoding::HashGrid, 2, 1e-2f); }\n"
+        '  catch (const std::exception& e) { std::puts(e.what()); return 0; }\n  return 1;\n}\n')
+    from rtc8_gb300 import build
+
+    libdir = build.LIB.parent
+    exe = tmp_path / "shim"
+    cuda_inc = Path(build.nvcc()).resolve().parent.parent / "include"
+    subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(cuda_inc), str(src), "-L", str(libdir),
+                    "-lrtc8_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    assert "HashGrid encoding is not implemented" in out

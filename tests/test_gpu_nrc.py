@@ -5,11 +5,15 @@ with the same FP16 rounding points (oracle): outputs within 2e-2 relative, gradi
 within 3e-2 relative L2 error (cosine > 0.999), loss within 1e-3 relative, Adam updates within
 1e-5 relative.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
 from oracle import orc
 from rtc8_gb300 import nrc
+
+ROOT = Path(__file__).resolve().parents[1]
 
 pytestmark = pytest.mark.gpu
 
@@ -148,4 +152,78 @@ def test_training_reduces_loss(cuda_device):
             losses.append(l)
     assert losses[-1] < 0.2 * losses[0], losses
     assert cache.device_errors() == 0
+    cache.finalize()
+
+
+def test_cpp_shim_matches_python_binding(cuda_device, tmp_path):
+    """The reference's C++ interface (include/rtc8_nrc.hpp, rtc8::NeuralRadianceCache) used as the
+    renderer uses it: initialize(TriangleWave, 2, 1e-2), one train step with the loss read back,
+    then inference, against the same calls through the Python binding (same default seed, so the
+    same initial weights; weight gradients are reduced with atomics, hence the tolerance)."""
+    import shutil
+    import subprocess
+
+    import torch
+
+    from rtc8_gb300 import build
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    n = 512
+    q = _queries(n, 7, volume=False)
+    tgt = np.abs(np.random.default_rng(8).standard_normal((n, 3))).astype(np.float32)
+    (tmp_path / "in.bin").write_bytes(q.astype(np.float32).tobytes() + tgt.tobytes())
+    src = tmp_path / "shim.cpp"
+    src.write_text(r'''
+#include "rtc8_nrc.hpp"
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <vector>
+int main(int argc, char** argv) {
+    const unsigned n = 512;
+    std::vector<float> h(n * 17), out(n * 3);
+    FILE* f = std::fopen(argv[1], "rb");
+    if (!f || std::fread(h.data(), sizeof(float), h.size(), f) != h.size()) return 2;
+    std::fclose(f);
+    float *d_in = nullptr, *d_tgt = nullptr, *d_out = nullptr;
+    cudaMalloc(&d_in, n * 14 * sizeof(float));
+    cudaMalloc(&d_tgt, n * 3 * sizeof(float));
+    cudaMalloc(&d_out, n * 3 * sizeof(float));
+    cudaMemcpy(d_in, h.data(), n * 14 * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_tgt, h.data() + n * 14, n * 3 * sizeof(float), cudaMemcpyHostToDevice);
+    rtc8::NeuralRadianceCache cache;
+    cache.initialize(rtc8::PositionEncoding::TriangleWave, 2, 1e-2f);
+    float loss = 0.0f;
+    cache.train(nullptr, d_in, d_tgt, n, &loss);
+    cache.infer(nullptr, d_in, n, d_out);
+    cudaMemcpy(out.data(), d_out, n * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    f = std::fopen(argv[2], "wb");
+    std::fwrite(&loss, sizeof(float), 1, f);
+    std::fwrite(out.data(), sizeof(float), out.size(), f);
+    std::fclose(f);
+    cache.finalize();
+    cudaFree(d_in); cudaFree(d_tgt); cudaFree(d_out);
+    return 0;
+}
+''')
+    libdir = build.LIB.parent
+    cuda = Path(build.nvcc()).resolve().parent.parent
+    exe = tmp_path / "shim"
+    subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(src),
+                    "-L", str(libdir), "-lrtc8_gb300", "-L", str(cuda / "lib64"), "-lcudart",
+                    f"-Wl,-rpath,{libdir}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)], check=True)
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    res = np.frombuffer((tmp_path / "out.bin").read_bytes(), dtype=np.float32)
+    loss_cpp, out_cpp = res[0], res[1:].reshape(n, 3)
+
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(nrc.PositionEncoding.TriangleWave, 2, 1e-2)
+    tq, tt = torch.from_numpy(q).cuda(), torch.from_numpy(tgt).cuda()
+    loss_py = cache.train(None, tq, tt, n, loss=True)
+    out = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    cache.infer(None, tq, n, out)
+    torch.cuda.synchronize()
+    assert loss_cpp == pytest.approx(loss_py, rel=1e-5)
+    np.testing.assert_allclose(out_cpp, out.cpu().numpy(), rtol=1e-4, atol=1e-5)
     cache.finalize()
