@@ -62,11 +62,14 @@ const char* vpt_last_error(void) { return g_last_error.c_str(); }
 
 int vpt_create(int32_t w, int32_t h, VptContext** out) {
     if (!out || w <= 0 || h <= 0) return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_create: bad arguments");
+    int device = 0, num_sms = 0;
+    VPT_CUDA(cudaGetDevice(&device));
+    VPT_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
     auto* c = new VptContext();
     c->width = w;
     c->height = h;
-    VPT_CUDA(cudaGetDevice(&c->device));
-    VPT_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    c->device = device;
+    c->num_sms = num_sms;
     int64_t npix = static_cast<int64_t>(w) * h;
     int rc;
     if ((rc = dev_alloc(&c->d_rng, npix)) || (rc = dev_alloc(&c->d_sum, 3 * npix)) ||

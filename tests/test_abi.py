@@ -78,3 +78,42 @@ def test_cpp_shim_compiles_links_and_refuses_hashgrid(lib, tmp_path):
                     "-lrtc8_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     assert "HashGrid encoding is not implemented" in out
+
+
+def test_cpp_renderer_header_compiles_and_orients_like_python(lib, tmp_path):
+    """include/rtc8_vpt.hpp: rtc8::VolumeRenderer and look_at_quaternion compile and link; the
+    camera quaternion equals the Python camera's (float32 rounding) for looks along the axes and
+    the diagonals, and a bad image size throws with the library's message (no device work)."""
+    import shutil
+    import subprocess
+
+    import numpy as np
+
+    from rtc8_gb300 import build
+    from rtc8_gb300.configs import look_at
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    eyes = [(0.0, 0.0, 3.0), (3.0, 0.0, 0.0), (0.0, 0.0, -3.0), (-2.0, 0.5, 0.1), (1.7, 1.1, -2.3),
+            (-1.0, -2.0, -1.5), (0.3, 0.2, 4.0)]
+    src = tmp_path / "vpt_shim.cpp"
+    calls = "\n".join(
+        f"  rtc8::look_at_quaternion({{{e[0]!r}, {e[1]!r}, {e[2]!r}}}, {{0.0, 0.0, 0.0}}, {{0.0, 1.0, 0.0}}, q);\n"
+        '  std::printf("%.9g %.9g %.9g %.9g\\n", q[0], q[1], q[2], q[3]);' for e in eyes)
+    src.write_text(
+        '#include "rtc8_vpt.hpp"\n#include <cstdio>\n'
+        "int main() {\n  float q[4];\n" + calls + "\n"
+        "  try { rtc8::VolumeRenderer r(0, 16); }\n"
+        '  catch (const std::exception& e) { std::printf("%s\\n", e.what()); return 0; }\n  return 1;\n}\n')
+    libdir = build.LIB.parent
+    exe = tmp_path / "vpt_shim"
+    cuda_inc = Path(build.nvcc()).resolve().parent.parent / "include"
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I", str(cuda_inc), str(src),
+                    "-L", str(libdir), "-lrtc8_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    lines = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines()
+    for e, line in zip(eyes, lines):
+        q = np.array([float(v) for v in line.split()])
+        want = look_at(e, (0.0, 0.0, 0.0)).astype(np.float32)
+        np.testing.assert_allclose(q, want, atol=1.5e-7)
+    assert "vpt_create" in lines[len(eyes)] and "bad arguments" in lines[len(eyes)]
