@@ -184,52 +184,85 @@ struct LeafCache {
 // util/SampleFromVoxels.h:419-459: first-order sampler, lerps along z, then y, then x.
 // When the 2x2x2 stencil lies inside one leaf (about 2/3 of the lookups) it reads one
 // table entry (or the lane's cached one) and eight values of that leaf.
-__device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz, LeafCache& cache) {
-    float fi = floorf(xyz.x), fj = floorf(xyz.y), fk = floorf(xyz.z);
-    float wx = xyz.x - fi, wy = xyz.y - fj, wz = xyz.z - fk;
-    int i = static_cast<int>(fi), j = static_cast<int>(fj), k = static_cast<int>(fk);
-    float v000, v001, v010, v011, v100, v101, v110, v111;
-    bool inside = static_cast<uint32_t>(i) < static_cast<uint32_t>(g.nx - 1) &&
-                  static_cast<uint32_t>(j) < static_cast<uint32_t>(g.ny - 1) &&
-                  static_cast<uint32_t>(k) < static_cast<uint32_t>(g.nz - 1);
-    if (inside && (i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7) {
-        int32_t key = ((i >> 3) * g.ly + (j >> 3)) * g.lz + (k >> 3);
-        int32_t slot;
-        if (key == cache.key) {
-            slot = cache.slot;
-        } else {
-            slot = __ldg(g.leaf_table + key);
-            cache.key = key;
-            cache.slot = slot;
-        }
-        if (slot < 0) return 0.0f;
-        const float* p = g.leaf_values + static_cast<int64_t>(slot) * 512 + (((i & 7) << 6) | ((j & 7) << 3) | (k & 7));
-        v000 = __ldg(p);
-        v001 = __ldg(p + 1);
-        v010 = __ldg(p + 8);
-        v011 = __ldg(p + 9);
-        v100 = __ldg(p + 64);
-        v101 = __ldg(p + 65);
-        v110 = __ldg(p + 72);
-        v111 = __ldg(p + 73);
-    } else {
-        v000 = grid_value(g, i, j, k);
-        v001 = grid_value(g, i, j, k + 1);
-        v010 = grid_value(g, i, j + 1, k);
-        v011 = grid_value(g, i, j + 1, k + 1);
-        v100 = grid_value(g, i + 1, j, k);
-        v101 = grid_value(g, i + 1, j, k + 1);
-        v110 = grid_value(g, i + 1, j + 1, k);
-        v111 = grid_value(g, i + 1, j + 1, k + 1);
-    }
+struct Stencil {
+    float wx, wy, wz;
+    int i, j, k;
+    bool fast;    // inside the grid and inside one leaf
+    int32_t key;  // that leaf's table index
+};
+
+__device__ __forceinline__ Stencil stencil_at(const Grid& g, V3 xyz) {
+    Stencil s;
+    const float fi = floorf(xyz.x), fj = floorf(xyz.y), fk = floorf(xyz.z);
+    s.wx = xyz.x - fi;
+    s.wy = xyz.y - fj;
+    s.wz = xyz.z - fk;
+    s.i = static_cast<int>(fi);
+    s.j = static_cast<int>(fj);
+    s.k = static_cast<int>(fk);
+    const bool inside = static_cast<uint32_t>(s.i) < static_cast<uint32_t>(g.nx - 1) &&
+                        static_cast<uint32_t>(s.j) < static_cast<uint32_t>(g.ny - 1) &&
+                        static_cast<uint32_t>(s.k) < static_cast<uint32_t>(g.nz - 1);
+    s.fast = inside && (s.i & 7) != 7 && (s.j & 7) != 7 && (s.k & 7) != 7;
+    s.key = ((s.i >> 3) * g.ly + (s.j >> 3)) * g.lz + (s.k >> 3);
+    return s;
+}
+
+// Table entry of a fast stencil's leaf through the lane's one-entry cache.
+__device__ __forceinline__ int32_t stencil_slot(const Grid& g, const Stencil& s, LeafCache& cache) {
+    if (s.key == cache.key) return cache.slot;
+    const int32_t slot = __ldg(g.leaf_table + s.key);
+    cache.key = s.key;
+    cache.slot = slot;
+    return slot;
+}
+
+// v = v000, v001, v010, v011, v100, v101, v110, v111 (x, y, z bits).
+__device__ __forceinline__ void stencil_load_fast(const Grid& g, const Stencil& s, int32_t slot, float (&v)[8]) {
+    const float* p = g.leaf_values + static_cast<int64_t>(slot) * 512 + (((s.i & 7) << 6) | ((s.j & 7) << 3) | (s.k & 7));
+    v[0] = __ldg(p);
+    v[1] = __ldg(p + 1);
+    v[2] = __ldg(p + 8);
+    v[3] = __ldg(p + 9);
+    v[4] = __ldg(p + 64);
+    v[5] = __ldg(p + 65);
+    v[6] = __ldg(p + 72);
+    v[7] = __ldg(p + 73);
+}
+
+__device__ __forceinline__ void stencil_load_slow(const Grid& g, const Stencil& s, float (&v)[8]) {
+    v[0] = grid_value(g, s.i, s.j, s.k);
+    v[1] = grid_value(g, s.i, s.j, s.k + 1);
+    v[2] = grid_value(g, s.i, s.j + 1, s.k);
+    v[3] = grid_value(g, s.i, s.j + 1, s.k + 1);
+    v[4] = grid_value(g, s.i + 1, s.j, s.k);
+    v[5] = grid_value(g, s.i + 1, s.j, s.k + 1);
+    v[6] = grid_value(g, s.i + 1, s.j + 1, s.k);
+    v[7] = grid_value(g, s.i + 1, s.j + 1, s.k + 1);
+}
+
+__device__ __forceinline__ float stencil_lerp(const Stencil& s, const float (&v)[8]) {
     auto lerp = [](float a, float b, float w) { return a + w * (b - a); };
-    float vy = lerp(v000, v001, wz);
-    float vy1 = lerp(v010, v011, wz);
-    float vx = lerp(vy, vy1, wy);
-    vy1 = lerp(v110, v111, wz);
-    vy = lerp(v100, v101, wz);
-    float vx1 = lerp(vy, vy1, wy);
-    return lerp(vx, vx1, wx);
+    float vy = lerp(v[0], v[1], s.wz);
+    float vy1 = lerp(v[2], v[3], s.wz);
+    const float vx = lerp(vy, vy1, s.wy);
+    vy1 = lerp(v[6], v[7], s.wz);
+    vy = lerp(v[4], v[5], s.wz);
+    const float vx1 = lerp(vy, vy1, s.wy);
+    return lerp(vx, vx1, s.wx);
+}
+
+__device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz, LeafCache& cache) {
+    const Stencil s = stencil_at(g, xyz);
+    float v[8];
+    if (s.fast) {
+        const int32_t slot = stencil_slot(g, s, cache);
+        if (slot < 0) return 0.0f;
+        stencil_load_fast(g, s, slot, v);
+    } else {
+        stencil_load_slow(g, s, v);
+    }
+    return stencil_lerp(s, v);
 }
 
 // util/Ray.h:343-363 + :512-520 (slab test, clipped to the ray's [tmin, tmax]).

@@ -89,6 +89,56 @@ __device__ __forceinline__ float cell_maj(const float* maj, const Grid& g, const
     return maj[(d.cell[0] * g.my + d.cell[1]) * g.mz + d.cell[2]];
 }
 
+enum : int { PASS_LOOKUP = 0, PASS_YIELD = 1, PASS_END = 2 };
+
+// One tracking pass of a segment from (t, texit, maj, dda): a free-flight distance
+// (optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378), with the majorant
+// grid sampled within the current cell, where an overshoot of the cell's exit restarts at the
+// exit (memoryless) and empty cells are crossed without draws, at most kCellStepsPerPass
+// crossings per pass. PASS_LOOKUP leaves t at the tentative collision; PASS_END means the segment
+// is over (also on a NaN distance); PASS_YIELD means the pass crossed its cells without one.
+template <bool kGridMajorant>
+__device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, float density_coeff, float t1, Pcg32& rng,
+                                          float& t, float& texit, float& maj, DdaState& dda,
+                                          unsigned long long& n_cells) {
+    if constexpr (!kGridMajorant) {
+        t += -logf(1.0f - rng.uniform()) / maj;
+        return (t <= t1) ? PASS_LOOKUP : PASS_END;
+    } else {
+        for (int c = 0; c < kCellStepsPerPass; ++c) {
+            if (maj > 0) {
+                const float tt = t + -logf(1.0f - rng.uniform()) / maj;
+                if (tt < texit) {
+                    t = tt;
+                    return PASS_LOOKUP;
+                }
+            }
+            t = texit;
+            if (texit >= t1) return PASS_END;
+            // Advance along the axis whose boundary comes first (x, then y, then z on ties);
+            // written with selects so the DDA state stays in registers.
+            const bool ax0 = dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2];
+            const bool ax1 = !ax0 && dda.tnext[1] <= dda.tnext[2];
+            const bool ax2 = !ax0 && !ax1;
+            if (ax0) dda.cell[0] += dda.step[0];
+            if (ax1) dda.cell[1] += dda.step[1];
+            if (ax2) dda.cell[2] += dda.step[2];
+            ++n_cells;
+            if (dda.cell[0] < 0 || dda.cell[0] >= g.mx || dda.cell[1] < 0 || dda.cell[1] >= g.my || dda.cell[2] < 0 ||
+                dda.cell[2] >= g.mz) {
+                t = t1;
+                return PASS_END;
+            }
+            if (ax0) dda.tnext[0] += dda.tdelta[0];
+            if (ax1) dda.tnext[1] += dda.tdelta[1];
+            if (ax2) dda.tnext[2] += dda.tdelta[2];
+            texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+            maj = density_coeff * cell_maj(maj_grid, g, dda);
+        }
+        return PASS_YIELD;
+    }
+}
+
 // createRadianceQuery (optix_pathtracing_kernels.cu:14-29) for an in-medium vertex: position in
 // the world box (basic_types.h:2835-2838), normal = vOut as toPolarYUp outputs (the first slot
 // holds acos(y), the second the azimuth), roughness, diffuse = albedo, specular = 0.
@@ -375,59 +425,14 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 break;
             }
             case ST_STEP: {
-                if constexpr (!kGridMajorant) {
-                    // optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378.
-                    t += -logf(1.0f - rng.uniform()) / maj;
-                    if (!(t <= t1)) {  // also ends the segment on a NaN distance
-                        st = shadow ? ST_NEE_DONE : ST_ESCAPE;
-                    } else {
-                        lookup_pos = seg_eye + seg_dir * t;
-                        need_lookup = true;
-                    }
+                const int r = track_pass<kGridMajorant>(g, maj_grid, P.density_coeff, t1, rng, t, texit, maj, dda, n_cells);
+                if (r == PASS_LOOKUP) {
+                    lookup_pos = seg_eye + seg_dir * t;
+                    need_lookup = true;
+                } else if (r == PASS_END) {
+                    st = shadow ? ST_NEE_DONE : ST_ESCAPE;
                 } else {
-                    // Majorant-grid DDA: sample within the current cell; overshooting its exit
-                    // restarts at the exit (memoryless); empty cells are skipped without draws.
-                    bool seg_end = false;
-                    for (int c = 0; c < kCellStepsPerPass; ++c) {
-                        if (maj > 0) {
-                            float tt = t + -logf(1.0f - rng.uniform()) / maj;
-                            if (tt < texit) {
-                                t = tt;
-                                lookup_pos = seg_eye + seg_dir * t;
-                                need_lookup = true;
-                                break;
-                            }
-                        }
-                        t = texit;
-                        if (texit >= t1) {
-                            seg_end = true;
-                            break;
-                        }
-                        // Advance along the axis whose boundary comes first (x, then y, then z on
-                        // ties); written with selects so the DDA state stays in registers.
-                        bool ax0 = dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2];
-                        bool ax1 = !ax0 && dda.tnext[1] <= dda.tnext[2];
-                        bool ax2 = !ax0 && !ax1;
-                        if (ax0) dda.cell[0] += dda.step[0];
-                        if (ax1) dda.cell[1] += dda.step[1];
-                        if (ax2) dda.cell[2] += dda.step[2];
-                        ++n_cells;
-                        if (dda.cell[0] < 0 || dda.cell[0] >= g.mx || dda.cell[1] < 0 || dda.cell[1] >= g.my ||
-                            dda.cell[2] < 0 || dda.cell[2] >= g.mz) {
-                            t = t1;
-                            seg_end = true;
-                            break;
-                        }
-                        if (ax0) dda.tnext[0] += dda.tdelta[0];
-                        if (ax1) dda.tnext[1] += dda.tdelta[1];
-                        if (ax2) dda.tnext[2] += dda.tdelta[2];
-                        texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
-                        maj = P.density_coeff * cell_maj(maj_grid, g, dda);
-                    }
-                    if (seg_end)
-                        st = shadow ? ST_NEE_DONE : ST_ESCAPE;
-                    else if (!need_lookup)
-                        yield = true;  // let the warp's lookups run before crossing more cells
+                    yield = true;  // let the warp's lookups run before crossing more cells
                 }
                 break;
             }
@@ -749,12 +754,13 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
         float density = 0.0f;
         if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos), leaf_cache);
 
-        if (need_lookup) {
+        // Outcome of one lookup at the lane's current tentative collision (majorant `maj`).
+        auto resolve = [&](float dens) {
             ++n_lookups;
             ++seg_steps;
             if (shadow) {
                 ++rec_shadow;
-                vis *= (1 - density / maj);
+                vis *= (1 - dens / maj);
                 // Russian roulette on the remaining visibility (configuration mode). Training
                 // suffixes keep plain ratio tracking: their NEE estimates are the cache's targets.
                 const float rr_thr = (kMayTrain && is_train) ? 0.0f : P.shadow_rr;
@@ -769,9 +775,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 }
             } else {
                 ++rec_primary;
-                if (rng.uniform() < density / maj) {
+                if (rng.uniform() < dens / maj) {
                     st = ST_VERTEX;
-                    last_density = density;
+                    last_density = dens;
                 }
             }
             if (st == ST_STEP && seg_steps >= step_cap) {
@@ -779,7 +785,8 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 end_code = END_STEP_CAP;
                 st = ST_END_SAMPLE;
             }
-        }
+        };
+        if (need_lookup) resolve(density);
     }
 
     // warp-reduce the work counters
