@@ -43,8 +43,9 @@ enum : uint32_t {
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
-// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp.
-constexpr int kCellStepsPerPass = 1;
+// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp
+// (1 -> 4 raised the 1024x1024 sparse workload by 12%; 6 to 64 measured within 2% of 4).
+constexpr int kCellStepsPerPass = 4;
 // Parked lanes of a warp that trigger a joint event phase.
 constexpr int kParkThreshold = 24;
 
@@ -202,6 +203,11 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
     const int park_threshold = P.park_threshold > 0 ? P.park_threshold : kParkThreshold;
     const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
     const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
+    // Camera constants of the launch (optix_pathtracing_kernels.cu:43-55).
+    const float cam_vh = 2 * tanf(P.cam_fovy * 0.5f);
+    const float cam_vw = P.cam_aspect * cam_vh;
+    const float sensor_area = cam_vw * cam_vh;
+    const M3 cam_rot = quat_to_m3(P.cam_quat[0], P.cam_quat[1], P.cam_quat[2], P.cam_quat[3]);
 
     uint32_t st = ST_FETCH;
     uint32_t pixel = 0, sample = 0;
@@ -377,12 +383,9 @@ __global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P
                 sqrt_spread = 0.0f;
                 prev_vertex = kInvalidVertex;
                 terminal_written = false;
-                float vh = 2 * tanf(P.cam_fovy * 0.5f);
-                float vw = P.cam_aspect * vh;
-                float sensor_area = vw * vh;
                 origin = v3(P.cam_pos[0], P.cam_pos[1], P.cam_pos[2]);
-                V3 local = normalize(v3(vw * (-0.5f + fx), vh * (0.5f - fy), -1));
-                dir = normalize(mul(quat_to_m3(P.cam_quat[0], P.cam_quat[1], P.cam_quat[2], P.cam_quat[3]), local));
+                V3 local = normalize(v3(cam_vw * (-0.5f + fx), cam_vh * (0.5f - fy), -1));
+                dir = normalize(mul(cam_rot, local));
                 float az = fabsf(local.z);
                 dir_pdf = 1 / (az * az * az * sensor_area);
                 float inv = 1.0f / dir_pdf;
