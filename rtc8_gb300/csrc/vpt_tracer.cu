@@ -48,6 +48,11 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 constexpr int kCellStepsPerPass = 4;
 // Parked lanes of a warp that trigger a joint event phase.
 constexpr int kParkThreshold = 24;
+// Resident CTAs of 128 threads per SM the register allocation is bounded for: the plain tracer
+// is fastest at 5 (96 registers, 6 and 7 measured 7% and 3% slower with spills); the radiance-
+// cache passes gain from more resident warps despite spills.
+constexpr int kPlainCtasPerSm = 5;
+constexpr int kNrcCtasPerSm = 7;
 
 struct DdaState {
     int cell[3];
@@ -185,7 +190,7 @@ __device__ __forceinline__ void train_item_to_pixel(uint32_t item, uint32_t w, u
 // kMode: kModePlain (pathTrace), kModeRenderNrc (pathTraceWithNRC) or kModeTrainNrc
 // (generateTrainingData), optix_pathtracing_kernels.cu:438-448.
 template <bool kGridMajorant, bool kLog, int kMode>
-__global__ void __launch_bounds__(128, 5) plain_trace_kernel(const TraceParams P) {
+__global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : kNrcCtasPerSm) plain_trace_kernel(const TraceParams P) {
     extern __shared__ float s_maj[];
     const Grid& g = P.grid;
     const float* maj_grid = g.maj;
