@@ -583,7 +583,7 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         rc3 = vpt::wf_run(c, tp, grid_maj, smem, s);
         if (rc3) return rc3;
     } else {
-        int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr), smem);
+        int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr, tp.stream_mode == 1), smem);
         vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
     }
     if (tp.stream_mode == 1)

@@ -117,7 +117,7 @@ int nrc_reseed_train_rng(VptContextImpl* c);
 int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
-const void* plain_kernel_ptr(bool grid_majorant, bool logged);
+const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel);
 // Wavefront plain tracer: runs the passes of one launch on `s` (vpt_wavefront.cu).
 int wf_run(VptContextImpl* c, const TraceParams& tp, bool grid_majorant, size_t smem, cudaStream_t s);
 int wf_ensure(VptContextImpl* c, uint32_t slots);

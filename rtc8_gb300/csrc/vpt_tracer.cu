@@ -48,10 +48,13 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 constexpr int kCellStepsPerPass = 4;
 // Parked lanes of a warp that trigger a joint event phase.
 constexpr int kParkThreshold = 24;
-// Resident CTAs of 128 threads per SM the register allocation is bounded for: the plain tracer
-// is fastest at 5 (96 registers, 6 and 7 measured 7% and 3% slower with spills); the radiance-
-// cache passes gain from more resident warps despite spills.
-constexpr int kPlainCtasPerSm = 5;
+// Resident CTAs of 128 threads per SM the register allocation is bounded for. The plain tracer
+// on sample-parallel streams holds its state in 72 registers at 7 CTAs/SM (1024^2 sparse 512^3:
+// 261 / 284 / 295 / 283 M paths/s at 5 / 6 / 7 / 8); per-pixel streams (and the logged parity
+// kernels) carry per-lane FP64 sums and stay at 5, where they need no spills; the radiance-cache
+// passes measured best at 7 (8 equal).
+constexpr int kPlainCtasPerSm = 7;
+constexpr int kPlainPerPixelCtasPerSm = 5;
 constexpr int kNrcCtasPerSm = 7;
 
 struct DdaState {
@@ -103,10 +106,14 @@ enum : int { PASS_LOOKUP = 0, PASS_YIELD = 1, PASS_END = 2 };
 // exit (memoryless) and empty cells are crossed without draws, at most kCellStepsPerPass
 // crossings per pass. PASS_LOOKUP leaves t at the tentative collision; PASS_END means the segment
 // is over (also on a NaN distance); PASS_YIELD means the pass crossed its cells without one.
+// The sign of a direction component: the DDA step along that axis (dda_init derives it from the
+// same sign, the index-space direction being the world direction times a positive scale).
+__device__ __forceinline__ int step_of(float d) { return d > 0 ? 1 : (d < 0 ? -1 : 0); }
+
 template <bool kGridMajorant>
-__device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, float density_coeff, float t1, Pcg32& rng,
-                                          float& t, float& texit, float& maj, DdaState& dda,
-                                          unsigned long long& n_cells) {
+__device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, float density_coeff, float t1, V3 dir,
+                                          Pcg32& rng, float& t, float& texit, float& maj, DdaState& dda,
+                                          uint32_t& n_cells) {
     if constexpr (!kGridMajorant) {
         t += -logf(1.0f - rng.uniform()) / maj;
         return (t <= t1) ? PASS_LOOKUP : PASS_END;
@@ -126,9 +133,9 @@ __device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, 
             const bool ax0 = dda.tnext[0] <= dda.tnext[1] && dda.tnext[0] <= dda.tnext[2];
             const bool ax1 = !ax0 && dda.tnext[1] <= dda.tnext[2];
             const bool ax2 = !ax0 && !ax1;
-            if (ax0) dda.cell[0] += dda.step[0];
-            if (ax1) dda.cell[1] += dda.step[1];
-            if (ax2) dda.cell[2] += dda.step[2];
+            if (ax0) dda.cell[0] += step_of(dir.x);
+            if (ax1) dda.cell[1] += step_of(dir.y);
+            if (ax2) dda.cell[2] += step_of(dir.z);
             ++n_cells;
             if (dda.cell[0] < 0 || dda.cell[0] >= g.mx || dda.cell[1] < 0 || dda.cell[1] >= g.my || dda.cell[2] < 0 ||
                 dda.cell[2] >= g.mz) {
@@ -189,8 +196,18 @@ __device__ __forceinline__ void train_item_to_pixel(uint32_t item, uint32_t w, u
 
 // kMode: kModePlain (pathTrace), kModeRenderNrc (pathTraceWithNRC) or kModeTrainNrc
 // (generateTrainingData), optix_pathtracing_kernels.cu:438-448.
-template <bool kGridMajorant, bool kLog, int kMode>
-__global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : kNrcCtasPerSm) plain_trace_kernel(const TraceParams P) {
+// kStreams: the RNG stream layout the kernel is compiled for (kStreamsPerPixel,
+// kStreamsSampleParallel), or kStreamsRuntime to follow TraceParams::stream_mode. A fixed layout
+// drops the other layout's state (the per-lane FP64 sums and running mean of per-pixel streams)
+// from the register allocation.
+constexpr int kStreamsPerPixel = 0, kStreamsSampleParallel = 1, kStreamsRuntime = 2;
+
+template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime>
+__global__ void __launch_bounds__(128, kMode != kModePlain                    ? kNrcCtasPerSm
+                                       : kStreams == kStreamsSampleParallel ? kPlainCtasPerSm
+                                                                            : kPlainPerPixelCtasPerSm)
+    plain_trace_kernel(const TraceParams P) {
+    const bool sample_parallel = kStreams == kStreamsRuntime ? P.stream_mode == 1 : kStreams == kStreamsSampleParallel;
     extern __shared__ float s_maj[];
     const Grid& g = P.grid;
     const float* maj_grid = g.maj;
@@ -229,7 +246,10 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
 
     // current segment
     bool shadow = false;
-    V3 seg_eye = v3(0, 0, 0), seg_dir = v3(0, 0, 1);
+    // The segment's eye and direction are not stored: a primary segment starts at the path's
+    // origin along its direction, a shadow segment at origin + trace_len * light_dir towards
+    // -light_dir (both unchanged while the segment is tracked).
+    const float trace_len = 2 * P.world_radius;
     float t = 0, t1 = 0, maj = global_maj, texit = 0;
     uint32_t seg_steps = 0;
     DdaState dda;
@@ -240,7 +260,9 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
     float area_pdf = 1.0f, vis = 1.0f;
     bool pick_sun = false;
 
-    unsigned long long n_lookups = 0, n_vertices = 0, n_samples = 0, n_cells = 0;
+    // Per-lane work counters (32-bit: a lane does far fewer than 2^32 steps in a launch), summed
+    // over the warp in 64 bits at the end.
+    uint32_t n_lookups = 0, n_vertices = 0, n_samples = 0, n_cells = 0;
     unsigned int err = 0;
     LeafCache leaf_cache;
 
@@ -266,7 +288,7 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
     } else if constexpr (kNrc) {
         // Sample-parallel streams: P.spp samples per pixel in one render pass, each its own
         // work item and record slot (sample-major: slot = sample * num_pixels + pixel).
-        if (P.stream_mode == 1) num_items = num_pixels * P.spp;
+        if (sample_parallel) num_items = num_pixels * P.spp;
         if constexpr (kCombo) num_items += num_train;
     }
     uint64_t* rng_buf = P.rng;  // per-pixel states the current sample continues (and writes back)
@@ -333,7 +355,7 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                     img_h = static_cast<uint32_t>(P.height);
                     slot = r;
                     rng_buf = P.rng;
-                    if (P.stream_mode == 1) {
+                    if (sample_parallel) {
                         pixel = r % num_pixels;
                         sample = r / num_pixels;
                         const ulonglong2 jump = P.sample_jumps[sample];
@@ -346,7 +368,7 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                     st = ST_CAMERA;
                     break;
                 }
-                if (P.stream_mode == 1) {
+                if (sample_parallel) {
                     // One (pixel, sample) per work item, samples of all pixels interleaved.
                     if (item >= num_pixels * P.spp) {
                         st = ST_DONE;
@@ -414,13 +436,11 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                 float a, b;
                 if (clip_ray(bmin, bmax, origin, dir, 0.0f, 1e10f, &a, &b)) {
                     shadow = false;
-                    seg_eye = origin;
-                    seg_dir = dir;
                     t = fmaxf(0.0f, a);
                     t1 = b;
                     seg_steps = 0;
                     if constexpr (kGridMajorant) {
-                        dda_init(g, seg_eye, seg_dir, t, &dda);
+                        dda_init(g, origin, dir, t, &dda);
                         texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
                         maj = P.density_coeff * cell_maj(maj_grid, g, dda);
                     } else {
@@ -433,8 +453,11 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                 break;
             }
             case ST_STEP: {
-                const int r = track_pass<kGridMajorant>(g, maj_grid, P.density_coeff, t1, rng, t, texit, maj, dda, n_cells);
+                const V3 seg_dir = shadow ? -light_dir : dir;
+                const int r = track_pass<kGridMajorant>(g, maj_grid, P.density_coeff, t1, seg_dir, rng, t, texit, maj,
+                                                        dda, n_cells);
                 if (r == PASS_LOOKUP) {
+                    const V3 seg_eye = shadow ? origin + trace_len * light_dir : origin;
                     lookup_pos = seg_eye + seg_dir * t;
                     need_lookup = true;
                 } else if (r == PASS_END) {
@@ -576,9 +599,8 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                     break;
                 }
                 vis = 1.0f;
-                float trace_len = 2 * P.world_radius;
-                seg_dir = -light_dir;
-                seg_eye = origin + trace_len * -seg_dir;
+                const V3 seg_dir = -light_dir;
+                const V3 seg_eye = origin + trace_len * light_dir;
                 float a, b;
                 if (clip_ray(bmin, bmax, seg_eye, seg_dir, 0.0f, trace_len, &a, &b)) {
                     shadow = true;
@@ -705,7 +727,7 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                         fc[1] = c.g;
                         fc[2] = c.b;
                     }
-                    if ((kMayTrain && is_train) || P.stream_mode != 1) rng_buf[rng_index] = rng.state;
+                    if ((kMayTrain && is_train) || !sample_parallel) rng_buf[rng_index] = rng.state;
                     st = ST_FETCH;
                     break;
                 }
@@ -713,7 +735,7 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
                     uint4 rec = make_uint4(path_length, rec_primary, rec_shadow, end_code);
                     reinterpret_cast<uint4*>(P.dlog)[static_cast<uint64_t>(pixel) * P.spp + sample] = rec;
                 }
-                if (P.stream_mode == 1) {
+                if (sample_parallel) {
                     if (all_nonneg_finite(contribution)) {
                         atomicAdd(P.sum_rgb + 3 * pixel, static_cast<double>(contribution.r));
                         atomicAdd(P.sum_rgb + 3 * pixel + 1, static_cast<double>(contribution.g));
@@ -798,19 +820,20 @@ __global__ void __launch_bounds__(128, kMode == kModePlain ? kPlainCtasPerSm : k
     }
 
     // warp-reduce the work counters
+    unsigned long long c_lookups = n_lookups, c_vertices = n_vertices, c_samples = n_samples, c_cells = n_cells;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        n_lookups += __shfl_down_sync(0xffffffffu, n_lookups, o);
-        n_vertices += __shfl_down_sync(0xffffffffu, n_vertices, o);
-        n_samples += __shfl_down_sync(0xffffffffu, n_samples, o);
-        n_cells += __shfl_down_sync(0xffffffffu, n_cells, o);
+        c_lookups += __shfl_down_sync(0xffffffffu, c_lookups, o);
+        c_vertices += __shfl_down_sync(0xffffffffu, c_vertices, o);
+        c_samples += __shfl_down_sync(0xffffffffu, c_samples, o);
+        c_cells += __shfl_down_sync(0xffffffffu, c_cells, o);
     }
     err = __reduce_or_sync(0xffffffffu, err);
     if ((threadIdx.x & 31) == 0) {
-        atomicAdd(P.counters + 0, n_lookups);
-        atomicAdd(P.counters + 1, n_vertices);
-        atomicAdd(P.counters + 2, n_samples);
-        atomicAdd(P.counters + 3, n_cells);
+        atomicAdd(P.counters + 0, c_lookups);
+        atomicAdd(P.counters + 1, c_vertices);
+        atomicAdd(P.counters + 2, c_samples);
+        atomicAdd(P.counters + 3, c_cells);
         if (err) atomicOr(P.error_flags, err);
     }
 }
@@ -915,25 +938,37 @@ void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int m
     pool_majorants_kernel<<<(n + 255) / 256, 256, 0, s>>>(fine, lx, ly, lz, out, mx, my, mz, factor);
 }
 
-const void* plain_kernel_ptr(bool grid_majorant, bool logged) {
+// Logged launches (decision records for the parity tests) follow the stream layout at run time;
+// the production launches use a kernel compiled for their layout.
+const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel) {
     if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true, kModePlain>)
                                      : reinterpret_cast<const void*>(plain_trace_kernel<false, true, kModePlain>);
-    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModePlain>)
-                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModePlain>);
+    if (sample_parallel)
+        return grid_majorant
+                   ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModePlain, kStreamsSampleParallel>)
+                   : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModePlain, kStreamsSampleParallel>);
+    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModePlain, kStreamsPerPixel>)
+                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModePlain, kStreamsPerPixel>);
 }
 
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s) {
     dim3 grid(grid_ctas), block(threads);
+    const size_t sm = grid_majorant ? smem : 0;
     if (p.dlog) {
         if (grid_majorant)
-            plain_trace_kernel<true, true, kModePlain><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, true, kModePlain><<<grid, block, sm, s>>>(p);
         else
-            plain_trace_kernel<false, true, kModePlain><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, true, kModePlain><<<grid, block, sm, s>>>(p);
+    } else if (p.stream_mode == 1) {
+        if (grid_majorant)
+            plain_trace_kernel<true, false, kModePlain, kStreamsSampleParallel><<<grid, block, sm, s>>>(p);
+        else
+            plain_trace_kernel<false, false, kModePlain, kStreamsSampleParallel><<<grid, block, sm, s>>>(p);
     } else {
         if (grid_majorant)
-            plain_trace_kernel<true, false, kModePlain><<<grid, block, smem, s>>>(p);
+            plain_trace_kernel<true, false, kModePlain, kStreamsPerPixel><<<grid, block, sm, s>>>(p);
         else
-            plain_trace_kernel<false, false, kModePlain><<<grid, block, 0, s>>>(p);
+            plain_trace_kernel<false, false, kModePlain, kStreamsPerPixel><<<grid, block, sm, s>>>(p);
     }
 }
 
