@@ -225,11 +225,9 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     const int park_threshold = P.park_threshold > 0 ? P.park_threshold : kParkThreshold;
     const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
     const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
-    // Camera constants of the launch (optix_pathtracing_kernels.cu:43-55).
+    // Sensor height of the launch's camera (optix_pathtracing_kernels.cu:43-55); the rest of the
+    // camera set-up is a few multiplies per sample, cheaper than keeping it in registers.
     const float cam_vh = 2 * tanf(P.cam_fovy * 0.5f);
-    const float cam_vw = P.cam_aspect * cam_vh;
-    const float sensor_area = cam_vw * cam_vh;
-    const M3 cam_rot = quat_to_m3(P.cam_quat[0], P.cam_quat[1], P.cam_quat[2], P.cam_quat[3]);
 
     uint32_t st = ST_FETCH;
     uint32_t pixel = 0, sample = 0;
@@ -410,9 +408,11 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                 sqrt_spread = 0.0f;
                 prev_vertex = kInvalidVertex;
                 terminal_written = false;
+                const float cam_vw = P.cam_aspect * cam_vh;
+                const float sensor_area = cam_vw * cam_vh;
                 origin = v3(P.cam_pos[0], P.cam_pos[1], P.cam_pos[2]);
                 V3 local = normalize(v3(cam_vw * (-0.5f + fx), cam_vh * (0.5f - fy), -1));
-                dir = normalize(mul(cam_rot, local));
+                dir = normalize(mul(quat_to_m3(P.cam_quat[0], P.cam_quat[1], P.cam_quat[2], P.cam_quat[3]), local));
                 float az = fabsf(local.z);
                 dir_pdf = 1 / (az * az * az * sensor_area);
                 float inv = 1.0f / dir_pdf;
