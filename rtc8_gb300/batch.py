@@ -22,7 +22,7 @@ from .configs import C1, SceneConfig, VolumeSpec
 from .renderer import Renderer, setup_scene
 
 # Launch shapes the autotuner tries: (CTAs per SM, park threshold); 0 = the defaults.
-LAUNCH_CANDIDATES = [(0, 0), (4, 16), (5, 16), (5, 28), (4, 24)]
+LAUNCH_CANDIDATES = [(0, 0), (0, 16), (0, 28), (6, 24), (5, 24)]
 
 
 def make_c4_scenes(count: int = 16, seed: int = 4) -> list[SceneConfig]:
