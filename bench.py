@@ -178,7 +178,7 @@ def scene_host_inputs(cfg):
 
 def mlp_bench(steps: int, warmup: int) -> dict:
     """The cache's MLP kernels alone at the sizes of a radiance-cache frame of the equal-error
-    comparison: inference over 256^2 pixels x spp_per_frame queries (2^22 at 64 samples per frame)
+    comparison: inference over 256^2 pixels x spp_per_frame queries (2^23 at 128 samples per frame)
     and training steps of 16384 records, volume encoding, 5 hidden layers of 64. FLOPs are those of
     the padded network (144x64 + 4x64x64 + 64x16 multiply-adds per record forward, 3x that per
     training record)."""

@@ -22,8 +22,15 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
-# Units whose float arithmetic must follow the reference's operation order.
-NO_FMA_UNITS = {"vpt_tracer.cu", "nrc_tracer.cu", "vpt_post.cu", "vpt_wavefront.cu"}
+# Units whose float arithmetic must follow the reference's operation order: no FMA contraction,
+# so products and sums round as in the oracle's restatement (compiled with -ffp-contract=off).
+NO_FMA_UNITS = {"vpt_tracer.cu", "vpt_post.cu", "vpt_wavefront.cu"}
+# The tracker units use the reference's own device arithmetic: it compiles its path-tracing
+# programs and kernels with --use_fast_math (renderer/CMakeLists.txt:48, 65, 91), i.e. intrinsic
+# transcendentals, approximate division and square root, denormals flushed. FMA contraction,
+# which --use_fast_math would also switch on, stays off (the explicit -fmad=false after it wins).
+FAST_MATH_UNITS = {"vpt_tracer.cu", "vpt_wavefront.cu"}
+FAST_MATH = ["--use_fast_math", "-fmad=false"]
 
 
 def nvcc() -> str:
@@ -38,6 +45,8 @@ def _compile(src: Path, verbose_ptxas: bool) -> tuple[Path, str]:
     cmd = [nvcc(), "-c", str(src), "-o", str(obj), *ARCH, *COMMON]
     if src.name in NO_FMA_UNITS:
         cmd += ["-fmad=false"]
+    if src.name in FAST_MATH_UNITS:
+        cmd += FAST_MATH
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     res = subprocess.run(cmd, capture_output=True, text=True)

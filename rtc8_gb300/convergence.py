@@ -133,12 +133,12 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
 # Radiance-cache settings of the equal-error comparison, from a sweep on the 64^3 cloud: the
 # volume cache of rtc8_nrc.h with Adam lr 5e-3 and an EMA (0.9) of the weights for inference;
 # render paths end at path-spread factor 0.32 (the reference's 0.01 leaves a cache bias near
-# relMSE 1e-3 on this scene), biased training suffixes at 0.08; 64 samples per pixel per frame
+# relMSE 1e-3 on this scene), biased training suffixes at 0.08; 128 samples per pixel per frame
 # with one training iteration per frame (the reference's default is 8 samples per frame,
 # renderer_main.cpp:359, a command-line setting). Render paths use the configuration's
 # shadow-ray roulette; the training suffixes do not.
 NRC_SETTINGS = {"termination": 0.32, "train_termination": 0.08, "ema_decay": 0.9, "learning_rate": 5e-3,
-                "spp_per_frame": 64}
+                "spp_per_frame": 128}
 
 
 def compare(cfg: SceneConfig, target: float = 1e-3, oracle_spp: int = 16384, time_budget: float = 60.0,
