@@ -65,6 +65,12 @@ int nrc_infer(NrcHandle* h, void* stream, const float* in, uint32_t n, float* ou
 /* Inference on a device-resident count (*dev_n <= n_max), so a pipeline needs no host sync. */
 int nrc_infer_device_count(NrcHandle* h, void* stream, const float* in, const uint32_t* dev_n, uint32_t n_max,
                            float* out);
+/* Inference on the records listed in idx[0 .. *dev_n) (*dev_n <= n_max, device-resident): record
+ * k = idx[i] reads in[14*k..] and writes out[3*k..]; the other records of `out` are left as they
+ * are. For query buffers where only some slots hold a query (a render pass lists the slots its
+ * paths ended with a cache query in). */
+int nrc_infer_indexed(NrcHandle* h, void* stream, const float* in, const uint32_t* idx, const uint32_t* dev_n,
+                      uint32_t n_max, float* out);
 /* One training step on n records: forward, relative-L2-luminance loss, backward, Adam. */
 int nrc_train(NrcHandle* h, void* stream, const float* in, const float* target, uint32_t n, float* loss_or_null);
 

@@ -186,6 +186,8 @@ _NRC = {
     "nrc_last_error": (C.c_char_p, []),
     "nrc_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "nrc_infer_device_count": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "nrc_infer_indexed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.c_void_p]),
     "nrc_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, c_float_p]),
     "nrc_get_layout": (C.c_int, [C.c_void_p, c_i32_p, c_i32_p, c_i32_p, c_i64_p]),
     "nrc_get_params": (C.c_int, [C.c_void_p, c_float_p]),

@@ -43,6 +43,10 @@ struct NrcBuffers {
     uint32_t* train_suffix = nullptr;    // max_train_suffixes
     float* inferred = nullptr;           // infer_capacity * 3
     float* frame_contribution = nullptr; // width * height * render_spp * 3
+    // Slots of the render queries a pass wrote (count in counters[8]), so that inference runs on
+    // those records only; null = the pass does not list them (inference over every slot, as the
+    // reference does).
+    uint32_t* infer_index = nullptr;     // width * height * render_spp
     float* train_query[2] = {nullptr, nullptr};   // kTrainBufferSize * 14
     float* train_target[2] = {nullptr, nullptr};  // kTrainBufferSize * 3
     TrainVertexInfo* train_vertex = nullptr;      // kTrainBufferSize
@@ -57,7 +61,7 @@ struct NrcBuffers {
     uint32_t* shufflers = nullptr;                // kNumTrainingDataPerFrame LCG states
     // [0..1] numTrainingData per buffer, [2..5] trainImageSize (x, y) per buffer,
     // [6] offsetToSelectUnbiasedPath, [7] training-pass query count of the current buffer
-    // (trainW * trainH), [8..15] unused.
+    // (trainW * trainH), [8] render queries listed in infer_index, [9..15] unused.
     uint32_t* counters = nullptr;
     float* stats = nullptr;          // per buffer: min rgb, max rgb, avg rgb (9 floats)
     uint32_t buffer_index = 0;       // nrcBufferIndex of the current training iteration

@@ -203,9 +203,15 @@ __device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* til
     (void)K;
 }
 
-__device__ __forceinline__ void load_query(const float* __restrict__ in, uint32_t row, uint32_t n, float* q) {
+// Record of row `row` of a launch: the row itself, or idx[row] for an indexed launch.
+__device__ __forceinline__ uint32_t record_of(const uint32_t* __restrict__ idx, uint32_t row) {
+    return idx ? __ldg(idx + row) : row;
+}
+
+__device__ __forceinline__ void load_query(const float* __restrict__ in, const uint32_t* __restrict__ idx, uint32_t row,
+                                           uint32_t n, float* q) {
     if (row < n) {
-        const float2* p = reinterpret_cast<const float2*>(in + static_cast<size_t>(row) * 14);
+        const float2* p = reinterpret_cast<const float2*>(in + static_cast<size_t>(record_of(idx, row)) * 14);
 #pragma unroll
         for (int i = 0; i < 7; ++i) {
             float2 v = __ldg(p + i);
@@ -294,9 +300,11 @@ __host__ __device__ constexpr uint32_t infer_tile_bytes(int in_dim) { return (kT
 // TA: the hidden activations stay in tensor memory (32 packed FP16 columns per group next to the
 // group's 64 accumulator columns) and feed the next layer's MMA as its A operand; only the encoded
 // input tile goes through shared memory.
+// idx (optional): row r of the launch is record idx[r] of `in` and `out`.
 template <int IN, int G, bool TA>
 __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
                                                              const float* __restrict__ in,
+                                                             const uint32_t* __restrict__ idx,
                                                              const uint32_t* __restrict__ dev_n, uint32_t n_max,
                                                              float* __restrict__ out, unsigned int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -331,14 +339,14 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
     bool ok = true;
     float q[14];
     const uint32_t stride = gridDim.x * G;
-    load_query(in, (blockIdx.x * G + g) * kTile + gt, n, q);
+    load_query(in, idx, (blockIdx.x * G + g) * kTile + gt, n, q);
     for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += stride) {
         const uint32_t row = tile * kTile + gt;
         encode_row(ly.enc, q, s_t, gt, IN);
         // The next tile's queries load while this tile runs through the layers. (Encoding it
         // during layer 1, when the input tile is already free in the TA form, measured slower:
         // the group's next epilogue waits for the encoder.)
-        load_query(in, (tile + stride) * kTile + gt, n, q);
+        load_query(in, idx, (tile + stride) * kTile + gt, n, q);
         fence_async_smem();
         named_sync(bar_id, kTile);
         for (int j = 0; j < ly.L && ok; ++j) {
@@ -392,7 +400,7 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
                 tmem_ld16(tmem + lane_base, v);
                 tmem_wait_ld();
                 if (row < n) {
-                    float* o = out + static_cast<size_t>(row) * 3;
+                    float* o = out + static_cast<size_t>(record_of(idx, row)) * 3;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) o[c] = ly.out_act == NRC_OUTPUT_EXP ? __expf(v[c]) : v[c];
                 }
@@ -441,7 +449,7 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, co
     }
     const uint32_t row = blockIdx.x * kTile + tid;
     float q[14];
-    load_query(in, row, n, q);
+    load_query(in, nullptr, row, n, q);
     encode_row(ly.enc, q, s_act0, tid, IN);
     fence_async_smem();
     tc_fence_before();
@@ -639,7 +647,7 @@ __global__ void encode_kernel(const NetLayout ly, const float* __restrict__ in, 
     __shared__ __align__(128) uint8_t tile[kTile * IN * 2];
     uint32_t row = blockIdx.x * kTile + threadIdx.x;
     float q[14];
-    load_query(in, row, n, q);
+    load_query(in, nullptr, row, n, q);
     encode_row(ly.enc, q, tile, threadIdx.x, IN);
     if (row < n)
         for (int c = 0; c < IN; c += 16) {
@@ -892,7 +900,8 @@ int nrc_destroy(NrcHandle* h) {
     return NRC_OK;
 }
 
-static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_t* dev_n, uint32_t n, float* out) {
+static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_t* idx, const uint32_t* dev_n,
+                      uint32_t n, float* out) {
     if (!h || !in || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer: null argument");
     if (n == 0) return NRC_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -904,32 +913,38 @@ static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_
     const dim3 block(kTile * G);
     if (G == 4) {
         if (vol)
-            mlp_infer_kernel<144, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
     } else if (G == 2) {
         if (vol)
-            mlp_infer_kernel<144, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
     } else {
         if (vol)
-            mlp_infer_kernel<144, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
     }
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
 }
 
 int nrc_infer(NrcHandle* h, void* stream, const float* in, uint32_t n, float* out) {
-    return infer_impl(h, stream, in, nullptr, n, out);
+    return infer_impl(h, stream, in, nullptr, nullptr, n, out);
 }
 
 int nrc_infer_device_count(NrcHandle* h, void* stream, const float* in, const uint32_t* dev_n, uint32_t n_max,
                            float* out) {
     if (!dev_n) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer_device_count: null count");
-    return infer_impl(h, stream, in, dev_n, n_max, out);
+    return infer_impl(h, stream, in, nullptr, dev_n, n_max, out);
+}
+
+int nrc_infer_indexed(NrcHandle* h, void* stream, const float* in, const uint32_t* idx, const uint32_t* dev_n,
+                      uint32_t n_max, float* out) {
+    if (!idx || !dev_n) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_infer_indexed: null index list or count");
+    return infer_impl(h, stream, in, idx, dev_n, n_max, out);
 }
 
 int nrc_train(NrcHandle* h, void* stream, const float* in, const float* target, uint32_t n, float* loss_out) {

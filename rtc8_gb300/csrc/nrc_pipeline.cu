@@ -58,6 +58,7 @@ int ensure_nrc(VptContext* c) {
     chk(alloc_zero(&b->train_suffix, npix));
     chk(alloc_zero(&b->inferred, static_cast<size_t>(b->infer_capacity) * 3));
     chk(alloc_zero(&b->frame_contribution, npix * 3));
+    chk(alloc_zero(&b->infer_index, npix));
     for (int i = 0; i < 2; ++i) {
         chk(alloc_zero(&b->train_query[i], static_cast<size_t>(vpt::kTrainBufferSize) * vpt::kQueryFloats));
         chk(alloc_zero(&b->train_target[i], static_cast<size_t>(vpt::kTrainBufferSize) * 3));
@@ -108,11 +109,13 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
     free_ptr(b.infer_terminal);
     free_ptr(b.inferred);
     free_ptr(b.frame_contribution);
+    free_ptr(b.infer_index);
     const uint32_t cap = static_cast<uint32_t>((slots + 127) / 128 * 128);
     cudaError_t e = alloc_zero(&b.infer_query, static_cast<size_t>(cap) * vpt::kQueryFloats);
     if (e == cudaSuccess) e = alloc_zero(&b.infer_terminal, slots);
     if (e == cudaSuccess) e = alloc_zero(&b.inferred, static_cast<size_t>(cap) * 3);
     if (e == cudaSuccess) e = alloc_zero(&b.frame_contribution, slots * 3);
+    if (e == cudaSuccess) e = alloc_zero(&b.infer_index, slots);
     if (e != cudaSuccess) {
         c->release_nrc();
         return fail(VPT_ERR_OUT_OF_MEMORY, std::string("render-pass buffers: ") + cudaGetErrorString(e));
@@ -124,8 +127,10 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
 
 // Launch of a radiance-cache pass of the persistent tracker: the training pass or a render pass
 // of one sample per pixel on the per-pixel streams (stream_mode 0), or a render pass of `spp`
-// samples per pixel on sample-parallel streams (stream_mode 1).
-int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0) {
+// samples per pixel on sample-parallel streams (stream_mode 1). With `index_queries` the render
+// paths also list the slots of the queries they write (infer_index, counters[8]).
+int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
+                bool index_queries = false) {
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;
@@ -141,6 +146,11 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     }
     tp.park_threshold = c->park_threshold;
     tp.nrc = *c->nrc;
+    if (index_queries) {
+        NRCP_CUDA(cudaMemsetAsync(c->nrc->counters + 8, 0, sizeof(uint32_t), s));
+    } else {
+        tp.nrc.infer_index = nullptr;
+    }
     tp.nrc_buf = buf;
     tp.nrc_density_query = c->nrc_query_density;
     tp.nrc_termination = c->nrc_termination;
@@ -189,6 +199,7 @@ void VptContextImpl::release_nrc() {
     free_ptr(nrc->train_suffix);
     free_ptr(nrc->inferred);
     free_ptr(nrc->frame_contribution);
+    free_ptr(nrc->infer_index);
     for (int i = 0; i < 2; ++i) {
         free_ptr(nrc->train_query[i]);
         free_ptr(nrc->train_target[i]);
@@ -341,7 +352,7 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
         if (batched && it == 0) {
             // The first training pass and the frame's render samples in one launch: the render
             // paths need the network only at their inference, after the training steps below.
-            if ((rc = launch_pass(c, s, vpt::kModeComboNrc, buf, spp, 1))) return rc;
+            if ((rc = launch_pass(c, s, vpt::kModeComboNrc, buf, spp, 1, true))) return rc;
         } else if ((rc = vpt_launch_generate_training(c, stream, buf))) {
             return rc;
         }
@@ -361,9 +372,11 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     }
     if (spp == 0) return VPT_OK;
     if (batched) {
-        if (train_iterations == 0 && (rc = launch_pass(c, s, vpt::kModeRenderNrc, 0, spp, 1))) return rc;
-        if (nrc_infer(net, stream, b.infer_query, npix * spp, b.inferred))
-            return fail(VPT_ERR_CUDA, std::string("nrc_infer: ") + nrc_last_error());
+        if (train_iterations == 0 && (rc = launch_pass(c, s, vpt::kModeRenderNrc, 0, spp, 1, true))) return rc;
+        // Only the slots whose paths ended with a cache query are inferred (the others are not
+        // read by the accumulation).
+        if (nrc_infer_indexed(net, stream, b.infer_query, b.infer_index, b.counters + 8, npix * spp, b.inferred))
+            return fail(VPT_ERR_CUDA, std::string("nrc_infer_indexed: ") + nrc_last_error());
         return vpt_accumulate_inferred_batch(c, stream, c->accum_samples, spp);
     }
     for (uint32_t i = 0; i < spp; ++i) {

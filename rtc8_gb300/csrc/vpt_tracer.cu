@@ -547,6 +547,16 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                             ti.tp[2] = throughput.b;
                             ti.bits = 1u | ((path_length & 0xFFu) << 1);
                             P.nrc.infer_terminal[slot] = ti;
+                            if (P.nrc.infer_index) {
+                                // List the slot for the inference (one atomic per converged group).
+                                const uint32_t m = __activemask();
+                                const int leader = __ffs(m) - 1;
+                                const uint32_t lane = threadIdx.x & 31;
+                                uint32_t base = 0;
+                                if (static_cast<int>(lane) == leader) base = atomicAdd(P.nrc.counters + 8, __popc(m));
+                                base = __shfl_sync(m, base, leader);
+                                P.nrc.infer_index[base + __popc(m & ((1u << lane) - 1u))] = slot;
+                            }
                         }
                         terminal_written = true;
                         end_code = END_CACHE;

@@ -91,6 +91,13 @@ class NeuralRadianceCache:
         _check(self.lib.nrc_infer(self.h, C.c_void_p(_ptr(stream)), C.c_void_p(_ptr(input_data)), num_data,
                                   C.c_void_p(_ptr(prediction_data))), "nrc_infer")
 
+    def infer_indexed(self, stream, input_data, index, count, max_count: int, prediction_data) -> None:
+        """nrc_infer_indexed: inference on the records index[0 .. *count) (device tensors; count
+        holds one uint32 on the device), leaving the other records of prediction_data as they are."""
+        _check(self.lib.nrc_infer_indexed(self.h, C.c_void_p(_ptr(stream)), C.c_void_p(_ptr(input_data)),
+                                          C.c_void_p(_ptr(index)), C.c_void_p(_ptr(count)), max_count,
+                                          C.c_void_p(_ptr(prediction_data))), "nrc_infer_indexed")
+
     def train(self, stream, input_data, target_data, num_data: int, loss: bool = False):
         out = C.c_float(0.0)
         _check(self.lib.nrc_train(self.h, C.c_void_p(_ptr(stream)), C.c_void_p(_ptr(input_data)),

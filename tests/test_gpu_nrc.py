@@ -97,6 +97,41 @@ def test_inference_matches_oracle(cuda_device, encoding, hidden):
     cache.finalize()
 
 
+def test_indexed_inference_matches_full_inference(cuda_device):
+    """nrc_infer_indexed (the render pass lists the slots that hold a query): the listed records
+    get exactly the full inference's values, in any list order, with the count read on the
+    device; unlisted records keep their contents."""
+    import torch
+
+    cfg = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=cfg)
+    n = 5000
+    q = torch.from_numpy(_queries(n, 4, volume=True)).cuda()
+    full = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    cache.infer(None, q, n, full)
+    rng = np.random.default_rng(9)
+    listed = rng.permutation(n)[: 777].astype(np.uint32)  # not a multiple of 128, shuffled
+    idx = torch.from_numpy(listed.view(np.int32)).cuda()
+    count = torch.tensor([len(listed)], dtype=torch.int32, device="cuda")
+    out = torch.full((n, 3), -5.0, dtype=torch.float32, device="cuda")
+    cache.infer_indexed(None, q, idx, count, n, out)
+    torch.cuda.synchronize()
+    got, ref = out.cpu().numpy(), full.cpu().numpy()
+    np.testing.assert_array_equal(got[listed], ref[listed])
+    mask = np.ones(n, bool)
+    mask[listed] = False
+    assert np.all(got[mask] == -5.0)
+    # an empty list leaves everything as it is
+    count.zero_()
+    out2 = torch.full((n, 3), 3.0, dtype=torch.float32, device="cuda")
+    cache.infer_indexed(None, q, idx, count, n, out2)
+    torch.cuda.synchronize()
+    assert torch.all(out2 == 3.0)
+    assert cache.device_errors() == 0
+    cache.finalize()
+
+
 @pytest.mark.parametrize("encoding,hidden", [(nrc.NRC_ENCODING_VOLUME, 5), (nrc.NRC_ENCODING_REFERENCE, 2)])
 def test_gradients_loss_and_adam_match_oracle(cuda_device, encoding, hidden):
     import torch

@@ -438,3 +438,40 @@ def test_combined_training_and_render_launch_matches_separate_passes(cuda_device
     cache.finalize()
     a.close()
     b.close()
+
+
+def test_batched_frame_infers_only_the_query_slots(cuda_device):
+    """A batched render frame lists the slots whose paths ended with a cache query and infers
+    only those: the count equals the number of query slots, every query slot holds the network's
+    prediction for its query (bit for bit, as a full inference gives it), and the other slots are
+    not written."""
+    import torch
+
+    spp = 4
+    cfg = small_config_mode(size=48, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=1)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=nrc.default_config(nrc.NRC_ENCODING_VOLUME))
+    r.nrc_set_termination_factor(0.32, 0.08)
+    r.nrc_frame(cache, 2, spp, True)  # allocates the render slots, trains a little
+    torch.cuda.synchronize()
+    v = r.nrc_views()
+    v["inferred"].fill_(-1.0e30)
+    r.nrc_frame(cache, 0, spp, False)  # render pass + indexed inference + accumulation
+    torch.cuda.synchronize()
+    n = cfg.width * cfg.height * spp
+    bits = _np(v["infer_terminal"])[:n, 3].copy().view(np.uint32)
+    has_query = (bits & 1) == 1
+    assert 0 < has_query.sum() < n
+    assert int(_np(v["counters"]).view(np.uint32)[8]) == int(has_query.sum())
+    got = _np(v["inferred"])[:n]
+    queries = v["infer_query"][:n][torch.from_numpy(has_query).cuda()].contiguous()
+    ref = torch.zeros((queries.shape[0], 3), dtype=torch.float32, device="cuda")
+    cache.infer(None, queries, queries.shape[0], ref)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(got[has_query], ref.cpu().numpy())
+    assert np.all(got[~has_query] == -1.0e30)
+    assert r.device_errors() == 0 and cache.device_errors() == 0
+    cache.finalize()
+    r.close()
