@@ -219,6 +219,64 @@ __global__ void accumulate_kernel(NrcBuffers b, float radiance_scale, uint32_t a
     }
 }
 
+// accumulate_kernel for spp > 1 with the samples spread over the threads: a block covers 32
+// pixels, its 8 warps take every 8th sample of them (coalesced loads of consecutive pixels'
+// slots), and the partial sums are added in shared memory in warp order.
+constexpr int kAccumParts = 8;
+__global__ void __launch_bounds__(32 * kAccumParts) accumulate_parallel_kernel(NrcBuffers b, float radiance_scale,
+                                                                               uint32_t accum_frames, uint32_t spp,
+                                                                               double* __restrict__ sum,
+                                                                               float* __restrict__ mean,
+                                                                               unsigned int* __restrict__ err) {
+    __shared__ double s_acc[kAccumParts][32][3];
+    const uint32_t npix = static_cast<uint32_t>(b.width) * static_cast<uint32_t>(b.height);
+    const uint32_t lane = threadIdx.x & 31, part = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * 32 + lane;
+    double acc[3] = {0, 0, 0};
+    if (i < npix) {
+        for (uint32_t smp = part; smp < spp; smp += kAccumParts) {
+            const size_t slot = static_cast<size_t>(smp) * npix + i;
+            const TerminalInfo t = b.infer_terminal[slot];
+            const RGB direct = load_rgb(b.frame_contribution + 3 * slot);
+            RGB radiance = rgb(0, 0, 0);
+            if (t.bits & 1u) {
+                radiance = max0(load_rgb(b.inferred + 3 * slot));
+                if (radiance_scale > 0) radiance = rdiv(radiance, radiance_scale);
+                radiance = radiance * reflectance(b.infer_query + kQueryFloats * slot);
+            }
+            RGB c = direct + rgb(t.tp[0], t.tp[1], t.tp[2]) * radiance;
+            if (!all_nonneg_finite(c)) {
+                atomicOr(err, 2u);
+                c = rgb(0, 0, 0);
+            }
+            acc[0] += c.r;
+            acc[1] += c.g;
+            acc[2] += c.b;
+        }
+    }
+    s_acc[part][lane][0] = acc[0];
+    s_acc[part][lane][1] = acc[1];
+    s_acc[part][lane][2] = acc[2];
+    __syncthreads();
+    if (part != 0 || i >= npix) return;
+    double t0 = 0, t1 = 0, t2 = 0;
+#pragma unroll
+    for (int w = 0; w < kAccumParts; ++w) {
+        t0 += s_acc[w][lane][0];
+        t1 += s_acc[w][lane][1];
+        t2 += s_acc[w][lane][2];
+    }
+    const double s0 = sum[3 * static_cast<size_t>(i)] + t0;
+    const double s1 = sum[3 * static_cast<size_t>(i) + 1] + t1;
+    const double s2 = sum[3 * static_cast<size_t>(i) + 2] + t2;
+    sum[3 * static_cast<size_t>(i)] = s0;
+    sum[3 * static_cast<size_t>(i) + 1] = s1;
+    sum[3 * static_cast<size_t>(i) + 2] = s2;
+    const double inv = 1.0 / (static_cast<double>(accum_frames) + spp);
+    store_rgb(mean + 3 * static_cast<size_t>(i),
+              rgb(static_cast<float>(s0 * inv), static_cast<float>(s1 * inv), static_cast<float>(s2 * inv)));
+}
+
 }  // namespace
 
 void nrc_prepare(const NrcBuffers& b, uint32_t buf, uint32_t offset, bool new_sequence, cudaStream_t s) {
@@ -235,6 +293,11 @@ void nrc_shuffle(const NrcBuffers& b, uint32_t buf, float radiance_scale, cudaSt
 void nrc_accumulate(const NrcBuffers& b, float radiance_scale, uint32_t accum_frames, uint32_t spp, bool from_sums,
                     double* sum, float* mean, unsigned int* err, cudaStream_t s) {
     uint32_t n = static_cast<uint32_t>(b.width) * static_cast<uint32_t>(b.height);
+    if (spp > 1) {
+        accumulate_parallel_kernel<<<(n + 31) / 32, 32 * kAccumParts, 0, s>>>(b, radiance_scale, accum_frames, spp, sum,
+                                                                              mean, err);
+        return;
+    }
     accumulate_kernel<<<(n + 255) / 256, 256, 0, s>>>(b, radiance_scale, accum_frames, spp, from_sums ? 1 : 0, sum, mean,
                                                       err);
 }
