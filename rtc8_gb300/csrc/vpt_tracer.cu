@@ -274,22 +274,14 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     constexpr bool kCombo = kMode == kModeComboNrc;
     constexpr bool kMayTrain = kMode == kModeTrainNrc || kCombo;
     bool is_train = kMode == kModeTrainNrc;
-    uint32_t img_w = static_cast<uint32_t>(P.width), img_h = static_cast<uint32_t>(P.height);
-    uint32_t num_items = num_pixels, num_train = 0, train_w = 0, train_h = 0;
+    // Training image of the pass (the adaptive size prepared on the device). The pass image
+    // size, the item counts and the state buffer a sample continues are derived from these and
+    // `is_train` where needed rather than held in registers.
+    uint32_t train_w = 0, train_h = 0;
     if constexpr (kMayTrain) {
         train_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
         train_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
-        num_train = min(train_w * train_h, num_pixels);
     }
-    if constexpr (kMode == kModeTrainNrc) {
-        num_items = num_train;
-    } else if constexpr (kNrc) {
-        // Sample-parallel streams: P.spp samples per pixel in one render pass, each its own
-        // work item and record slot (sample-major: slot = sample * num_pixels + pixel).
-        if (sample_parallel) num_items = num_pixels * P.spp;
-        if constexpr (kCombo) num_items += num_train;
-    }
-    uint64_t* rng_buf = P.rng;  // per-pixel states the current sample continues (and writes back)
     uint32_t slot = 0;  // record index of the current sample in the pass buffers
     const float term_factor = P.nrc_termination > 0 ? P.nrc_termination : kPathTerminationFactor;
     // Biased training suffixes end at twice the render factor (optix_pathtracing_kernels.cu:
@@ -299,7 +291,7 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     uint32_t rng_index = 0;
     float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
     uint32_t prev_vertex = kInvalidVertex;
-    RGB prev_local_tp = rgb(0, 0, 0), nee_value = rgb(0, 0, 0);
+    RGB nee_value = rgb(0, 0, 0);
     bool unbiased = false, terminal_written = false;
 
     while (true) {
@@ -326,6 +318,16 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                 base = __shfl_sync(need, base, leader);
                 const uint32_t item = base + __popc(need & ((1u << lane) - 1u));
                 if constexpr (kNrc) {
+                    const uint32_t num_train = kMayTrain ? min(train_w * train_h, num_pixels) : 0u;
+                    // Sample-parallel streams: P.spp samples per pixel in one render pass, each
+                    // its own work item and record slot (sample-major: slot = sample * pixels + pixel).
+                    uint32_t num_items = num_pixels;
+                    if constexpr (kMode == kModeTrainNrc) {
+                        num_items = num_train;
+                    } else {
+                        if (sample_parallel) num_items = num_pixels * P.spp;
+                        if constexpr (kCombo) num_items += num_train;
+                    }
                     if (item >= num_items) {
                         st = ST_DONE;
                         break;
@@ -335,13 +337,10 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     if (kMayTrain && is_train) {
                         uint32_t px, py;
                         train_item_to_pixel(item, train_w, train_h, P.nrc.counters[6], &px, &py);
-                        img_w = train_w;
-                        img_h = train_h;
                         pixel = py * train_w + px;  // linear index in the training image
                         slot = pixel;
                         rng_index = py * static_cast<uint32_t>(P.width) + px;
-                        rng_buf = kCombo ? P.nrc.train_rng : P.rng;
-                        rng.state = rng_buf[rng_index];
+                        rng.state = (kCombo ? P.nrc.train_rng : P.rng)[rng_index];
                         // optix_pathtracing_kernels.cu:60-66: one unbiased suffix per 4x4 tile.
                         const uint32_t tile_index = (py % 4) * 4 + (px % 4);
                         unbiased = (tile_index + P.nrc.counters[6]) % 16 == 0;
@@ -349,10 +348,7 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                         break;
                     }
                     const uint32_t r = kCombo ? item - num_train : item;
-                    img_w = static_cast<uint32_t>(P.width);
-                    img_h = static_cast<uint32_t>(P.height);
                     slot = r;
-                    rng_buf = P.rng;
                     if (sample_parallel) {
                         pixel = r % num_pixels;
                         sample = r / num_pixels;
@@ -399,6 +395,8 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
             }
             case ST_CAMERA: {
                 // optix_pathtracing_kernels.cu:43-55, 76-81.
+                const uint32_t img_w = (kMayTrain && is_train) ? train_w : static_cast<uint32_t>(P.width);
+                const uint32_t img_h = (kMayTrain && is_train) ? train_h : static_cast<uint32_t>(P.height);
                 uint32_t px = pixel % img_w;
                 uint32_t py = pixel / img_w;
                 float ux = rng.uniform();
@@ -483,8 +481,10 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     if (kMayTrain && is_train) {
                         // :148-152: the environment hit completes the previous vertex's target.
                         if (prev_vertex != kInvalidVertex) {
+                            // The previous vertex's local throughput, as this lane recorded it.
+                            const TrainVertexInfo& pv = P.nrc.train_vertex[prev_vertex];
                             float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(prev_vertex);
-                            RGB add = prev_local_tp * implicit;
+                            RGB add = rgb(pv.local_tp[0], pv.local_tp[1], pv.local_tp[2]) * implicit;
                             tg[0] += add.r;
                             tg[1] += add.g;
                             tg[2] += add.b;
@@ -695,7 +695,6 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                         tg[0] = nee_value.r;
                         tg[1] = nee_value.g;
                         tg[2] = nee_value.b;
-                        prev_local_tp = local_tp;
                         prev_vertex = idx;
                     } else {
                         write_query(P.nrc.train_end_query + kQueryFloats * static_cast<size_t>(slot), origin, v_out,
@@ -737,7 +736,8 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                         fc[1] = c.g;
                         fc[2] = c.b;
                     }
-                    if ((kMayTrain && is_train) || !sample_parallel) rng_buf[rng_index] = rng.state;
+                    if ((kMayTrain && is_train) || !sample_parallel)
+                        ((kCombo && is_train) ? P.nrc.train_rng : P.rng)[rng_index] = rng.state;
                     st = ST_FETCH;
                     break;
                 }
