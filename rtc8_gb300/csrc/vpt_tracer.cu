@@ -46,8 +46,12 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 // Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp
 // (1 -> 4 raised the 1024x1024 sparse workload by 12%; 6 to 64 measured within 2% of 4).
 constexpr int kCellStepsPerPass = 4;
-// Parked lanes of a warp that trigger a joint event phase.
-constexpr int kParkThreshold = 24;
+// Parked lanes of a warp that trigger a joint event phase. Plain tracer (C2 / C5 at 7 CTAs/SM):
+// 12 -> 432 / 913, 16 -> 450 / 939, 20 -> 452 / 932, 24 -> 442 / 916, 28 -> 419 / 862 M paths/s;
+// the radiance-cache passes (shorter paths, more event work per path) are faster at 24 (frame
+// 4.56 ms against 4.75 ms at 20).
+constexpr int kParkThreshold = 20;
+constexpr int kNrcParkThreshold = 24;
 // Resident CTAs of 128 threads per SM the register allocation is bounded for. The plain tracer
 // on sample-parallel streams holds its state in 72 registers at 7 CTAs/SM (1024^2 sparse 512^3:
 // 261 / 284 / 295 / 283 M paths/s at 5 / 6 / 7 / 8); per-pixel streams (and the logged parity
@@ -222,7 +226,8 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
     const float global_maj = P.density_coeff * g.global_majorant;
     const uint32_t step_cap = P.max_steps > 0 ? static_cast<uint32_t>(P.max_steps) : kHardStepCap;
-    const int park_threshold = P.park_threshold > 0 ? P.park_threshold : kParkThreshold;
+    const int park_threshold =
+        P.park_threshold > 0 ? P.park_threshold : (kMode == kModePlain ? kParkThreshold : kNrcParkThreshold);
     const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
     const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
     // Sensor height of the launch's camera (optix_pathtracing_kernels.cu:43-55); the rest of the
