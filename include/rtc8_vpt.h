@@ -297,7 +297,9 @@ int vpt_synchronize(VptContext* ctx, void* stream);
 int vpt_set_tracker(VptContext* ctx, int32_t kind, int32_t slots_per_sm, int32_t pass_steps,
                     int32_t track_ctas_per_sm);
 /* Launch shape of the persistent tracker (CTAs per SM, threads per CTA) and the number of
- * parked lanes of a warp that triggers its joint event phase; 0 = defaults. */
+ * parked lanes of a warp that triggers its joint event phase; 0 = defaults (as many 128-thread
+ * CTAs as fit: 7 per SM for the plain tracer on sample-parallel streams; park threshold 20 for
+ * the plain tracer, 24 for the radiance-cache passes). */
 int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,
                          int32_t park_threshold);
 
