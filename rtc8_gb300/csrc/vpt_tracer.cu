@@ -43,9 +43,13 @@ enum : uint32_t {
 // (zero or non-finite majorants, albedo 1 in a huge medium) can keep a launch running forever.
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
-// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp
-// (1 -> 4 raised the 1024x1024 sparse workload by 12%; 6 to 64 measured within 2% of 4).
-constexpr int kCellStepsPerPass = 4;
+// Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp. With
+// the current arithmetic (C2 / C5 / C1 M paths/s): 2 -> - / 925 / 861, 4 -> 454 / 927 / 852,
+// 8 -> 471 / 979 / 888, 16 -> 480 / 977 / 898, 32 -> 481 / 974 / 870 (1 -> 4 had raised C2 by 12%
+// with IEEE division and libm-accurate functions). The radiance-cache passes keep 4 (frame
+// 4.55 ms against 4.68 ms at 16).
+constexpr int kCellStepsPerPass = 16;
+constexpr int kNrcCellStepsPerPass = 4;
 // Parked lanes of a warp that trigger a joint event phase. Plain tracer (C2 / C5 at 7 CTAs/SM):
 // 12 -> 432 / 913, 16 -> 450 / 939, 20 -> 452 / 932, 24 -> 442 / 916, 28 -> 419 / 862 M paths/s;
 // the radiance-cache passes (shorter paths, more event work per path) are faster at 24 (frame
@@ -107,14 +111,14 @@ enum : int { PASS_LOOKUP = 0, PASS_YIELD = 1, PASS_END = 2 };
 // One tracking pass of a segment from (t, texit, maj, dda): a free-flight distance
 // (optix_pathtracing_kernels.cu:113-118 / renderer_kernel_common.h:374-378), with the majorant
 // grid sampled within the current cell, where an overshoot of the cell's exit restarts at the
-// exit (memoryless) and empty cells are crossed without draws, at most kCellStepsPerPass
-// crossings per pass. PASS_LOOKUP leaves t at the tentative collision; PASS_END means the segment
+// exit (memoryless) and empty cells are crossed without draws, at most kCells crossings per
+// pass. PASS_LOOKUP leaves t at the tentative collision; PASS_END means the segment
 // is over (also on a NaN distance); PASS_YIELD means the pass crossed its cells without one.
 // The sign of a direction component: the DDA step along that axis (dda_init derives it from the
 // same sign, the index-space direction being the world direction times a positive scale).
 __device__ __forceinline__ int step_of(float d) { return d > 0 ? 1 : (d < 0 ? -1 : 0); }
 
-template <bool kGridMajorant>
+template <bool kGridMajorant, int kCells>
 __device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, float density_coeff, float t1, V3 dir,
                                           Pcg32& rng, float& t, float& texit, float& maj, DdaState& dda,
                                           uint32_t& n_cells) {
@@ -122,7 +126,7 @@ __device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, 
         t += -logf(1.0f - rng.uniform()) / maj;
         return (t <= t1) ? PASS_LOOKUP : PASS_END;
     } else {
-        for (int c = 0; c < kCellStepsPerPass; ++c) {
+        for (int c = 0; c < kCells; ++c) {
             if (maj > 0) {
                 const float tt = t + -logf(1.0f - rng.uniform()) / maj;
                 if (tt < texit) {
@@ -457,8 +461,9 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
             }
             case ST_STEP: {
                 const V3 seg_dir = shadow ? -light_dir : dir;
-                const int r = track_pass<kGridMajorant>(g, maj_grid, P.density_coeff, t1, seg_dir, rng, t, texit, maj,
-                                                        dda, n_cells);
+                constexpr int kCells = kMode == kModePlain ? kCellStepsPerPass : kNrcCellStepsPerPass;
+                const int r = track_pass<kGridMajorant, kCells>(g, maj_grid, P.density_coeff, t1, seg_dir, rng, t, texit,
+                                                                maj, dda, n_cells);
                 if (r == PASS_LOOKUP) {
                     const V3 seg_eye = shadow ? origin + trace_len * light_dir : origin;
                     lookup_pos = seg_eye + seg_dir * t;
