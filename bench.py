@@ -305,6 +305,19 @@ def batch_bench(steps: int, warmup: int, spp: int = 4) -> dict:
 
 
 # ------------------------------------------------------------------------------ main
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time for the same timed region (every rank passed a barrier before it):
+    whole-job throughput is the units all ranks processed divided by this time."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,11 +431,7 @@ def main():
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     cnt = r.counters()
-    total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(step_ms)), world, dev)
     paths_per_rank = cfg.width * cfg.height * STEP_SPP * args.steps
     value = world * paths_per_rank / (total_ms / 1000.0)
 
@@ -442,7 +451,9 @@ def main():
         t1 = time.perf_counter()
         if i >= warmup:
             e2e_ms.append(1000.0 * (t1 - t0))
-    e2e_total = sum(e2e_ms)
+    if world > 1:
+        dist.barrier()
+    e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
     e2e_value = world * paths_per_rank / (e2e_total / 1000.0)
 
     # ---- roofline of the tracer kernel (algorithmic bytes per launch / average launch time)
