@@ -1,0 +1,118 @@
+"""Test infrastructure only (the oracle): float64 restatement of the reference's Hosek-Wilkie sky.
+
+Imported by tests/ only. Follows:
+* the Hosek-Wilkie 2013 model's radiance (ArHosekSkyModel_GetRadianceInternal and
+  arhosekskymodel_radiance, restated in renderer/gpu_kernels/analytic_sky_kernels.cu:16-66):
+  per-band model state = 11 x 9 configuration values, 11 radiances, 11 sky emission correction
+  factors; the radiance at a wavelength interpolates the two neighbouring 40 nm channels;
+* the sky texture (analytic_sky_kernels.cu:220-276, without the solar disc): texel (x, y) ->
+  polar angles (y from the zenith), the lower hemisphere mirrored, 16 bands weighted by the CIE
+  1931 CMF integrals into XYZ, XYZ -> linear sRGB (common/basic_types.h:3000-3010), the HSV
+  saturation push towards blue (:257-266 with basic_types.h:3114-3160), and the lower hemisphere
+  blended into the "sea" colour (:268-274).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+BANDS = 16
+
+
+def radiance_internal(cfg, theta, gamma):
+    """ArHosekSkyModel_GetRadianceInternal for one configuration (9 values)."""
+    exp_m = np.exp(cfg[4] * gamma)
+    ray_m = np.cos(gamma) ** 2
+    mie_m = (1.0 + np.cos(gamma) ** 2) / (1.0 + cfg[8] ** 2 - 2.0 * cfg[8] * np.cos(gamma)) ** 1.5
+    zenith = np.sqrt(np.cos(theta))
+    return (1.0 + cfg[0] * np.exp(cfg[1] / (np.cos(theta) + 0.01))) * (
+        cfg[2] + cfg[3] * exp_m + cfg[5] * ray_m + cfg[6] * mie_m + cfg[7] * zenith)
+
+
+def unpack_state(state: np.ndarray) -> dict:
+    """One band's 122 floats: configs[11][9], radiances[11], emission correction[11], solar radius."""
+    s = np.asarray(state, dtype=np.float64)
+    return {"configs": s[:99].reshape(11, 9), "radiances": s[99:110], "ecf": s[110:121], "solar_radius": s[121]}
+
+
+def sky_radiance(state: dict, theta, gamma, wavelength: float):
+    """arhosekskymodel_radiance: the sky (no solar disc) at one wavelength in nm."""
+    low = int((wavelength - 320.0) / 40.0)
+    if low < 0 or low >= 11:
+        return np.zeros_like(np.asarray(theta, dtype=np.float64))
+    interp = math.fmod((wavelength - 320.0) / 40.0, 1.0)
+    val_low = radiance_internal(state["configs"][low], theta, gamma) * state["radiances"][low] * state["ecf"][low]
+    if interp < 1e-6:
+        return val_low
+    result = (1.0 - interp) * val_low
+    if low + 1 < 11:
+        result = result + interp * radiance_internal(state["configs"][low + 1], theta, gamma) * \
+            state["radiances"][low + 1] * state["ecf"][low + 1]
+    return result
+
+
+def _rgb_to_hsv(r, g, b):
+    mn = np.minimum(np.minimum(r, g), b)
+    mx = np.maximum(np.maximum(r, g), b)
+    delta = mx - mn
+    grey = (delta < 1e-5) | (mx == 0.0)
+    safe = np.where(grey, 1.0, delta)
+    h = np.where(r >= mx, (g - b) / safe, np.where(g >= mx, 2.0 + (b - r) / safe, 4.0 + (r - g) / safe))
+    h = np.fmod(h / 6.0 + 1.0, 1.0)
+    s = np.where(grey, 0.0, delta / np.where(mx == 0.0, 1.0, mx))
+    return np.where(grey, 0.0, h), s, mx
+
+
+def _hsv_to_rgb(h, s, v):
+    h = h - np.floor(h)
+    hi = np.floor(h * 6).astype(np.int64)
+    f = h * 6 - hi
+    m, n, k = v * (1 - s), v * (1 - s * f), v * (1 - s * (1 - f))
+    table = [(v, k, m), (n, v, m), (m, v, k), (m, n, v), (k, m, v), (v, m, n)]
+    out = [np.zeros_like(h) for _ in range(3)]
+    for i, (a, b, c) in enumerate(table):
+        sel = hi == i
+        for ch, val in enumerate((a, b, c)):
+            out[ch] = np.where(sel, val, out[ch])
+    grey = s == 0
+    return [np.where(grey, v, o) for o in out]
+
+
+def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, sun_dir) -> np.ndarray:
+    """The sky texture without the solar disc: (height, width, 3) float64."""
+    bands = [unpack_state(states[b]) for b in range(BANDS)]
+    cmf = np.asarray(cmf, dtype=np.float64)
+    xs, ys, zs, centers, integral = cmf[:16], cmf[16:32], cmf[32:48], cmf[48:64], cmf[64]
+    yy, xx = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+    theta = math.pi * (yy + 0.5) / height
+    phi = 2 * math.pi * (xx + 0.5) / width
+    lower = theta >= 0.5 * math.pi
+    m_theta = np.where(lower, math.pi - theta, theta)
+    view = np.stack([-np.sin(phi) * np.sin(m_theta), np.cos(m_theta), np.cos(phi) * np.sin(m_theta)], axis=-1)
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    gamma = np.arccos(np.clip(view @ sd, -1.0, 1.0))
+    X = np.zeros_like(theta)
+    Y = np.zeros_like(theta)
+    Z = np.zeros_like(theta)
+    for b in range(BANDS):
+        wl = min(max(float(centers[b]), 320.0), 720.0)
+        v = sky_radiance(bands[b], m_theta, gamma, wl)
+        X += xs[b] * v
+        Y += ys[b] * v
+        Z += zs[b] * v
+    X, Y, Z = X / integral, Y / integral, Z / integral
+    r = 3.2404542 * X - 1.5371385 * Y - 0.4985314 * Z
+    g = -0.9692660 * X + 1.8760108 * Y + 0.0415560 * Z
+    bl = 0.0556434 * X - 0.2040259 * Y + 1.0572252 * Z
+    max_v = np.maximum(r, np.maximum(g, bl))
+    h, s, _ = _rgb_to_hsv(r / max_v, g / max_v, bl / max_v)
+    diff_angle = 2 * math.pi * np.fmod(h - 2.0 / 3 + 1.0, 1.0)
+    t_s = s * (0.5 * (1 + np.cos(diff_angle)))
+    s = (1 - t_s) * s + t_s
+    r, g, bl = (max_v * c for c in _hsv_to_rgb(h, s, np.ones_like(h)))
+    sea_b = (1 - sd[1]) * 0.01 + sd[1] * 0.1
+    sea = 0.5 * np.array([0.01, 0.01, sea_b])
+    t = np.where(lower, np.cos(m_theta) ** (1 / 5.0), 0.0)
+    out = np.stack([r, g, bl], axis=-1)
+    return np.where(lower[..., None], (1 - t)[..., None] * out + t[..., None] * sea, out)
