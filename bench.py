@@ -16,8 +16,9 @@ tracker instead of the persistent megakernel.
 
 `--impl reference` times the reference's per-path CPU algorithm on the host cores. The reference's
 own implementation (OptiX raygen + tiny-cuda-nn) cannot be built on this platform, so the arm runs
-the project's CPU restatement of it (the oracle), with all host threads, on a bounded sample of
-the same workload.
+the project's CPU restatement of it (the oracle), with all host threads, on whole 16-spp frames of
+the same workload. Its inputs (the fBm volume and the Hosek-Wilkie sky texture) are built on the
+host by the oracle as well: that arm loads no product library and touches no GPU.
 """
 from __future__ import annotations
 
@@ -115,6 +116,25 @@ def _cfg(name):
     return {"c1": C1, "c2": C2, "c5": C5}[name]
 
 
+def _mlp_tensor_pipe():
+    """Tensor-pipe utilisation of the MLP kernels recorded from an ncu capture in profiles/*.md
+    (lines `tensor_pipe_active[<kernel>]: <percent of peak, elapsed cycles>`)."""
+    out = {}
+    pat = re.compile(r"tensor_pipe_active\[(\w+)\]:\s*([0-9.]+)")
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for k, v in pat.findall(f.read_text()):
+            out[k] = {"pct_of_peak": float(v), "source": f.name}
+    return out
+
+
+def _config_dict(cfg, world: int, active_leaves: int, total_leaves: int) -> dict:
+    """The workload description both arms print (the same dict for the GPU arm and the CPU arm)."""
+    return {"workload": _workload_name(cfg), "spp_per_step": STEP_SPP,
+            "l2": f"GPU arm: flushed between steps ({L2_FLUSH_BYTES >> 20} MB write); CPU arm: not applicable",
+            "active_leaves": int(active_leaves), "total_leaves": int(total_leaves),
+            "parallelism": f"replicas x{world}"}
+
+
 def _workload_name(cfg):
     v = cfg.volume
     return (f"{cfg.name}: plain volumetric path tracing, {cfg.width}x{cfg.height}, {STEP_SPP} spp per step, "
@@ -159,21 +179,71 @@ def cpu_sample(cfg, vox: np.ndarray, env_rgb: np.ndarray | None, target_seconds:
 
 
 def scene_host_inputs(cfg):
-    """Dense volume and environment image of a configuration, generated by the product on the
-    GPU and copied to the host for the CPU legs."""
-    from rtc8_gb300.renderer import Renderer, setup_scene
+    """Dense volume and environment image of a configuration for the CPU legs, built on the host
+    by the oracle: its fBm generator (bit-identical to the device generator) and its float64
+    restatement of the Hosek-Wilkie sky texture. No product library is loaded."""
+    from oracle import orc
+    from oracle import sky as osky
+    from rtc8_gb300 import sky as psky
+    from rtc8_gb300.configs import sun_direction
 
-    r = Renderer(16, 16)
-    setup_scene(r, cfg)
-    vox = r.download_volume()
+    vox = orc.fbm_volume(cfg.volume)
     env = None
     if cfg.sky is not None:
-        env = r.download_environment(cfg.sky.width, cfg.sky.height)
+        st = psky.load_sky_state(cfg.sky, cfg.sun_elevation_deg)
+        d = sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg).astype(np.float32)
+        env = osky.sky_texture(cfg.sky.width, cfg.sky.height, st["states"], st["cmf"], d).astype(np.float32)
     elif cfg.env_constant is not None:
-        from rtc8_gb300.renderer import constant_environment
-        env = constant_environment(cfg.env_constant)
-    r.close()
+        env = np.full((32, 64, 3), cfg.env_constant, dtype=np.float32)
     return vox, env
+
+
+def leaf_counts(vox: np.ndarray) -> tuple[int, int]:
+    """Non-empty and total 8^3 leaves of a dense volume."""
+    lx, ly, lz = [(d + 7) // 8 for d in vox.shape]
+    pad = np.zeros((lx * 8, ly * 8, lz * 8), np.float32)
+    pad[:vox.shape[0], :vox.shape[1], :vox.shape[2]] = vox
+    active = pad.reshape(lx, 8, ly, 8, lz, 8).max(axis=(1, 3, 5)) > 0
+    return int(active.sum()), lx * ly * lz
+
+
+def reference_arm(args, cfg, world: int) -> dict:
+    """The CPU arm: the oracle's plain tracer (the reference's per-path algorithm restated in
+    host C++, OpenMP over image rows, all host threads) on whole frames of the workload, STEP_SPP
+    samples per pixel per step, timed step by step with the host clock."""
+    from oracle import orc
+
+    t_setup = time.perf_counter()
+    vox, env = scene_host_inputs(cfg)
+    active, total = leaf_counts(vox)
+    sc = orc.scene_from_config(cfg, vox, env)
+    del vox
+    rng = orc.seed_states(cfg.width, cfg.height, cfg.rng_seed)
+    sum_rgb = np.zeros((cfg.height, cfg.width, 3), dtype=np.float64)
+    mean_rgb = np.zeros((cfg.height, cfg.width, 3), dtype=np.float32)
+    threads = os.cpu_count() or 1
+    setup_s = time.perf_counter() - t_setup
+    step_s = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        orc.render_plain(sc, rng, STEP_SPP, accum_base=i * STEP_SPP, threads=threads, sum_rgb=sum_rgb,
+                         mean_rgb=mean_rgb)
+        step_s.append(time.perf_counter() - t0)
+    timed = step_s[args.warmup:] or step_s[-1:]
+    ms = 1000.0 * sum(timed) / len(timed)
+    paths = cfg.width * cfg.height * STEP_SPP
+    value = paths / (ms / 1000.0)
+    sample = (f"{len(timed)} timed frames of {cfg.width}x{cfg.height} x {STEP_SPP} spp of {cfg.name} after "
+              f"{args.warmup} untimed ones, oracle restatement with OpenMP; inputs built on the host by the "
+              f"oracle in {setup_s:.1f} s")
+    return {"impl": "reference", "metric": "paths/s (plain volumetric path tracing)", "value": value,
+            "unit": "paths/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded fBm volume and Hosek-Wilkie sky built on the host)",
+            "config": _config_dict(cfg, world, active, total),
+            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
 
 
 def mlp_bench(steps: int, warmup: int) -> dict:
@@ -329,6 +399,7 @@ def main():
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
     ap.add_argument("--no-nrc", action="store_true", help="skip the NRC-vs-plain equal-error comparison")
+    ap.add_argument("--no-mlp", action="store_true", help="skip the MLP kernel figures of the default line")
     ap.add_argument("--tracker", default="megakernel", choices=["megakernel", "wavefront"],
                     help="plain tracker: the persistent megakernel (default) or the wavefront form")
     ap.add_argument("--mlp", action="store_true",
@@ -338,14 +409,21 @@ def main():
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
 
-    import torch
-    import torch.distributed as dist
-
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        # Rank 0 alone runs the CPU arm; it needs neither a GPU nor a process group.
+        if rank == 0:
+            print(json.dumps(reference_arm(args, _cfg(args.config if args.config != "c4" else "c2"), world)),
+                  flush=True)
+        return
+
+    import torch
+    import torch.distributed as dist
+
     if world > 1:
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        dist.init_process_group("nccl")
     if args.config == "c4" and args.impl == "ours":
         if rank == 0:
             torch.cuda.set_device(local)
@@ -354,30 +432,6 @@ def main():
     cfg = _cfg(args.config if args.config != "c4" else "c1")
     if args.image:
         cfg = cfg.replace(width=args.image, height=args.image)
-    workload = _workload_name(cfg)
-
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        torch.cuda.set_device(local)
-        vox, env = scene_host_inputs(cfg)
-        vals = []
-        sample = None
-        for _ in range(args.warmup + args.steps):
-            s = cpu_sample(cfg, vox, env, target_seconds=max(2.0, 60.0 / max(1, args.warmup + args.steps)))
-            vals.append(s["value"])
-            sample = s
-        v = statistics.mean(vals[args.warmup:]) if args.steps else vals[-1]
-        line = {"impl": "reference", "metric": "paths/s (plain volumetric path tracing)", "value": v,
-                "unit": "paths/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1000.0 * cfg.width * cfg.height * STEP_SPP / v, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": workload},
-                "cpu_baseline": {"value": v, "unit": "paths/s", "cores": sample["cores"], "kind": "port",
-                                 "sample": sample["sample"]},
-                "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
 
     from rtc8_gb300.renderer import Renderer, setup_scene
 
@@ -456,45 +510,68 @@ def main():
     e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
     e2e_value = world * paths_per_rank / (e2e_total / 1000.0)
 
-    # ---- roofline of the tracer kernel (algorithmic bytes per launch / average launch time)
+    # ---- roofline of the tracer kernel (algorithmic bytes per launch / average launch time).
+    # Algorithmic unit of the tracking work: 32 B per density lookup (the 2x2x2 FP32 stencil),
+    # 120 B per path vertex (path state read and written once per vertex) and 48 B per sample
+    # (FP64 RGB accumulator read and written); lookups, vertices and samples from device counters.
     lookups_per_launch = cnt["lookups"] / args.steps
+    vertices_per_launch = cnt["vertices"] / args.steps
+    samples_per_launch = cnt["samples"] / args.steps
+    alg_bytes = 32.0 * lookups_per_launch + 120.0 * vertices_per_launch + 48.0 * samples_per_launch
+    launch_s = total_ms / args.steps / 1000.0
+    achieved = alg_bytes / launch_s / 1e9
     pixels = cfg.width * cfg.height
-    alg_bytes = 32.0 * lookups_per_launch + 88.0 * pixels
-    achieved = alg_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    # The persistent tracker keeps path state in registers, so the bytes it must move are fewer:
+    reg_bytes = 32.0 * lookups_per_launch + 88.0 * pixels
     peak, peak_kind = _peaks()
     traffic, prof = _profile_traffic("plain_trace_kernel", args.config)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs", "traffic_source": prof,
-                "algorithmic_bytes_per_launch": alg_bytes, "lookups_per_launch": lookups_per_launch}
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "algorithmic_unit": "32 B x lookups + 120 B x path vertices + 48 B x samples",
+                "lookups_per_launch": lookups_per_launch, "vertices_per_launch": vertices_per_launch,
+                "samples_per_launch": samples_per_launch,
+                "register_resident_state": {"bytes_per_launch": reg_bytes,
+                                            "achieved": reg_bytes / launch_s / 1e9,
+                                            "frac": reg_bytes / launch_s / 1e9 / peak,
+                                            "unit": "32 B x lookups + 88 B x pixels (PCG state, FP64 sum, "
+                                                    "FP32 mean)"}}
 
     # ---- radiance cache vs plain at equal error (NRC form of the 256x256 dense 64^3 configuration)
     nrc_cmp = None
     if rank == 0 and not args.no_nrc:
         from rtc8_gb300 import convergence
         from rtc8_gb300.configs import C1
-        res = convergence.compare(C1, target=1e-3, oracle_spp=16384, time_budget=60.0)
+        res = convergence.compare(C1, target=1e-3, oracle_spp=16384, time_budget=60.0, seeds=3,
+                                  extra_settings={"adam_lr_1e-2": {"learning_rate": 1e-2}})
         nrc_cmp = {k: v for k, v in res.items() if k != "curves"}
         nrc_cmp["workload"] = (f"{C1.name}: 256x256, dense fBm 64^3, sigma_t max {C1.volume.sigma_t_max}, "
                                f"albedo {C1.albedo}, HG g {C1.phase_param}, sun + constant env 0.5")
-        nrc_cmp["time"] = "GPU time of each estimator's launches (CUDA events), error evaluation excluded"
+        nrc_cmp["time"] = ("seconds: GPU time of each estimator's launches (CUDA events); wall_seconds: host "
+                           "wall clock around the same launches; error evaluation excluded from both")
+
+    mlp = None
+    if rank == 0 and not args.no_mlp:
+        mlp = mlp_bench(10, warmup)
+        mlp["tensor_pipe_ncu"] = _mlp_tensor_pipe()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         vox, env = scene_host_inputs(cfg)
         cpu = cpu_sample(cfg, vox, env, target_seconds=12.0)
+        del vox
 
     if rank == 0:
         line = {"metric": "paths/s (plain volumetric path tracing)", "value": value, "unit": "paths/s",
                 "n_gpus": world, "steps": args.steps, "warmup": warmup, "ms_per_step": total_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded fBm volume generated on the device)",
-                "config": {"workload": workload, "spp_per_step": STEP_SPP, "l2": "flushed between steps "
-                           f"({L2_FLUSH_BYTES >> 20} MB write)", "active_leaves": info["active_leaves"],
-                           "total_leaves": info["total_leaves"], "parallelism": f"replicas x{world}"},
+                "config": _config_dict(cfg, world, info["active_leaves"], info["total_leaves"]),
                 "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": args.steps * (3 if cfg.rng_stream_mode == 1 else 1),  # jump table, tracer, mean
                 "nrc_vs_plain": nrc_cmp,
+                "mlp": mlp,
                 "roofline": roofline,
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),

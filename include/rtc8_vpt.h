@@ -229,7 +229,22 @@ int vpt_launch_plain_logged(VptContext* ctx, void* stream, uint32_t spp, uint32_
  * call <= VPT_NOALLOC_MAX_SPP (larger requests fail with VPT_ERR_INVALID_ARGUMENT). All calls
  * share the one array, so calls that overlap on the GPU race. The first call with a device
  * current looks the array's address up (cudaGetSymbolAddress): make it before any stream
- * capture. Work counters and device error bits of these launches are not reported. */
+ * capture. The address is looked up again when the device's current context changes (after
+ * cudaDeviceReset, for instance). Device error bits (VPT_DEVERR_*: a segment's step cap, a
+ * non-finite sample) are ORed into `device_errors` when the caller gives that word; work
+ * counters of these launches are not reported.
+ *
+ * Buffer layouts (the ones a VptContext builds; x is the slowest axis everywhere):
+ *   leaf_table   lx*ly*lz int32 slots (lx = ceil(nx / 8), the same for y and z), the slot of
+ *                leaf cell (cx, cy, cz) at (cx*ly + cy)*lz + cz; -1 = empty leaf (density 0)
+ *   leaf_values  512 floats per non-empty slot, voxel (x, y, z) of the leaf at x<<6 | y<<3 | z
+ *   majorants    mx*my*mz floats, cell (cx, cy, cz) at (cx*my + cy)*mz + cz; a cell covers
+ *                2^max(3, majorant_cell_log2) voxels per axis and holds the max density over
+ *                its voxels plus one voxel below and two above on each axis
+ *   env_texels   env_h rows of env_w float4 (R, G, B, unused), row y = polar angle from +y
+ *   imp_mips     num_mips levels back to back, level l = max(map_w>>l, 1) x max(map_h>>l, 1)
+ *                floats, row-major; level 0 is the map_w x map_h importance map and the last
+ *                level is 1x1 (map_w, map_h: the next powers of two of env_w, env_h). */
 #define VPT_NOALLOC_MAX_SPP 4096u
 typedef struct VptNoAllocTrace {
     VptFrameParams frame;
@@ -253,6 +268,7 @@ typedef struct VptNoAllocTrace {
     uint64_t* rng;              /* width*height seed states */
     double* sum_rgb;            /* 3 per pixel */
     float* mean_rgb;            /* 3 per pixel */
+    uint32_t* device_errors;    /* optional device word receiving VPT_DEVERR_* bits, or NULL */
 } VptNoAllocTrace;
 int vpt_launch_plain_noalloc(const VptNoAllocTrace* args, void* stream);
 /* ---- image output -------------------------------------------------------------------- */

@@ -13,7 +13,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "liboracle.so"
-SRCS = [HERE / "vpt_oracle.cpp", HERE / "nrc_oracle.cpp", HERE / "nrc_setup_oracle.cpp"]
+SRCS = [HERE / "vpt_oracle.cpp", HERE / "nrc_oracle.cpp", HERE / "nrc_setup_oracle.cpp", HERE / "scene_oracle.cpp"]
 FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 
 

@@ -5,9 +5,10 @@
 # under tests/golden/ and rtc8_gb300/data/ by tests/golden/make_golden.py.
 #
 #   REF=<path to the reference checkout> oracle/build_ref.sh
+# (without REF: a checkout named "reference" next to this repository)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${REF:-/root/reference}"
+REF="${REF:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 if [[ ! -d "$REF/common" ]]; then
     echo "reference checkout not found at $REF" >&2

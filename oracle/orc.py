@@ -133,6 +133,23 @@ def tonemap(mean_rgb: np.ndarray, brightness: float = 1.0, srgb: bool = True) ->
     return out, rgba
 
 
+def fbm_volume(spec) -> np.ndarray:
+    """Dense fBm volume of a rtc8_gb300.configs.VolumeSpec built on the host (oracle/scene_oracle.cpp),
+    bit-identical to the device generator."""
+    L = lib()
+    fn = L.orc_fbm_volume
+    fn.restype = None
+    fn.argtypes = [C.c_int32, C.c_uint32, C.c_int64, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, f32p,
+                   f32p]
+    n = spec.n
+    out = np.empty((n, n, n), dtype=np.float32)
+    scratch = np.empty((n, n, n), dtype=np.float32) if spec.union_seed is not None else None
+    fn(n, spec.seed & 0xFFFFFFFF, -1 if spec.union_seed is None else int(spec.union_seed), spec.octaves,
+       spec.lacunarity, spec.gain, spec.base_frequency, spec.threshold, p(out, C.c_float),
+       p(scratch, C.c_float) if scratch is not None else None)
+    return out
+
+
 def pool_cells(cells: np.ndarray, factor: int) -> np.ndarray:
     """Majorant cells of `factor`^3 times the volume (max-pooling, ragged edges included)."""
     cx, cy, cz = cells.shape

@@ -20,14 +20,27 @@ import numpy as np
 BANDS = 16
 
 
-def radiance_internal(cfg, theta, gamma):
+class Angles:
+    """View angles of a batch of texels with the trigonometric terms the radiance formula reuses."""
+
+    def __init__(self, theta, gamma):
+        self.theta = np.asarray(theta, dtype=np.float64)
+        self.gamma = np.asarray(gamma, dtype=np.float64)
+        self.cos_t = np.cos(self.theta)
+        self.cos_g = np.cos(self.gamma)
+        self.cos_g2 = self.cos_g ** 2
+        self.zenith = np.sqrt(self.cos_t)
+        self.inv_ct = 1.0 / (self.cos_t + 0.01)
+
+
+def radiance_internal(cfg, theta, gamma, ang: "Angles | None" = None):
     """ArHosekSkyModel_GetRadianceInternal for one configuration (9 values)."""
-    exp_m = np.exp(cfg[4] * gamma)
-    ray_m = np.cos(gamma) ** 2
-    mie_m = (1.0 + np.cos(gamma) ** 2) / (1.0 + cfg[8] ** 2 - 2.0 * cfg[8] * np.cos(gamma)) ** 1.5
-    zenith = np.sqrt(np.cos(theta))
-    return (1.0 + cfg[0] * np.exp(cfg[1] / (np.cos(theta) + 0.01))) * (
-        cfg[2] + cfg[3] * exp_m + cfg[5] * ray_m + cfg[6] * mie_m + cfg[7] * zenith)
+    a = ang if ang is not None else Angles(theta, gamma)
+    exp_m = np.exp(cfg[4] * a.gamma)
+    ray_m = a.cos_g2
+    mie_m = (1.0 + a.cos_g2) / (1.0 + cfg[8] ** 2 - 2.0 * cfg[8] * a.cos_g) ** 1.5
+    return (1.0 + cfg[0] * np.exp(cfg[1] * a.inv_ct)) * (
+        cfg[2] + cfg[3] * exp_m + cfg[5] * ray_m + cfg[6] * mie_m + cfg[7] * a.zenith)
 
 
 def unpack_state(state: np.ndarray) -> dict:
@@ -36,18 +49,19 @@ def unpack_state(state: np.ndarray) -> dict:
     return {"configs": s[:99].reshape(11, 9), "radiances": s[99:110], "ecf": s[110:121], "solar_radius": s[121]}
 
 
-def sky_radiance(state: dict, theta, gamma, wavelength: float):
+def sky_radiance(state: dict, theta, gamma, wavelength: float, ang: "Angles | None" = None):
     """arhosekskymodel_radiance: the sky (no solar disc) at one wavelength in nm."""
     low = int((wavelength - 320.0) / 40.0)
     if low < 0 or low >= 11:
         return np.zeros_like(np.asarray(theta, dtype=np.float64))
+    a = ang if ang is not None else Angles(theta, gamma)
     interp = math.fmod((wavelength - 320.0) / 40.0, 1.0)
-    val_low = radiance_internal(state["configs"][low], theta, gamma) * state["radiances"][low] * state["ecf"][low]
+    val_low = radiance_internal(state["configs"][low], theta, gamma, a) * state["radiances"][low] * state["ecf"][low]
     if interp < 1e-6:
         return val_low
     result = (1.0 - interp) * val_low
     if low + 1 < 11:
-        result = result + interp * radiance_internal(state["configs"][low + 1], theta, gamma) * \
+        result = result + interp * radiance_internal(state["configs"][low + 1], theta, gamma, a) * \
             state["radiances"][low + 1] * state["ecf"][low + 1]
     return result
 
@@ -95,9 +109,10 @@ def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, su
     X = np.zeros_like(theta)
     Y = np.zeros_like(theta)
     Z = np.zeros_like(theta)
+    ang = Angles(m_theta, gamma)
     for b in range(BANDS):
         wl = min(max(float(centers[b]), 320.0), 720.0)
-        v = sky_radiance(bands[b], m_theta, gamma, wl)
+        v = sky_radiance(bands[b], m_theta, gamma, wl, ang)
         X += xs[b] * v
         Y += ys[b] * v
         Z += zs[b] * v

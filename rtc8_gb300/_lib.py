@@ -66,6 +66,7 @@ class VptNoAllocTrace(C.Structure):
         ("imp_mips", C.c_void_p), ("map_w", C.c_int32), ("map_h", C.c_int32), ("num_mips", C.c_int32),
         ("imp_integral", C.c_float),
         ("rng", C.c_void_p), ("sum_rgb", C.c_void_p), ("mean_rgb", C.c_void_p),
+        ("device_errors", C.c_void_p),
     ]
 
 

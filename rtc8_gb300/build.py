@@ -24,7 +24,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-Xptxas", "-warn-spills"]
 # Units whose float arithmetic must follow the reference's operation order: no FMA contraction,
 # so products and sums round as in the oracle's restatement (compiled with -ffp-contract=off).
-NO_FMA_UNITS = {"vpt_tracer.cu", "vpt_post.cu", "vpt_wavefront.cu"}
+# The scene unit is among them so that the seeded fBm volumes equal the host generator's bit for bit.
+NO_FMA_UNITS = {"vpt_tracer.cu", "vpt_post.cu", "vpt_wavefront.cu", "vpt_scene.cu"}
 # The tracker units use the reference's own device arithmetic: it compiles its path-tracing
 # programs and kernels with --use_fast_math (renderer/CMakeLists.txt:48, 65, 91), i.e. intrinsic
 # transcendentals, approximate division and square root, denormals flushed. FMA contraction,

@@ -11,7 +11,10 @@
 //
 // The array is shared by all calls: calls that overlap on the GPU (different streams, or
 // threads) race on it. Its address is looked up with cudaGetSymbolAddress on the first call
-// made with a device current, so make that first call before any stream capture.
+// made with a device current, so make that first call before any stream capture. The address
+// belongs to the context it was looked up in: when the current context of the device changes
+// (for instance after cudaDeviceReset), the next call looks it up again.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,22 +37,57 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+    unsigned long long context_id;  // unique id of the context the address was looked up in
+    unsigned char* ptr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (looked up once per device).
+// Driver entry points reached through the runtime (the library does not link libcuda).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Unique id of the calling thread's current context; false when none is current yet.
+bool current_context_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+            return false;
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(b);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of the scratch array in the current device's current context (looked up once
+// per device and context).
 int scratch_address(unsigned char** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return ctx_set_error(VPT_ERR_CUDA, "vpt_launch_plain_noalloc: no usable current device");
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    ScratchSlot& slot = g_scratch[dev];
+    unsigned long long id = 0;
+    const bool have_id = current_context_id(&id);
+    if (!slot.ptr || !have_id || slot.context_id != id) {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the primary context current
         if (e != cudaSuccess || !p)
             return ctx_set_error(VPT_ERR_CUDA, "vpt_launch_plain_noalloc: cudaGetSymbolAddress of the scratch failed");
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        if (!current_context_id(&id))
+            return ctx_set_error(VPT_ERR_CUDA, "vpt_launch_plain_noalloc: no current context after the set-up");
+        slot.ptr = static_cast<unsigned char*>(p);
+        slot.context_id = id;
     }
-    *out = g_scratch_ptr[dev];
+    *out = slot.ptr;
     return VPT_OK;
 }
 
@@ -162,7 +200,8 @@ extern "C" int vpt_launch_plain_noalloc(const VptNoAllocTrace* a, void* stream) 
     tp.mean_rgb = a->mean_rgb;
     tp.work_counter = reinterpret_cast<unsigned int*>(scratch);
     tp.counters = reinterpret_cast<unsigned long long*>(scratch + 8);
-    tp.error_flags = reinterpret_cast<unsigned int*>(scratch + 72);
+    // Error bits go to the caller's word when one is given (ORed in; the caller clears it).
+    tp.error_flags = a->device_errors ? a->device_errors : reinterpret_cast<unsigned int*>(scratch + 72);
     ulonglong2* jumps = reinterpret_cast<ulonglong2*>(scratch + kScratchHeader);
     tp.sample_jumps = jumps;
 

@@ -26,6 +26,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -351,20 +353,43 @@ int parse_file_header(FILE* f, uint64_t grid_index, VptNanoVdbInfo* info) {
     return VPT_OK;
 }
 
+// Host memory the flattened grid may take: at most 2^26 leaves (128 GiB of values, more than one
+// GPU holds) over at most 2^30 leaf cells (4 GiB of table).
+constexpr int64_t kMaxFlatLeaves = int64_t(1) << 26;
+constexpr int64_t kMaxLeafCells = int64_t(1) << 30;
+
+// Runs an ABI body so that no C++ exception crosses the C boundary: host allocation failures
+// become VPT_ERR_OUT_OF_MEMORY, anything else VPT_ERR_INVALID_ARGUMENT.
+template <class F>
+int guarded(const char* what, F&& body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail(VPT_ERR_OUT_OF_MEMORY, std::string(what) + ": out of host memory");
+    } catch (const std::exception& e) {
+        return fail(VPT_ERR_INVALID_ARGUMENT, std::string(what) + ": " + e.what());
+    } catch (...) {
+        return fail(VPT_ERR_INVALID_ARGUMENT, std::string(what) + ": unexpected error");
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
 int vpt_nvdb_file_info(const char* path, uint64_t grid_index, VptNanoVdbInfo* info) {
     if (!path || !info) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nvdb_file_info: bad arguments");
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return fail(VPT_ERR_INVALID_ARGUMENT, std::string("vpt_nvdb_file_info: cannot open ") + path);
-    int rc = parse_file_header(f, grid_index, info);
-    std::fclose(f);
-    return rc;
+    return guarded("vpt_nvdb_file_info", [&] {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) return fail(VPT_ERR_INVALID_ARGUMENT, std::string("vpt_nvdb_file_info: cannot open ") + path);
+        int rc = parse_file_header(f, grid_index, info);
+        std::fclose(f);
+        return rc;
+    });
 }
 
 int vpt_nanovdb_grid_info(const void* grid, uint64_t bytes, VptNanoVdbInfo* info) {
+    return guarded("vpt_nanovdb_grid_info", [&] {
     if (!info) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nanovdb_grid_info: null info");
     Parsed g;
     int rc = parse_grid(grid, bytes, &g);
@@ -376,10 +401,12 @@ int vpt_nanovdb_grid_info(const void* grid, uint64_t bytes, VptNanoVdbInfo* info
         info->flat_leaves = flatten(s, g, [](int64_t, const int32_t*, const float*, float) {});
     }
     return VPT_OK;
+    });
 }
 
 int vpt_nanovdb_decode_leaves(const void* grid, uint64_t bytes, int64_t capacity, int32_t* leaf_origins,
                               float* leaf_values, int64_t* count) {
+    return guarded("vpt_nanovdb_decode_leaves", [&] {
     if (!count) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nanovdb_decode_leaves: null count");
     Parsed g;
     int rc = parse_grid(grid, bytes, &g);
@@ -404,9 +431,11 @@ int vpt_nanovdb_decode_leaves(const void* grid, uint64_t bytes, int64_t capacity
         }
     });
     return VPT_OK;
+    });
 }
 
 int vpt_set_volume_nanovdb(VptContext* c, const void* grid, uint64_t bytes) {
+    return guarded("vpt_set_volume_nanovdb", [&] {
     if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nanovdb: null context");
     Parsed g;
     int rc = parse_grid(grid, bytes, &g);
@@ -416,9 +445,14 @@ int vpt_set_volume_nanovdb(VptContext* c, const void* grid, uint64_t bytes) {
     sample_extent(g.info, lo, hi);
     const int32_t lx = (hi[0] - lo[0]) / 8, ly = (hi[1] - lo[1]) / 8, lz = (hi[2] - lo[2]) / 8;
     const int64_t cells = static_cast<int64_t>(lx) * ly * lz;
-    if (cells > (int64_t(1) << 31) - 1) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nanovdb: grid too large");
+    if (cells > kMaxLeafCells)
+        return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nanovdb: grid too large (" + std::to_string(cells) +
+                                                  " leaf cells, at most 2^30)");
     Span s{static_cast<const uint8_t*>(grid), bytes};
     const int64_t n = flatten(s, g, [](int64_t, const int32_t*, const float*, float) {});
+    if (n > kMaxFlatLeaves)
+        return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nanovdb: grid too large (" + std::to_string(n) +
+                                                  " leaves, at most 2^26)");
     std::vector<int32_t> table(static_cast<size_t>(cells), -1);
     std::vector<int32_t> origins(static_cast<size_t>(3 * n));
     std::vector<float> values(static_cast<size_t>(512 * std::max<int64_t>(n, 1)));
@@ -436,9 +470,11 @@ int vpt_set_volume_nanovdb(VptContext* c, const void* grid, uint64_t bytes) {
     });
     if (dup) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nanovdb: two nodes cover the same 8^3 cell");
     return vpt::upload_sparse_grid(c, table, lx, ly, lz, origins, values.data(), n, lo, g.info);
+    });
 }
 
 int vpt_set_volume_nvdb_file(VptContext* c, const char* path, uint64_t grid_index) {
+    return guarded("vpt_set_volume_nvdb_file", [&] {
     if (!c || !path) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nvdb_file: bad arguments");
     FILE* f = std::fopen(path, "rb");
     if (!f) return fail(VPT_ERR_INVALID_ARGUMENT, std::string("vpt_set_volume_nvdb_file: cannot open ") + path);
@@ -461,6 +497,7 @@ int vpt_set_volume_nvdb_file(VptContext* c, const char* path, uint64_t grid_inde
     std::fclose(f);
     if (!ok) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_set_volume_nvdb_file: truncated grid payload");
     return vpt_set_volume_nanovdb(c, buf.data(), buf.size());
+    });
 }
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 """Regenerates the golden fixtures from programs built against the reference's own sources.
 
-Run in a checkout that has the reference next to it (REF, default /root/reference):
+Run with the reference checkout in REF (default: a checkout named "reference" next to this
+repository):
 
     python tests/golden/make_golden.py
 
@@ -42,6 +43,7 @@ def run(name: str, *args: str) -> dict:
 
 def main() -> int:
     env = dict(os.environ)
+    env.setdefault("REF", str(ROOT.parent / "reference"))
     subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh")], check=True, env=env)
     basic = run("ref_kat_basic")
     (GOLDEN / "ref_basic_types.json").write_text(json.dumps(basic))

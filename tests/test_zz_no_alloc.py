@@ -113,3 +113,51 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(cuda_device):
     assert lib.vpt_launch_plain_noalloc(C.byref(args), None) == -1
     assert b"VPT_NOALLOC_MAX_SPP" in lib.vpt_last_error()
     r.close()
+
+
+def test_noalloc_reports_device_errors_in_the_callers_word(cuda_device):
+    """A segment that hits its step cap sets VPT_DEVERR_STEP_CAP in the caller's error word, as
+    vpt_get_device_errors reports it for a context launch."""
+    import torch
+
+    from ._scenes import small_reference_mode
+
+    cfg = small_reference_mode(size=16, n=16, sigma=60.0).replace(max_steps_per_segment=3)
+    vox = volume_for(cfg)
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg, volume=vox)
+    args, bufs = _caller_buffers(r, cfg, vox)
+    word = torch.zeros(1, dtype=torch.int32, device="cuda")
+    args.device_errors = word.data_ptr()
+    args.spp = 2
+    lib = _lib.load()
+    assert lib.vpt_launch_plain_noalloc(C.byref(args), None) == 0, lib.vpt_last_error()
+    r.launch_plain(2)
+    torch.cuda.synchronize()
+    assert r.device_errors() & 0x1
+    assert int(word.item()) == r.device_errors()
+    r.close()
+
+
+def test_noalloc_leaves_device_memory_unchanged(cuda_device):
+    """After the first call (which looks the scratch address up), further calls change the
+    device's free memory by nothing."""
+    import torch
+
+    cfg = small_config_mode(size=24, n=24)
+    vox = volume_for(cfg)
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg, volume=vox)
+    args, bufs = _caller_buffers(r, cfg, vox)
+    lib = _lib.load()
+    args.spp = 2
+    assert lib.vpt_launch_plain_noalloc(C.byref(args), None) == 0, lib.vpt_last_error()
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for call in range(1, 4):
+        args.accum_base, args.stream_base = 2 * call, 2 * call
+        assert lib.vpt_launch_plain_noalloc(C.byref(args), None) == 0, lib.vpt_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert bufs["sum"].sum().item() > 0
+    r.close()
