@@ -37,6 +37,15 @@ extern "C" {
 #define NRC_ENCODING_VOLUME 1      /* sin/cos 12 frequencies on position, OneBlob(32) on the
                                       outgoing direction (theta, phi), identity on the local
                                       density (roughness slot) and albedo (diffuse.r) */
+#define NRC_ENCODING_HASHGRID 2    /* the reference's default (network_interface.cu:99-122):
+                                      multiresolution hash grid on position (16 levels x 2
+                                      features, 2^15 entries per level, base resolution 16,
+                                      per-level scale 2; positions clamped to [0,1]^3), then
+                                      OneBlob(4) and identity as NRC_ENCODING_REFERENCE. The
+                                      tables are trained parameters: they follow the MLP
+                                      matrices in nrc_get_params / nrc_set_params /
+                                      nrc_get_gradients (level by level, entry by entry, two
+                                      features per entry) */
 
 #define NRC_OUTPUT_NONE 0          /* reference: output_activation None */
 #define NRC_OUTPUT_EXP 1
@@ -75,7 +84,8 @@ int nrc_infer_indexed(NrcHandle* h, void* stream, const float* in, const uint32_
 int nrc_train(NrcHandle* h, void* stream, const float* in, const float* target, uint32_t n, float* loss_or_null);
 
 /* Parameter access (FP32 master weights, layer by layer, each layer row-major
- * [out][in] with the padded sizes reported by nrc_get_layout). */
+ * [out][in] with the padded sizes reported by nrc_get_layout; with NRC_ENCODING_HASHGRID the
+ * hash-grid tables follow the last layer, and total_params counts them). */
 int nrc_get_layout(NrcHandle* h, int32_t* num_layers, int32_t* in_dims, int32_t* out_dims, int64_t* total_params);
 int nrc_get_params(NrcHandle* h, float* host_params);
 int nrc_set_params(NrcHandle* h, const float* host_params);

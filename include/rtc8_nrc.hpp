@@ -8,9 +8,9 @@
  * the caller owns the device buffers (14-float RadianceQuery inputs, 3-float outputs), calls
  * are asynchronous on `stream`, and a non-null lossOnCPU makes train() synchronise and return
  * the batch loss. Errors throw std::runtime_error carrying nrc_last_error(), as tiny-cuda-nn
- * threw from inside the reference's implementation. PositionEncoding::HashGrid (the reference's
- * default multiresolution hash grid) is not implemented and throws from initialize();
- * PositionEncoding::TriangleWave selects the reference's TriangleWave + OneBlob encoding.
+ * threw from inside the reference's implementation. PositionEncoding::HashGrid selects the
+ * reference's default multiresolution hash grid + OneBlob encoding (renderer_scene.cpp:50 calls
+ * initialize(HashGrid, 2, 0.01f)); PositionEncoding::TriangleWave the TriangleWave + OneBlob one.
  * initialize(const NrcConfig&) is an addition that selects any configuration of rtc8_nrc.h
  * (for example the volume encoding).
  */
@@ -50,10 +50,9 @@ public:
 
     // network_interface.cu:50-134: encoding, hidden layers of 64, Adam learning rate.
     void initialize(PositionEncoding posEnc, uint32_t numHiddenLayers, float learningRate) {
-        if (posEnc == PositionEncoding::HashGrid)
-            throw std::runtime_error("NeuralRadianceCache::initialize: the HashGrid encoding is not implemented");
         NrcConfig cfg;
-        nrc_default_config(NRC_ENCODING_REFERENCE, &cfg);
+        nrc_default_config(posEnc == PositionEncoding::HashGrid ? NRC_ENCODING_HASHGRID : NRC_ENCODING_REFERENCE,
+                           &cfg);
         cfg.num_hidden_layers = static_cast<int32_t>(numHiddenLayers);
         cfg.learning_rate = learningRate;
         initialize(cfg);

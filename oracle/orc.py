@@ -278,7 +278,8 @@ def render_plain(sc: OracleScene, rng: np.ndarray, spp: int, accum_base: int = 0
 _NRC_FUNCS = {
     "orc_nrc_in_dim": (C.c_int, [C.c_int]),
     "orc_nrc_num_params": (C.c_int64, [C.c_int, C.c_int]),
-    "orc_nrc_encode": (None, [C.c_int, f32p, C.c_int, f32p]),
+    "orc_nrc_encode": (None, [C.c_int, f32p, C.c_int, f32p, f32p]),
+    "orc_nrc_grid_params": (C.c_int64, []),
     "orc_nrc_forward": (None, [C.c_int, C.c_int, C.c_int, f32p, f32p, C.c_int, f32p]),
     "orc_nrc_loss_grad": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_float, f32p, f32p, f32p, C.c_int, f32p]),
     "orc_adam": (None, [f32p, f32p, f32p, f32p, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
@@ -295,13 +296,19 @@ def nrc_lib():
     return L
 
 
-def nrc_encode(encoding: int, queries: np.ndarray) -> np.ndarray:
+def nrc_encode(encoding: int, queries: np.ndarray, grid: np.ndarray | None = None) -> np.ndarray:
+    """Encoded inputs; `grid` = the hash-grid tables (encoding 2: the parameters after the MLP's)."""
     q = np.ascontiguousarray(queries, np.float32)
     n = len(q)
     d = nrc_lib().orc_nrc_in_dim(encoding)
     out = np.zeros((n, d), np.float32)
-    nrc_lib().orc_nrc_encode(encoding, p(q, C.c_float), n, p(out, C.c_float))
+    g = None if grid is None else np.ascontiguousarray(grid, np.float32)
+    nrc_lib().orc_nrc_encode(encoding, p(q, C.c_float), n, p(out, C.c_float), None if g is None else p(g, C.c_float))
     return out
+
+
+def nrc_grid_params() -> int:
+    return int(nrc_lib().orc_nrc_grid_params())
 
 
 def nrc_forward(encoding: int, hidden: int, out_act: int, params: np.ndarray, queries: np.ndarray) -> np.ndarray:

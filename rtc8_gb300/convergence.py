@@ -120,7 +120,7 @@ def plain_curve(cfg: SceneConfig, ref: np.ndarray, target: float, chunk_spp: int
 def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None, spp_per_frame: int = 8,
               eval_every: int = 1, max_frames: int = 4096, time_budget: float = 60.0,
               query_density: bool = True, termination: float = 0.0, warmup_frames: int = 0,
-              train_termination: float = 0.0) -> dict:
+              train_termination: float = 0.0, train_iterations: int = 1) -> dict:
     """relMSE of the radiance-cache renderer after every `eval_every` frames of `spp_per_frame`
     samples per pixel (the reference renders 8 samples per frame, renderer_main.cpp:359). The
     images of the first frame and of `warmup_frames` more frames (rendered while the cache is
@@ -149,7 +149,7 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
     while frames < max_frames and time.perf_counter() - wall0 < time_budget:
         def run():
             for _ in range(eval_every):
-                r.nrc_frame(cache, 1, spp_per_frame, False, s.cuda_stream)
+                r.nrc_frame(cache, train_iterations, spp_per_frame, False, s.cuda_stream)
         dt, dw = _timed(s, run)
         t, wall, frames = t + dt, wall + dw, frames + eval_every
         img = r.image()
@@ -186,7 +186,7 @@ def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, tim
     plain = plain_curve(cfg, ref, target, time_budget=time_budget)
     cache = nrc_curve(cfg, ref, target, net_config=net, spp_per_frame=st["spp_per_frame"], time_budget=time_budget,
                       termination=st["termination"], train_termination=st.get("train_termination", 0.0),
-                      max_frames=max(16, 16384 // st["spp_per_frame"]))
+                      train_iterations=st.get("train_iterations", 1), max_frames=max(16, 16384 // st["spp_per_frame"]))
     out = {"rng_seed": cfg.rng_seed,
            "plain": {"reached": plain["reached"], "first_below": plain["first_below"],
                      "last": plain["curve"][-1] if plain["curve"] else None},

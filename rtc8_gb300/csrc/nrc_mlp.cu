@@ -1,6 +1,9 @@
 // Neural radiance cache: a fully fused FP16 MLP (64-wide hidden layers, ReLU, no biases) on the
 // Blackwell tensor cores. Replaces tiny-cuda-nn's FullyFusedMLP + encodings + Trainer
-// (renderer/network_interface.cu:50-192).
+// (renderer/network_interface.cu:50-192), including the reference's default position encoding,
+// the multiresolution hash grid (network_interface.cu:99-122), whose tables are gathered into the
+// first layer's operand tile, trained by a scatter-add of the first layer's input gradient, and
+// updated by the same Adam / EMA kernel as the weights.
 //
 // One CTA of 128 threads works on 128-row tiles (one thread per row): the encoded input tile
 // and every hidden activation tile are FP16 in shared memory (core-matrix layout, nrc_tc.cuh),
@@ -44,6 +47,14 @@ constexpr int kOutPad = 16;
 constexpr int kMaxMats = 8;
 constexpr float kPiF = 3.14159265358979323846f;
 
+// Multiresolution hash grid of the reference's HashGrid option (network_interface.cu:99-109):
+// 16 levels of 2 features, at most 2^15 entries per level, base resolution 16, per-level scale 2.
+constexpr int kGridLevels = 16;
+constexpr int kGridFeatures = 2;
+constexpr uint32_t kGridMaxEntries = 1u << 15;
+constexpr float kGridBaseResolution = 16.0f;
+constexpr float kGridLog2PerLevelScale = 1.0f;  // log2(2)
+
 // Network shape: matrix j maps in[j] -> out[j] features; matrix 0 reads the encoded input.
 struct NetLayout {
     int enc;
@@ -53,17 +64,46 @@ struct NetLayout {
     int in[kMaxMats], out[kMaxMats];
     int poff[kMaxMats];    // FP32 parameter offset of matrix j
     uint32_t boff[kMaxMats];  // byte offset of matrix j in the FP16 weight image
-    int nparams;
+    int nparams;           // MLP weights; hash-grid parameters follow them in the parameter vector
     uint32_t blob_bytes;
     int out_act;
     float loss_scale;
+    // Hash grid (NRC_ENCODING_HASHGRID only): level l holds grid_size[l] entries of two features,
+    // entries grid_off[l] .. grid_off[l] + grid_size[l] of the table image; a lattice point of the
+    // level's grid_res^3 lattice is stored densely or hashed (bit l of grid_hashed).
+    int grid_params;       // 2 x entries, 0 without the hash grid
+    uint32_t grid_off[kGridLevels], grid_size[kGridLevels], grid_res[kGridLevels];
+    float grid_scale[kGridLevels];
+    uint32_t grid_hashed;
 };
+
+// Level geometry of the hash grid: scale 16 * 2^l - 1, resolution ceil(scale) + 1, table size
+// min(resolution^3 rounded up to a multiple of 8, 2^15), hashed when the lattice outgrows it.
+void grid_layout(NetLayout& l) {
+    uint32_t off = 0;
+    l.grid_hashed = 0;
+    for (int lv = 0; lv < kGridLevels; ++lv) {
+        const float scale = std::exp2(static_cast<float>(lv) * kGridLog2PerLevelScale) * kGridBaseResolution - 1.0f;
+        const uint32_t res = static_cast<uint32_t>(std::ceil(scale)) + 1u;
+        const uint64_t cells = static_cast<uint64_t>(res) * res * res;
+        const uint64_t padded = (cells + 7) / 8 * 8;
+        const uint32_t size = static_cast<uint32_t>(std::min<uint64_t>(padded, kGridMaxEntries));
+        l.grid_scale[lv] = scale;
+        l.grid_res[lv] = res;
+        l.grid_size[lv] = size;
+        l.grid_off[lv] = off;
+        if (cells > size) l.grid_hashed |= 1u << lv;
+        off += size;
+    }
+    l.grid_params = static_cast<int>(off) * kGridFeatures;
+}
 
 NetLayout make_layout(int enc, int hidden, int out_act, float loss_scale) {
     NetLayout l{};
     l.enc = enc;
-    l.in_dim = enc == NRC_ENCODING_REFERENCE ? 64 : 144;
-    l.in_real = enc == NRC_ENCODING_REFERENCE ? 62 : 138;
+    l.in_dim = enc == NRC_ENCODING_VOLUME ? 144 : 64;
+    l.in_real = enc == NRC_ENCODING_VOLUME ? 138 : (enc == NRC_ENCODING_HASHGRID ? 58 : 62);
+    if (enc == NRC_ENCODING_HASHGRID) grid_layout(l);
     l.L = hidden + 1;
     int po = 0;
     uint32_t bo = 0;
@@ -188,8 +228,108 @@ __device__ __forceinline__ void encode_row_volume(const float* q, uint8_t* tile,
     store8(tile, r, 17, K, last);
 }
 
-__device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* tile, int r, int K) {
-    if (enc == NRC_ENCODING_REFERENCE) {
+// The 8 lattice corners of a position in hash-grid level `lv`: table entries (feature pairs) and
+// trilinear weights. pos = scale x + 1/2 (one rounding), corner c takes floor(pos) + bit d of c
+// on axis d with weight frac or 1 - frac; dense levels index x + y res + z res^2, hashed levels
+// x ^ 2654435761 y ^ 805459861 z (the published spatial hash of the multiresolution hash
+// encoding, Mueller et al. 2022), both modulo the level's table size.
+__device__ __forceinline__ void grid_corners(const NetLayout& ly, int lv, const float* p, uint32_t (&e)[8],
+                                             float (&w)[8]) {
+    const float scale = ly.grid_scale[lv];
+    const uint32_t res = ly.grid_res[lv], size = ly.grid_size[lv], off = ly.grid_off[lv];
+    const bool hashed = (ly.grid_hashed >> lv) & 1u;
+    float fr[3];
+    uint32_t g[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float pos = fmaf(scale, p[d], 0.5f);
+        const float fl = floorf(pos);
+        fr[d] = pos - fl;
+        g[d] = static_cast<uint32_t>(static_cast<int>(fl));
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t x = g[0] + (c & 1), y = g[1] + ((c >> 1) & 1), z = g[2] + ((c >> 2) & 1);
+        const float wx = (c & 1) ? fr[0] : 1.0f - fr[0];
+        const float wy = (c & 2) ? fr[1] : 1.0f - fr[1];
+        const float wz = (c & 4) ? fr[2] : 1.0f - fr[2];
+        w[c] = (wx * wy) * wz;
+        const uint32_t i = hashed ? (x ^ (y * 2654435761u) ^ (z * 805459861u)) : (x + (y + z * res) * res);
+        e[c] = off + i % size;
+    }
+}
+
+// Hash-grid position in [0, 1]^3 (positions outside the world box are clamped to it).
+__device__ __forceinline__ void grid_position(const float* q, float (&p)[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p[d] = fminf(fmaxf(q[d], 0.0f), 1.0f);
+}
+
+// NRC_ENCODING_HASHGRID (64 features): levels 0..15 x 2 features from the FP16 tables (feature
+// 2 lv + f), then the reference encoding's OneBlob(4) on the 5 angle / roughness inputs
+// (32 + 4a + b) and identity on the 6 reflectance values (52..57), 6 zeros.
+__device__ __forceinline__ void encode_row_hashgrid(const NetLayout& ly, const uint32_t* __restrict__ grid,
+                                                    const float* q, uint8_t* tile, int r) {
+    float p[3];
+    grid_position(q, p);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float v[8];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            uint32_t e[8];
+            float w[8];
+            grid_corners(ly, 4 * k + h, p, e, w);
+            uint32_t raw[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) raw[c] = __ldg(grid + e[c]);
+            float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&raw[c]));
+                f0 += w[c] * f.x;
+                f1 += w[c] * f.y;
+            }
+            v[2 * h] = f0;
+            v[2 * h + 1] = f1;
+        }
+        store8(tile, r, k, 64, v);
+    }
+#pragma unroll
+    for (int k = 4; k < 8; ++k) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = reference_feature(8 * k + i + 4, q);
+        store8(tile, r, k, 64, v);
+    }
+}
+
+// Adds the gradient of the 32 hash-grid features of one query (`d`, loss-scaled) into the FP32
+// table gradient: corner c of level lv receives w_c x d[2 lv + f].
+__device__ __forceinline__ void grid_backward(const NetLayout& ly, const float* q, const float (&d)[32],
+                                              float* __restrict__ grid_grad) {
+    float p[3];
+    grid_position(q, p);
+#pragma unroll 1
+    for (int lv = 0; lv < kGridLevels; ++lv) {
+        const float d0 = d[2 * lv], d1 = d[2 * lv + 1];
+        if (d0 == 0.0f && d1 == 0.0f) continue;
+        uint32_t e[8];
+        float w[8];
+        grid_corners(ly, lv, p, e, w);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+            atomicAdd(reinterpret_cast<float2*>(grid_grad) + e[c], make_float2(w[c] * d0, w[c] * d1));
+    }
+}
+
+// Kernels specialised for the 144-wide volume input compile only its encoder.
+template <int IN>
+__device__ __forceinline__ void encode_row(const NetLayout& ly, const uint32_t* __restrict__ grid, const float* q,
+                                           uint8_t* tile, int r) {
+    if constexpr (IN == 144) {
+        encode_row_volume(q, tile, r);
+    } else if (ly.enc == NRC_ENCODING_REFERENCE) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             float v[8];
@@ -198,9 +338,8 @@ __device__ __forceinline__ void encode_row(int enc, const float* q, uint8_t* til
             store8(tile, r, k, 64, v);
         }
     } else {
-        encode_row_volume(q, tile, r);
+        encode_row_hashgrid(ly, grid, q, tile, r);
     }
-    (void)K;
 }
 
 // Record of row `row` of a launch: the row itself, or idx[row] for an indexed launch.
@@ -303,6 +442,7 @@ __host__ __device__ constexpr uint32_t infer_tile_bytes(int in_dim) { return (kT
 // idx (optional): row r of the launch is record idx[r] of `in` and `out`.
 template <int IN, int G, bool TA>
 __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+                                                             const uint32_t* __restrict__ grid,
                                                              const float* __restrict__ in,
                                                              const uint32_t* __restrict__ idx,
                                                              const uint32_t* __restrict__ dev_n, uint32_t n_max,
@@ -342,7 +482,7 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
     load_query(in, idx, (blockIdx.x * G + g) * kTile + gt, n, q);
     for (uint32_t tile = blockIdx.x * G + g; tile < ntiles && ok; tile += stride) {
         const uint32_t row = tile * kTile + gt;
-        encode_row(ly.enc, q, s_t, gt, IN);
+        encode_row<IN>(ly, grid, q, s_t, gt);
         // The next tile's queries load while this tile runs through the layers. (Encoding it
         // during layer 1, when the input tile is already free in the TA form, measured slower:
         // the group's next epilogue waits for the encoder.)
@@ -420,8 +560,11 @@ __global__ void __launch_bounds__(kTile* G, 1) mlp_infer_kernel(const NetLayout 
 // One CTA per 128-sample tile: forward keeping all activations, relative-L2-luminance loss
 // gradient (denominator held constant), backward with weight gradients reduced into `grad`
 // (scaled by loss_scale) and the batch loss added to `loss`.
+// With the hash grid the backward pass also computes the first layer's input gradient and
+// scatters its 32 hash features into the table gradient (grad + ly.nparams).
 template <int IN>
 __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, const uint8_t* __restrict__ blob,
+                                                          const uint32_t* __restrict__ grid,
                                                           const float* __restrict__ in, const float* __restrict__ target,
                                                           uint32_t n, float* __restrict__ grad, float* __restrict__ loss,
                                                           unsigned int* __restrict__ err) {
@@ -450,7 +593,7 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, co
     const uint32_t row = blockIdx.x * kTile + tid;
     float q[14];
     load_query(in, nullptr, row, n, q);
-    encode_row(ly.enc, q, s_act0, tid, IN);
+    encode_row<IN>(ly, grid, q, s_act0, tid);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -533,7 +676,7 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, co
                 uint64_t bd = smem_desc(smem_u32(act(j)) + ks * 2 * (N_in * 16), static_cast<uint32_t>(N_in * 16), 128);
                 mma_f16(tm_dw, ad, bd, idw, ks > 0 ? 1u : 0u);
             }
-            if (j > 0) {
+            if (j > 0 || (IN == 64 && ly.enc == NRC_ENCODING_HASHGRID)) {
                 // input gradient: M = 128 samples, N = in_j, K = out_j; W_j read MN-major
                 const uint32_t idx = idesc_f16(kTile, N_in, 0, 1);
                 for (int ks = 0; ks < K_out / 16; ++ks) {
@@ -579,6 +722,18 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const NetLayout ly, co
             }
             dz = dz_next;
             dz_next = dz_next == s_dza ? s_dzb : s_dza;
+        } else if (IN == 64 && ly.enc == NRC_ENCODING_HASHGRID) {
+            // gradient of the encoded input's hash features (columns 0..31) into the tables
+            float a[16], b[16], d[32];
+            tmem_ld16(tm_dx + lane_base, a);
+            tmem_ld16(tm_dx + lane_base + 16, b);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                d[i] = a[i];
+                d[16 + i] = b[i];
+            }
+            if (row < n) grid_backward(ly, q, d, grad + ly.nparams);
         }
         tc_fence_before();
         fence_async_smem();
@@ -610,14 +765,47 @@ __global__ void pack_kernel(const NetLayout ly, const float* __restrict__ w, uin
     *reinterpret_cast<__half*>(blob + ly.boff[x.j] + cm_offset(x.o, x.i, ly.in[x.j])) = __float2half_rn(w[p]);
 }
 
+// FP16 image of the hash-grid tables (entry-major, two features per 32-bit word).
+__global__ void pack_grid_kernel(const NetLayout ly, const float* __restrict__ w, __half* __restrict__ grid) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ly.grid_params) return;
+    grid[p] = __float2half_rn(w[ly.nparams + p]);
+}
+
 // Adam with L2 regularisation on unscaled gradients, optional EMA of the weights (inference
-// weights = bias-corrected EMA), and repacking of both FP16 images.
+// weights = bias-corrected EMA), and repacking of both FP16 images. Parameters ly.nparams and
+// beyond are hash-grid table entries (FP16 images grid_train / grid_infer); as published for the
+// multiresolution hash encoding (Mueller et al. 2022, section 4), they take no L2 term and an
+// entry whose gradient is exactly 0 skips its Adam step (its moments and value stay as they are).
 __global__ void adam_kernel(const NetLayout ly, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ grad, float* __restrict__ ema, uint8_t* __restrict__ blob_train,
-                            uint8_t* __restrict__ blob_infer, float lr, float beta1, float beta2, float eps, float l2,
+                            uint8_t* __restrict__ blob_infer, __half* __restrict__ grid_train,
+                            __half* __restrict__ grid_infer, float lr, float beta1, float beta2, float eps, float l2,
                             float inv_scale, float c1, float c2, float ema_decay, float ema_corr) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= ly.nparams) return;
+    if (p >= ly.nparams + ly.grid_params) return;
+    if (p >= ly.nparams) {
+        float wi = w[p];
+        const float gr = grad[p];
+        if (gr != 0.0f) {
+            float g = gr * inv_scale;
+            float mi = beta1 * m[p] + (1.0f - beta1) * g;
+            float vi = beta2 * v[p] + (1.0f - beta2) * g * g;
+            m[p] = mi;
+            v[p] = vi;
+            wi -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+            w[p] = wi;
+            grid_train[p - ly.nparams] = __float2half_rn(wi);
+        }
+        float wi_inf = wi;
+        if (ema_decay > 0.0f) {
+            float e = ema_decay * ema[p] + (1.0f - ema_decay) * wi;
+            ema[p] = e;
+            wi_inf = e / ema_corr;
+        }
+        grid_infer[p - ly.nparams] = __float2half_rn(wi_inf);
+        return;
+    }
     ParamIndex x = param_index(ly, p);
     bool real = x.i < (x.j == 0 ? ly.in_real : ly.in[x.j]) && x.o < (x.j == ly.L - 1 ? 3 : ly.out[x.j]);
     float wi = w[p];
@@ -642,13 +830,14 @@ __global__ void adam_kernel(const NetLayout ly, float* __restrict__ w, float* __
 }
 
 template <int IN>
-__global__ void encode_kernel(const NetLayout ly, const float* __restrict__ in, uint32_t n, float* __restrict__ out) {
+__global__ void encode_kernel(const NetLayout ly, const uint32_t* __restrict__ grid, const float* __restrict__ in,
+                              uint32_t n, float* __restrict__ out) {
     // Encodes one 128-row tile per CTA into shared memory, then writes FP32 rows.
     __shared__ __align__(128) uint8_t tile[kTile * IN * 2];
     uint32_t row = blockIdx.x * kTile + threadIdx.x;
     float q[14];
     load_query(in, nullptr, row, n, q);
-    encode_row(ly.enc, q, tile, threadIdx.x, IN);
+    encode_row<IN>(ly, grid, q, tile, threadIdx.x);
     if (row < n)
         for (int c = 0; c < IN; c += 16) {
             float v[16];
@@ -764,8 +953,13 @@ struct NrcHandle {
     int infer_groups = 1;  // 128-row tiles in flight per inference CTA
     float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *ema = nullptr, *loss = nullptr;
     uint8_t *blob_train = nullptr, *blob_infer = nullptr;
+    __half *grid_train = nullptr, *grid_infer = nullptr;  // FP16 hash-grid tables (hash grid only)
     unsigned int* err = nullptr;
     uint64_t steps = 0;
+    int total_params() const { return ly.nparams + ly.grid_params; }
+    const uint32_t* grid_words(bool train) const {
+        return reinterpret_cast<const uint32_t*>(train ? grid_train : grid_infer);
+    }
 };
 
 namespace {
@@ -785,6 +979,11 @@ int repack(NrcHandle* h, cudaStream_t s) {
     int n = h->ly.nparams;
     pack_kernel<<<(n + 255) / 256, 256, 0, s>>>(h->ly, h->w, h->blob_train);
     pack_kernel<<<(n + 255) / 256, 256, 0, s>>>(h->ly, h->cfg.ema_decay > 0 ? h->ema : h->w, h->blob_infer);
+    if (h->ly.grid_params > 0) {
+        const int g = h->ly.grid_params;
+        pack_grid_kernel<<<(g + 255) / 256, 256, 0, s>>>(h->ly, h->w, h->grid_train);
+        pack_grid_kernel<<<(g + 255) / 256, 256, 0, s>>>(h->ly, h->cfg.ema_decay > 0 ? h->ema : h->w, h->grid_infer);
+    }
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
 }
@@ -803,11 +1002,11 @@ void nrc_default_config(int32_t encoding, NrcConfig* c) {
     c->learning_rate = 1e-2f;
     c->loss_scale = 128.0f;
     c->seed = 1;
-    if (encoding == NRC_ENCODING_REFERENCE) {
-        // network_interface.cu:83-129 (TriangleWave option): 2 hidden layers, EMA 0.99, l2 1e-6,
-        // epsilon 1e-8, output activation None.
+    if (encoding == NRC_ENCODING_REFERENCE || encoding == NRC_ENCODING_HASHGRID) {
+        // network_interface.cu:50-122: 2 hidden layers (renderer_scene.cpp:50), EMA 0.99, l2 1e-6,
+        // output activation None; Adam epsilon 1e-8 with TriangleWave, 1e-15 with the hash grid.
         c->num_hidden_layers = 2;
-        c->epsilon = 1e-8f;
+        c->epsilon = encoding == NRC_ENCODING_HASHGRID ? 1e-15f : 1e-8f;
         c->l2_reg = 1e-6f;
         c->ema_decay = 0.99f;
         c->output_activation = NRC_OUTPUT_NONE;
@@ -823,11 +1022,13 @@ void nrc_default_config(int32_t encoding, NrcConfig* c) {
 
 int nrc_create(const NrcConfig* cfg, NrcHandle** out) {
     if (!cfg || !out) return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: null argument");
-    if (cfg->encoding != NRC_ENCODING_REFERENCE && cfg->encoding != NRC_ENCODING_VOLUME)
+    if (cfg->encoding != NRC_ENCODING_REFERENCE && cfg->encoding != NRC_ENCODING_VOLUME &&
+        cfg->encoding != NRC_ENCODING_HASHGRID)
         return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: unknown encoding");
     int max_hidden = cfg->encoding == NRC_ENCODING_VOLUME ? 5 : 7;  // training tile must fit in shared memory
     if (cfg->num_hidden_layers < 1 || cfg->num_hidden_layers > max_hidden)
-        return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: num_hidden_layers out of range (1..5 volume, 1..7 reference)");
+        return fail(NRC_ERR_INVALID_ARGUMENT,
+                    "nrc_create: num_hidden_layers out of range (1..5 volume, 1..7 reference and hash grid)");
     if (!(cfg->learning_rate > 0) || !(cfg->loss_scale > 0) || cfg->ema_decay < 0 || cfg->ema_decay >= 1)
         return fail(NRC_ERR_INVALID_ARGUMENT, "nrc_create: bad optimiser settings");
     auto* h = new NrcHandle();
@@ -836,11 +1037,13 @@ int nrc_create(const NrcConfig* cfg, NrcHandle** out) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
-    const int np = h->ly.nparams;
+    const int np = h->total_params();
+    const int ng = std::max(h->ly.grid_params, 2);
     int rc;
     if ((rc = alloc(&h->w, np)) || (rc = alloc(&h->m, np)) || (rc = alloc(&h->v, np)) || (rc = alloc(&h->grad, np)) ||
         (rc = alloc(&h->ema, np)) || (rc = alloc(&h->loss, 1)) || (rc = alloc(&h->blob_train, h->ly.blob_bytes)) ||
-        (rc = alloc(&h->blob_infer, h->ly.blob_bytes)) || (rc = alloc(&h->err, 1))) {
+        (rc = alloc(&h->blob_infer, h->ly.blob_bytes)) || (rc = alloc(&h->grid_train, ng)) ||
+        (rc = alloc(&h->grid_infer, ng)) || (rc = alloc(&h->err, 1))) {
         nrc_destroy(h);
         return rc;
     }
@@ -855,6 +1058,9 @@ int nrc_create(const NrcConfig* cfg, NrcHandle** out) {
         for (int o = 0; o < out_real; ++o)
             for (int i = 0; i < in_real; ++i) w[h->ly.poff[j] + o * h->ly.in[j] + i] = u(gen);
     }
+    // Hash-grid entries start uniform in [-1e-4, 1e-4] (the published initialisation).
+    std::uniform_real_distribution<float> ug(-1e-4f, 1e-4f);
+    for (int p = h->ly.nparams; p < np; ++p) w[p] = ug(gen);
     if (cudaMemcpy(h->w, w.data(), np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(h->m, 0, np * sizeof(float)) != cudaSuccess || cudaMemset(h->v, 0, np * sizeof(float)) != cudaSuccess ||
         cudaMemset(h->grad, 0, np * sizeof(float)) != cudaSuccess ||
@@ -895,6 +1101,8 @@ int nrc_destroy(NrcHandle* h) {
     cudaFree(h->loss);
     cudaFree(h->blob_train);
     cudaFree(h->blob_infer);
+    cudaFree(h->grid_train);
+    cudaFree(h->grid_infer);
     cudaFree(h->err);
     delete h;
     return NRC_OK;
@@ -911,21 +1119,22 @@ static int infer_impl(NrcHandle* h, void* stream, const float* in, const uint32_
     const uint32_t smem = infer_smem(h->ly, G);
     const bool vol = h->cfg.encoding == NRC_ENCODING_VOLUME;
     const dim3 block(kTile * G);
+    const uint32_t* gw = h->grid_words(false);
     if (G == 4) {
         if (vol)
-            mlp_infer_kernel<144, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 4, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
     } else if (G == 2) {
         if (vol)
-            mlp_infer_kernel<144, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 2, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
     } else {
         if (vol)
-            mlp_infer_kernel<144, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<144, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
         else
-            mlp_infer_kernel<64, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, in, idx, dev_n, n, out, h->err);
+            mlp_infer_kernel<64, 1, kInferTmemActivations><<<grid, block, smem, s>>>(h->ly, h->blob_infer, gw, in, idx, dev_n, n, out, h->err);
     }
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
@@ -952,23 +1161,26 @@ int nrc_train(NrcHandle* h, void* stream, const float* in, const float* target, 
     if (n == 0) return NRC_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const NetLayout& ly = h->ly;
-    NRC_CUDA(cudaMemsetAsync(h->grad, 0, ly.nparams * sizeof(float), s));
+    const int np = h->total_params();
+    NRC_CUDA(cudaMemsetAsync(h->grad, 0, np * sizeof(float), s));
     NRC_CUDA(cudaMemsetAsync(h->loss, 0, sizeof(float), s));
     uint32_t tiles = (n + kTile - 1) / kTile;
     uint32_t smem = train_smem(ly);
+    const uint32_t* gw = h->grid_words(true);
     if (h->cfg.encoding == NRC_ENCODING_VOLUME)
-        mlp_train_kernel<144><<<tiles, kTile, smem, s>>>(ly, h->blob_train, in, target, n, h->grad, h->loss, h->err);
+        mlp_train_kernel<144><<<tiles, kTile, smem, s>>>(ly, h->blob_train, gw, in, target, n, h->grad, h->loss, h->err);
     else
-        mlp_train_kernel<64><<<tiles, kTile, smem, s>>>(ly, h->blob_train, in, target, n, h->grad, h->loss, h->err);
+        mlp_train_kernel<64><<<tiles, kTile, smem, s>>>(ly, h->blob_train, gw, in, target, n, h->grad, h->loss, h->err);
     ++h->steps;
     const NrcConfig& c = h->cfg;
     float c1 = 1.0f - std::pow(c.beta1, static_cast<float>(h->steps));
     float c2 = 1.0f - std::pow(c.beta2, static_cast<float>(h->steps));
     // The EMA starts from the initial weights (not from zero), so it needs no bias correction.
     const float ema_corr = 1.0f;
-    adam_kernel<<<(ly.nparams + 255) / 256, 256, 0, s>>>(ly, h->w, h->m, h->v, h->grad, h->ema, h->blob_train,
-                                                         h->blob_infer, c.learning_rate, c.beta1, c.beta2, c.epsilon,
-                                                         c.l2_reg, 1.0f / c.loss_scale, c1, c2, c.ema_decay, ema_corr);
+    adam_kernel<<<(np + 255) / 256, 256, 0, s>>>(ly, h->w, h->m, h->v, h->grad, h->ema, h->blob_train, h->blob_infer,
+                                                 h->grid_train, h->grid_infer, c.learning_rate, c.beta1, c.beta2,
+                                                 c.epsilon, c.l2_reg, 1.0f / c.loss_scale, c1, c2, c.ema_decay,
+                                                 ema_corr);
     NRC_CUDA(cudaGetLastError());
     if (loss_out) {
         NRC_CUDA(cudaMemcpyAsync(loss_out, h->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -984,22 +1196,22 @@ int nrc_get_layout(NrcHandle* h, int32_t* num_layers, int32_t* in_dims, int32_t*
         if (in_dims) in_dims[j] = h->ly.in[j];
         if (out_dims) out_dims[j] = h->ly.out[j];
     }
-    if (total) *total = h->ly.nparams;
+    if (total) *total = h->total_params();
     return NRC_OK;
 }
 
 int nrc_get_params(NrcHandle* h, float* host) {
     if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
     NRC_CUDA(cudaDeviceSynchronize());
-    NRC_CUDA(cudaMemcpy(host, h->w, h->ly.nparams * sizeof(float), cudaMemcpyDeviceToHost));
+    NRC_CUDA(cudaMemcpy(host, h->w, h->total_params() * sizeof(float), cudaMemcpyDeviceToHost));
     return NRC_OK;
 }
 
 int nrc_set_params(NrcHandle* h, const float* host) {
     if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
     NRC_CUDA(cudaDeviceSynchronize());
-    NRC_CUDA(cudaMemcpy(h->w, host, h->ly.nparams * sizeof(float), cudaMemcpyHostToDevice));
-    NRC_CUDA(cudaMemcpy(h->ema, host, h->ly.nparams * sizeof(float), cudaMemcpyHostToDevice));
+    NRC_CUDA(cudaMemcpy(h->w, host, h->total_params() * sizeof(float), cudaMemcpyHostToDevice));
+    NRC_CUDA(cudaMemcpy(h->ema, host, h->total_params() * sizeof(float), cudaMemcpyHostToDevice));
     int rc = repack(h, 0);
     if (rc) return rc;
     NRC_CUDA(cudaDeviceSynchronize());
@@ -1009,9 +1221,9 @@ int nrc_set_params(NrcHandle* h, const float* host) {
 int nrc_get_gradients(NrcHandle* h, float* host) {
     if (!h || !host) return fail(NRC_ERR_INVALID_ARGUMENT, "null argument");
     NRC_CUDA(cudaDeviceSynchronize());
-    NRC_CUDA(cudaMemcpy(host, h->grad, h->ly.nparams * sizeof(float), cudaMemcpyDeviceToHost));
+    NRC_CUDA(cudaMemcpy(host, h->grad, h->total_params() * sizeof(float), cudaMemcpyDeviceToHost));
     const float inv = 1.0f / h->cfg.loss_scale;
-    for (int i = 0; i < h->ly.nparams; ++i) host[i] *= inv;
+    for (int i = 0; i < h->total_params(); ++i) host[i] *= inv;
     return NRC_OK;
 }
 
@@ -1021,9 +1233,9 @@ int nrc_encode(NrcHandle* h, void* stream, const float* in, uint32_t n, float* o
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t tiles = (n + kTile - 1) / kTile;
     if (h->cfg.encoding == NRC_ENCODING_VOLUME)
-        encode_kernel<144><<<tiles, kTile, 0, s>>>(h->ly, in, n, out);
+        encode_kernel<144><<<tiles, kTile, 0, s>>>(h->ly, h->grid_words(true), in, n, out);
     else
-        encode_kernel<64><<<tiles, kTile, 0, s>>>(h->ly, in, n, out);
+        encode_kernel<64><<<tiles, kTile, 0, s>>>(h->ly, h->grid_words(true), in, n, out);
     NRC_CUDA(cudaGetLastError());
     return NRC_OK;
 }

@@ -2,7 +2,7 @@
 over the C ABI in include/rtc8_nrc.h.
 
     cache = NeuralRadianceCache()
-    cache.initialize(PositionEncoding.TriangleWave, num_hidden_layers=2, learning_rate=1e-2)
+    cache.initialize(PositionEncoding.HashGrid, num_hidden_layers=2, learning_rate=1e-2)
     cache.infer(stream, input_ptr, n, prediction_ptr)
     cache.train(stream, input_ptr, target_ptr, n)      # loss=True returns the batch loss (syncs)
     cache.finalize()
@@ -22,13 +22,14 @@ from ._lib import NrcConfig
 
 NRC_ENCODING_REFERENCE = 0
 NRC_ENCODING_VOLUME = 1
+NRC_ENCODING_HASHGRID = 2
 NRC_OUTPUT_NONE = 0
 NRC_OUTPUT_EXP = 1
 
 
 class PositionEncoding(enum.IntEnum):
-    """network_interface.h:8-11. TriangleWave maps to the reference encoding of this library;
-    HashGrid is not provided (the GB300 cache uses the frequency / one-blob volume encoding)."""
+    """network_interface.h:8-11: TriangleWave -> NRC_ENCODING_REFERENCE, HashGrid (the
+    reference's default, renderer_scene.cpp:50) -> NRC_ENCODING_HASHGRID."""
     TriangleWave = 0
     HashGrid = 1
 
@@ -66,9 +67,8 @@ class NeuralRadianceCache:
     def initialize(self, pos_encoding: PositionEncoding = PositionEncoding.TriangleWave, num_hidden_layers: int = 2,
                    learning_rate: float = 1e-2, config: NrcConfig | None = None) -> None:
         if config is None:
-            if pos_encoding == PositionEncoding.HashGrid:
-                raise NrcError("HashGrid position encoding is not provided; use TriangleWave or a volume config")
-            config = default_config(NRC_ENCODING_REFERENCE)
+            config = default_config(NRC_ENCODING_HASHGRID if pos_encoding == PositionEncoding.HashGrid
+                                    else NRC_ENCODING_REFERENCE)
             config.num_hidden_layers = num_hidden_layers
             config.learning_rate = learning_rate
         self.config = config

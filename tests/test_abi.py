@@ -53,10 +53,11 @@ def test_library_built_for_sm_103a():
     assert "arch=compute_103a,code=sm_103a" in build.ARCH
 
 
-def test_cpp_shim_compiles_links_and_refuses_hashgrid(lib, tmp_path):
+def test_cpp_shim_compiles_links_and_checks_hashgrid_arguments(lib, tmp_path):
     """include/rtc8_nrc.hpp: the reference's rtc8::NeuralRadianceCache interface over the C ABI
-    compiles and links as the renderer would use it; the unimplemented HashGrid encoding throws
-    (no device work, so this runs without a GPU)."""
+    compiles and links as the renderer would use it, with the reference's own HashGrid call
+    (renderer_scene.cpp:50); an out-of-range layer count throws the library's message before any
+    device work, so this runs without a GPU (the GPU tests run the valid call)."""
     import shutil
     import subprocess
 
@@ -66,8 +67,9 @@ def test_cpp_shim_compiles_links_and_refuses_hashgrid(lib, tmp_path):
     src = tmp_path / "shim.cpp"
     src.write_text(
         '#include "rtc8_nrc.hpp"\n#include <cstdio>\n'
-        "int main() {\n  rtc8::NeuralRadianceCache cache;\n"
-        "  try { cache.initialize(rtc8::PositionEncoding::HashGrid, 2, 1e-2f); }\n"
+        "int main(int argc, char**) {\n  rtc8::NeuralRadianceCache cache;\n"
+        "  if (argc > 1) cache.initialize(rtc8::PositionEncoding::HashGrid, 2, 0.01f);\n"
+        "  try { cache.initialize(rtc8::PositionEncoding::HashGrid, 9, 1e-2f); }\n"
         '  catch (const std::exception& e) { std::puts(e.what()); return 0; }\n  return 1;\n}\n')
     from rtc8_gb300 import build
 
@@ -77,7 +79,7 @@ def test_cpp_shim_compiles_links_and_refuses_hashgrid(lib, tmp_path):
     subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(cuda_inc), str(src), "-L", str(libdir),
                     "-lrtc8_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
-    assert "HashGrid encoding is not implemented" in out
+    assert "num_hidden_layers out of range" in out and "hash grid" in out
 
 
 def test_cpp_renderer_header_compiles_and_orients_like_python(lib, tmp_path):

@@ -190,11 +190,13 @@ def test_training_reduces_loss(cuda_device):
     cache.finalize()
 
 
-def test_cpp_shim_matches_python_binding(cuda_device, tmp_path):
+@pytest.mark.parametrize("encoding", ["TriangleWave", "HashGrid"])
+def test_cpp_shim_matches_python_binding(cuda_device, tmp_path, encoding):
     """The reference's C++ interface (include/rtc8_nrc.hpp, rtc8::NeuralRadianceCache) used as the
-    renderer uses it: initialize(TriangleWave, 2, 1e-2), one train step with the loss read back,
-    then inference, against the same calls through the Python binding (same default seed, so the
-    same initial weights; weight gradients are reduced with atomics, hence the tolerance)."""
+    renderer uses it: initialize(<encoding>, 2, 1e-2) (renderer_scene.cpp:50 passes HashGrid), one
+    train step with the loss read back, then inference, against the same calls through the Python
+    binding (same default seed, so the same initial weights; gradients are reduced with atomics,
+    hence the tolerance)."""
     import shutil
     import subprocess
 
@@ -228,7 +230,7 @@ int main(int argc, char** argv) {
     cudaMemcpy(d_in, h.data(), n * 14 * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(d_tgt, h.data() + n * 14, n * 3 * sizeof(float), cudaMemcpyHostToDevice);
     rtc8::NeuralRadianceCache cache;
-    cache.initialize(rtc8::PositionEncoding::TriangleWave, 2, 1e-2f);
+    cache.initialize(rtc8::PositionEncoding::ENCODING, 2, 1e-2f);
     float loss = 0.0f;
     cache.train(nullptr, d_in, d_tgt, n, &loss);
     cache.infer(nullptr, d_in, n, d_out);
@@ -245,7 +247,8 @@ int main(int argc, char** argv) {
     libdir = build.LIB.parent
     cuda = Path(build.nvcc()).resolve().parent.parent
     exe = tmp_path / "shim"
-    subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(src),
+    subprocess.run([cxx, "-std=c++17", f"-DENCODING={encoding}", "-I", str(ROOT / "include"), "-I",
+                    str(cuda / "include"), str(src),
                     "-L", str(libdir), "-lrtc8_gb300", "-L", str(cuda / "lib64"), "-lcudart",
                     f"-Wl,-rpath,{libdir}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)], check=True)
     subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
@@ -253,7 +256,7 @@ int main(int argc, char** argv) {
     loss_cpp, out_cpp = res[0], res[1:].reshape(n, 3)
 
     cache = nrc.NeuralRadianceCache()
-    cache.initialize(nrc.PositionEncoding.TriangleWave, 2, 1e-2)
+    cache.initialize(nrc.PositionEncoding[encoding], 2, 1e-2)
     tq, tt = torch.from_numpy(q).cuda(), torch.from_numpy(tgt).cuda()
     loss_py = cache.train(None, tq, tt, n, loss=True)
     out = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
