@@ -295,9 +295,9 @@ def mlp_bench(steps: int, warmup: int) -> dict:
 
 
 def nrc_frame_loop(frames: int, warmup: int) -> dict:
-    """The radiance-cache frame loop (1 training iteration + spp_per_frame samples per frame, the
-    settings of the equal-error comparison) on the 256x256 dense 64^3 scene; returns the mean
-    frame time."""
+    """The radiance-cache frame loop (train_iterations training iterations + spp_per_frame samples
+    per frame, the settings of the equal-error comparison) on the 256x256 dense 64^3 scene; returns
+    the mean frame time."""
     import torch
 
     from rtc8_gb300 import convergence, nrc
@@ -315,16 +315,18 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
     cache.initialize(config=net)
     s = torch.cuda.Stream()
     r.nrc_frame(cache, 8, st["spp_per_frame"], True, s.cuda_stream)
+    iters = st.get("train_iterations", 1)
     for _ in range(warmup):
-        r.nrc_frame(cache, 1, st["spp_per_frame"], False, s.cuda_stream)
+        r.nrc_frame(cache, iters, st["spp_per_frame"], False, s.cuda_stream)
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(s)
     for _ in range(frames):
-        r.nrc_frame(cache, 1, st["spp_per_frame"], False, s.cuda_stream)
+        r.nrc_frame(cache, iters, st["spp_per_frame"], False, s.cuda_stream)
     b.record(s)
     torch.cuda.synchronize()
     out = {"nrc_frame_ms": a.elapsed_time(b) / frames, "frames": frames, "spp_per_frame": st["spp_per_frame"],
+           "train_iterations_per_frame": iters,
            "device_errors": r.device_errors() | cache.device_errors()}
     cache.finalize()
     r.close()

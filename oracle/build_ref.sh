@@ -32,4 +32,10 @@ g++ -O2 -std=c++17 -w -DNANOVDB_USE_ZIP -I "$REF/ext/nanovdb" "$HERE/ref_nvdb_fi
 NVCC="${NVCC:-nvcc}"
 "$NVCC" -std=c++17 -O2 -w -x cu -DCUDA_UTIL_DONT_USE_GL_INTEROP -I "$REF/common" "$HERE/ref_kat_basic.cu" "$REF/common/basic_types.cpp" \
     -o "$OUT/ref_kat_basic"
+# Known-answer kernels over the reference's own device code (PTX, run on the GPU host by
+# oracle/kat_device_loader.cpp): the reference's CUDA flags (renderer/CMakeLists.txt:37-51), with
+# oracle/optix_stub standing in for the absent OptiX SDK headers.
+"$NVCC" -ptx -std=c++17 -arch=compute_90 --use_fast_math -w -DCUDA_UTIL_DONT_USE_GL_INTEROP \
+    -I "$HERE/optix_stub" -I "$REF" -I "$REF/common" -I "$REF/ext/nanovdb" \
+    "$HERE/ref_kat_device.cu" -o "$OUT/ref_kat_device.ptx"
 echo "built reference known-answer programs in $OUT"

@@ -53,6 +53,7 @@ _FUNCS = {
     "orc_clip_rays": (None, [C.POINTER(OrcScene), f32p, f32p, C.c_int32, f32p, f32p, i32p]),
     "orc_env_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p, f32p]),
     "orc_env_evaluate": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p]),
+    "orc_imp_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p]),
     "orc_phase_sample": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p, f32p]),
     "orc_phase_eval": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p]),
     "orc_polar_yup": (None, [f32p, C.c_int32, f32p]),

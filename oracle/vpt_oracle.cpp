@@ -996,6 +996,20 @@ void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, f
     }
 }
 
+// The hierarchical importance walk alone: per u pair, (pixel x, pixel y, remapped u0, u1, prob).
+void orc_imp_sample(const OrcScene* sc, const float* u, int32_t n, float* out) {
+    for (int i = 0; i < n; ++i) {
+        int px, py;
+        float r0, r1, prob;
+        imp_sample(*sc, u[2 * i], u[2 * i + 1], &px, &py, &r0, &r1, &prob);
+        out[5 * i] = static_cast<float>(px);
+        out[5 * i + 1] = static_cast<float>(py);
+        out[5 * i + 2] = r0;
+        out[5 * i + 3] = r1;
+        out[5 * i + 4] = prob;
+    }
+}
+
 void orc_env_evaluate(const OrcScene* sc, const float* dir, int32_t n, float* pdf, float* out) {
     for (int i = 0; i < n; ++i) {
         float p;

@@ -131,6 +131,7 @@ void orc_clip_rays(const OrcScene* sc, const float* org, const float* dir, int32
 void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, float* pdf,
                     float* rgb);
 void orc_env_evaluate(const OrcScene* sc, const float* dir, int32_t n, float* pdf, float* rgb);
+void orc_imp_sample(const OrcScene* sc, const float* u, int32_t n, float* out5);
 void orc_phase_sample(int32_t kind, float param, const float* u, int32_t n, float* dir_local,
                       float* pdf);
 void orc_phase_eval(int32_t kind, float param, const float* dir_local, int32_t n, float* pdf);

@@ -165,15 +165,15 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
             "device_errors": errors, "image": img}
 
 
-# Radiance-cache settings of the equal-error comparison, from a sweep on the 64^3 cloud: the
-# volume cache of rtc8_nrc.h with Adam lr 5e-3 and an EMA (0.9) of the weights for inference;
-# render paths end at path-spread factor 0.32 (the reference's 0.01 leaves a cache bias near
-# relMSE 1e-3 on this scene), biased training suffixes at 0.08; 128 samples per pixel per frame
-# with one training iteration per frame (the reference's default is 8 samples per frame,
-# renderer_main.cpp:359, a command-line setting). Render paths use the configuration's
-# shadow-ray roulette; the training suffixes do not.
-NRC_SETTINGS = {"termination": 0.32, "train_termination": 0.08, "ema_decay": 0.9, "learning_rate": 5e-3,
-                "spp_per_frame": 128}
+# Radiance-cache settings of the equal-error comparison, from sweeps on the 64^3 cloud with five
+# RNG seeds that the comparison itself does not use, judged by the sustained criterion: the volume
+# cache of rtc8_nrc.h with Adam lr 5e-3 and the raw weights for inference (an EMA of the weights
+# lagged behind: decay 0.9 -> 0.85x median, 0.99 -> 0.2x); render paths end at path-spread factor
+# 1.28 and biased training suffixes at 0.08; 128 samples per pixel per frame with four training
+# iterations (generate, propagate, shuffle, 4 x 16384-record steps) per frame. Render paths use the
+# configuration's shadow-ray roulette; the training suffixes do not.
+NRC_SETTINGS = {"termination": 1.28, "train_termination": 0.08, "ema_decay": 0.0, "learning_rate": 5e-3,
+                "spp_per_frame": 128, "train_iterations": 4}
 
 
 def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, time_budget: float) -> dict:

@@ -1,0 +1,227 @@
+"""The oracle against the reference's own device code, executed on a GPU (CPU test).
+
+tests/golden/ref_device_kat.npz holds seeded inputs and the outputs of the reference's
+PCG32RNG, SchlickPhaseFunction, HierarchicalImportanceMap and ImageBasedEnvironmentalLight
+(common/common_renderer_types.h), of its importance-map kernels
+(renderer/gpu_kernels/compute_light_probs.cu:161-211) and of its four radiance-cache set-up
+kernels (renderer/gpu_kernels/nrc_set_up_kernels.cu:4-219), compiled from the reference's sources
+with its own CUDA flags (--use_fast_math) by oracle/build_ref.sh and run by
+tests/golden/make_golden_device.py. The oracle restates them with IEEE arithmetic, so values that
+pass through a fast-math division, square root or sine are compared with a tolerance of a few ulps
+and everything else exactly.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import orc
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "ref_device_kat.npz"
+INVALID = 0x3FFFFF
+
+
+@pytest.fixture(scope="module")
+def kat():
+    z = np.load(GOLDEN)
+    return {k: z[k] for k in z.files}
+
+
+def _f(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def test_record_layouts_match_the_products(kat):
+    """Byte sizes of the records the product writes in the reference's layouts."""
+    s = kat["out:sizes.out"]
+    assert s[2] == 56          # RadianceQuery: 14 floats
+    assert s[3] == 16          # TerminalInfo: throughput + bit fields
+    assert s[4] == 16          # TrainingVertexInfo
+    assert s[5] == 4           # TrainingSuffixTerminalInfo: prev:22, hasQuery:1, pathLength:8, unbiased:1
+    assert s[6] == 4           # LinearCongruentialGenerator
+    assert s[7] == 12 and s[8] == 12
+
+
+def test_pcg32_matches_reference(kat):
+    states = kat["in:pcg.states"]
+    raw = kat["out:pcg.raw"].reshape(-1, 8)
+    f01 = kat["out:pcg.f01"].reshape(-1, 8)
+    for i, st in enumerate(states):
+        fl, _ = orc.pcg_floats(int(st), 16)
+        want = (((raw[i] >> np.uint32(9)) | np.uint32(0x3F800000)).view(np.float32) - np.float32(1.0))
+        np.testing.assert_array_equal(fl[:8], want)
+        np.testing.assert_array_equal(fl[8:], f01[i])
+
+
+def test_schlick_phase_function_matches_reference(kat):
+    ks = kat["in:schlick.k"]
+    u = _f(kat["in:schlick.u"])
+    ref = kat["out:schlick.out"].reshape(len(ks), -1, 6)
+    n = len(u)
+    for j, k in enumerate(ks):
+        dl, pdf = np.zeros(3 * n, np.float32), np.zeros(n, np.float32)
+        orc.lib().orc_phase_sample(0, float(k), orc.p(u, orc.C.c_float), n, orc.p(dl, orc.C.c_float),
+                                   orc.p(pdf, orc.C.c_float))
+        dl3 = dl.reshape(-1, 3)
+        # cos(theta) to a few ulps; the in-plane part sin(theta) = sqrt(1 - cos^2) is ill-conditioned
+        # near the poles, where the reference's approximate division (cos(theta) = -0.99999994 for
+        # k = -0.9, u1 = 0, exactly -1 in IEEE arithmetic) moves it by up to ~3.5e-4
+        np.testing.assert_allclose(dl3[:, 2], ref[j, :, 2], rtol=0, atol=3e-6)
+        np.testing.assert_allclose(dl3[:, 0:2], ref[j, :, 0:2], rtol=0, atol=5e-4)
+        assert np.mean(np.all(np.abs(dl3 - ref[j, :, 0:3]) <= 3e-6, axis=1)) >= 0.98
+        np.testing.assert_allclose(pdf, ref[j, :, 3], rtol=2e-5)
+        rd = _f(ref[j, :, 0:3])
+        pe = np.zeros(n, np.float32)
+        orc.lib().orc_phase_eval(0, float(k), orc.p(rd, orc.C.c_float), n, orc.p(pe, orc.C.c_float))
+        np.testing.assert_allclose(pe, ref[j, :, 4], rtol=2e-5)
+        np.testing.assert_allclose(ref[j, :, 5], ref[j, :, 4], rtol=1e-6)   # f = p for a phase function
+
+
+def _env_scene(img):
+    return orc.make_scene(voxels=np.zeros((2, 2, 2), np.float32), voxel_size=1.0, origin=[0, 0, 0],
+                          density_coeff=1.0, albedo=1.0, phase_kind=0, phase_param=0.0, env_rgb=img, width=1,
+                          height=1, cam_aspect=1.0, cam_fovy=0.7, cam_pos=[0, 0, 3], cam_quat=[0, 0, 0, 1])
+
+
+def test_importance_map_build_matches_reference(kat):
+    img = _f(kat["in:env.rgb"])
+    mips, _, info = orc.importance_map(img)
+    ref = kat["out:env.mips"]
+    assert len(mips) == len(ref)
+    np.testing.assert_allclose(mips, ref, rtol=1e-5, atol=1e-30)
+    assert info["integral"] == pytest.approx(float(kat["out:env.integral"][0]), rel=1e-5)
+
+
+def test_environment_sampling_matches_reference(kat):
+    img = _f(kat["in:env.rgb"])
+    sc = _env_scene(img)
+    u = _f(kat["in:env.u"])
+    n = len(u)
+    ref = kat["out:env.out"].reshape(n, 15)
+    # hierarchical importance walk
+    walk = np.zeros(5 * n, np.float32)
+    orc.lib().orc_imp_sample(sc.ref, orc.p(u, orc.C.c_float), n, orc.p(walk, orc.C.c_float))
+    walk = walk.reshape(n, 5)
+    same_pix = np.all(walk[:, 0:2] == ref[:, 0:2], axis=1)
+    assert same_pix.mean() >= 0.999, same_pix.mean()
+    # remapped u after ~11 levels of divisions (approximate in the reference's fast-math build)
+    np.testing.assert_allclose(walk[same_pix, 2:4], ref[same_pix, 2:4], rtol=0, atol=2e-4)
+    assert np.mean(np.all(np.abs(walk[same_pix, 2:4] - ref[same_pix, 2:4]) <= 2e-5, axis=1)) >= 0.95
+    np.testing.assert_allclose(walk[same_pix, 4], ref[same_pix, 4], rtol=2e-5)
+    # ImageBasedEnvironmentalLight::sample: direction from (phi, theta), density, radiance
+    d, pdf, c = np.zeros(3 * n, np.float32), np.zeros(n, np.float32), np.zeros(3 * n, np.float32)
+    orc.lib().orc_env_sample(sc.ref, orc.p(u, orc.C.c_float), n, orc.p(d, orc.C.c_float), orc.p(pdf, orc.C.c_float),
+                             orc.p(c, orc.C.c_float))
+    phi, theta = ref[:, 5].astype(np.float64), ref[:, 6].astype(np.float64)
+    ref_dir = np.stack([-np.sin(phi) * np.sin(theta), np.cos(theta), np.cos(phi) * np.sin(theta)], 1)
+    np.testing.assert_allclose(d.reshape(-1, 3)[same_pix], ref_dir[same_pix], rtol=0, atol=3e-5)
+    np.testing.assert_array_equal(c.reshape(-1, 3)[same_pix], ref[same_pix, 8:11])
+    zero = ref[:, 7] == 0            # sin(theta) = 0: the reference returns density 0 and no radiance
+    np.testing.assert_array_equal(pdf[zero & same_pix], 0.0)
+    ok = same_pix & ~zero
+    # the density divides by sin(theta), which the reference's fast-math sine gets only to an
+    # absolute ~1e-6: relative agreement where sin(theta) is not tiny, looser at the poles
+    well = ok & (np.sin(theta) > 1e-2)
+    np.testing.assert_allclose(pdf[well], ref[well, 7], rtol=5e-5)
+    np.testing.assert_allclose(pdf[ok], ref[ok, 7], rtol=1e-2)
+    # ImageBasedEnvironmentalLight::evaluate at the sampled direction
+    pe, ce = np.zeros(n, np.float32), np.zeros(3 * n, np.float32)
+    rdir = _f(ref_dir)
+    orc.lib().orc_env_evaluate(sc.ref, orc.p(rdir, orc.C.c_float), n, orc.p(pe, orc.C.c_float),
+                               orc.p(ce, orc.C.c_float))
+    same_texel = np.all(ce.reshape(-1, 3) == ref[:, 12:15], axis=1)
+    assert same_texel[ok].mean() >= 0.995
+    both = well & same_texel
+    np.testing.assert_allclose(pe[both], ref[both, 11], rtol=5e-5)
+
+
+def _params(kat):
+    p = kat["in:nrc.params"]
+    return {"w": int(p[0]), "h": int(p[1]), "max_suffix": int(p[2]), "buf": int(p[3]), "offset": int(p[4]),
+            "new_seq": int(p[5]), "prev_count": int(p[6]), "prev_w": int(p[7]), "prev_h": int(p[8]),
+            "accum_frames": int(p[9]), "shuffle_count": int(p[10]), "n_vert": int(p[11]),
+            "radiance_scale": float(p[12:13].view(np.float32)[0])}
+
+
+def test_prepare_matches_reference(kat):
+    p = _params(kat)
+    counters = np.zeros(16, np.uint32)
+    prev = 1 - p["buf"]
+    counters[prev] = p["prev_count"]
+    counters[2 + 2 * prev], counters[3 + 2 * prev] = p["prev_w"], p["prev_h"]
+    stats = np.zeros(18, np.float32)
+    suffix = np.full(p["w"] * p["h"], 0xFFFFFFFF, np.uint32)
+    orc.nrc_prepare(counters, stats, suffix, p["w"], p["h"], p["buf"], p["offset"], bool(p["new_seq"]))
+    ref = kat["out:prep.out"]
+    assert (counters[2 + 2 * p["buf"]], counters[3 + 2 * p["buf"]], counters[p["buf"]]) == tuple(ref)
+    assert tuple(ref[:2]) == (10, 10)       # 8 / sqrt(40000 / 65536), capped by the image
+    mm = kat["out:prep.minmax"]
+    s = stats[9 * p["buf"]: 9 * p["buf"] + 9]
+    np.testing.assert_array_equal(s[0:6], mm)
+    np.testing.assert_array_equal(s[6:9], kat["out:prep.avg"])
+    term = kat["out:prep.term"].reshape(3, -1)
+    m = p["max_suffix"]
+    np.testing.assert_array_equal(suffix[:m] & INVALID, term[0])
+    np.testing.assert_array_equal((suffix[:m] >> 22) & 1, term[1])
+    np.testing.assert_array_equal((suffix[:m] >> 23) & 0xFF, term[2])
+
+
+def test_propagate_matches_reference(kat):
+    p = _params(kat)
+    m, nv = p["max_suffix"], p["n_vert"]
+    term = kat["in:prop.term"].reshape(3, m)
+    suffix = (term[0] & INVALID) | ((term[1] & 1) << 22) | ((term[2] & 0xFF) << 23)
+    vertex = np.zeros((orc.TRAIN_BUFFER_SIZE, 4), np.float32)
+    vertex[:nv, 0:3] = kat["in:prop.vtp"]
+    vertex[:nv, 3] = (kat["in:prop.vprev"] & INVALID).astype(np.uint32).view(np.float32)
+    vertex[nv:, 3] = np.full(orc.TRAIN_BUFFER_SIZE - nv, INVALID, np.uint32).view(np.float32)
+    q0 = np.zeros((orc.TRAIN_BUFFER_SIZE, 14), np.float32)
+    q0[:nv] = kat["in:prop.query0"]
+    t0 = np.zeros((orc.TRAIN_BUFFER_SIZE, 3), np.float32)
+    t0[:nv] = kat["in:prop.target0"]
+    orc.nrc_propagate(m, suffix.astype(np.uint32), _f(kat["in:prop.inferred"]), _f(kat["in:prop.query"]), vertex,
+                      q0, t0, p["radiance_scale"])
+    ref = kat["out:prop.target_out"].reshape(-1, 3)
+    changed = np.any(ref != kat["in:prop.target0"], axis=1)
+    assert changed.sum() > 100
+    np.testing.assert_allclose(t0[:nv], ref, rtol=1e-5, atol=1e-7)
+
+
+def test_shuffle_matches_reference(kat):
+    p = _params(kat)
+    nv, count = p["n_vert"], p["shuffle_count"]
+    q0 = np.zeros((orc.TRAIN_BUFFER_SIZE, 14), np.float32)
+    q0[:nv] = kat["in:shuf.query0"]
+    t0 = np.zeros((orc.TRAIN_BUFFER_SIZE, 3), np.float32)
+    t0[:nv] = kat["in:shuf.target0"]
+    q1 = np.zeros((orc.TRAIN_PER_FRAME, 14), np.float32)
+    t1 = np.zeros((orc.TRAIN_PER_FRAME, 3), np.float32)
+    stats = np.array([np.inf] * 3 + [-np.inf] * 3 + [0.0] * 3, np.float32)
+    writers = orc.nrc_shuffle(count, stats, orc.nrc_shufflers(), q0, t0, q1, t1, p["radiance_scale"])
+    rq = kat["out:shuf.query1"].reshape(-1, 14)
+    rt = kat["out:shuf.target1"].reshape(-1, 3)
+    one = writers == 1
+    assert one.mean() > 0.3
+    np.testing.assert_array_equal(q1[one], rq[one])
+    np.testing.assert_array_equal(t1[one], rt[one])
+    none = writers == 0
+    np.testing.assert_array_equal(rq[none], 0.0)
+    # a slot written by several threads holds one of their records (the write order is a race)
+    multi = np.nonzero(writers > 1)[0][:500]
+    ids = np.round(rq[multi, 0] * nv).astype(int)
+    assert np.all((rq[multi, 0] == 0) | np.isclose(rq[multi, 0], ids / nv))
+    np.testing.assert_array_equal(stats[0:6], kat["out:shuf.minmax"])
+    np.testing.assert_allclose(stats[6:9], kat["out:shuf.avg"], rtol=1e-5)
+
+
+def test_accumulate_matches_reference(kat):
+    p = _params(kat)
+    npix = p["w"] * p["h"]
+    terminal = np.zeros((npix, 4), np.float32)
+    terminal[:, 0:3] = kat["in:acc.ttp"]
+    terminal[:, 3] = (kat["in:acc.hasq"] & 1).astype(np.uint32).view(np.float32)
+    mean = _f(kat["in:acc.prev"]).copy()
+    sums = np.zeros((npix, 3), np.float64)
+    orc.nrc_accumulate(npix, terminal, _f(kat["in:acc.contrib"]), _f(kat["in:acc.inferred"]),
+                       _f(kat["in:acc.query"]), p["radiance_scale"], p["accum_frames"], sums, mean)
+    np.testing.assert_allclose(mean, kat["out:acc.out"].reshape(-1, 3), rtol=2e-6, atol=1e-7)
