@@ -196,10 +196,15 @@ int vpt_download_importance_map(VptContext* ctx, float* host_mips);
 /* Hosek-Wilkie sky texture (renderer/gpu_kernels/analytic_sky_kernels.cu:220-276) from
  * per-band model states computed on the host (16 bands). `states` holds, per band:
  * configs[11][9], radiances[11], emission_correction_factor_sky[11], solar_radius (122 floats);
- * `solar` holds per band the direct solar radiance at the sun's elevation before limb darkening
- * followed by 6 limb-darkening coefficients (7 floats). `cmf` holds xs[16], ys[16], zs[16],
+ * `solar` holds the model's solar-disc data (VPT_SKY_SOLAR_FLOATS floats): the weight of the
+ * upper of the two integer turbidities around the requested turbidity, then for each of the 11
+ * model channels (320..720 nm) the model's direct-radiance tables of the lower and of the upper
+ * turbidity (45 pieces x 4 cubic coefficients each, in the model's order), then the 6
+ * limb-darkening coefficients per channel; the direct solar radiance is evaluated at each disc
+ * texel's own elevation (analytic_sky_kernels.cu:69-214). `cmf` holds xs[16], ys[16], zs[16],
  * center wavelengths[16] and the CMF integral (65 floats). include_solar_disc = 0 leaves the
- * disc out (the configurations model the sun as a separate delta light). */
+ * disc out (the configurations model the sun as a separate delta light; `solar` is then unread). */
+#define VPT_SKY_SOLAR_FLOATS (1 + 11 * 2 * 180 + 11 * 6)
 int vpt_generate_sky(VptContext* ctx, int32_t width, int32_t height, const float* states,
                      const float* solar, const float* cmf, const float sun_direction[3],
                      int32_t include_solar_disc);

@@ -71,6 +71,28 @@ int main(int argc, char** argv) {
             arhosekskymodelstate_free(st);
         }
         printf("]");
+        /* Direct solar radiance with limb darkening around the sun (elevation offsets d, angles
+         * gamma from the sun's centre inside the disc), as the sky kernel evaluates it per texel. */
+        printf(",\n \"solar_kat\": [");
+        int first_s = 1;
+        for (int b = 0; b < kBands; b += 5) {
+            double a = alb >= 0 ? alb : 0.5 * (1.0 - (b + 0.5) / kBands);
+            ArHosekSkyModelState* st = arhosekskymodelstate_alloc_init(elev, turb, a);
+            double wl = center_wavelength(b);
+            if (wl < 320.0) wl = 320.0;
+            if (wl > 720.0) wl = 720.0;
+            const double ds[3] = {-0.004, 0.0, 0.003}, gs[3] = {0.0, 0.002, 0.004};
+            for (int i = 0; i < 3; ++i)
+                for (int g = 0; g < 3; ++g) {
+                    double e = elev + ds[i];
+                    if (e <= 0.0) continue;
+                    double v = arhosekskymodel_solar_radiance_internal2(st, wl, e, gs[g]);
+                    printf("%s[%d, %.9g, %.9g, %.9g]", first_s ? "" : ", ", b, e, gs[g], v);
+                    first_s = 0;
+                }
+            arhosekskymodelstate_free(st);
+        }
+        printf("]");
         if (r == 0) {
             /* Reference radiance at fixed view angles (theta from zenith, gamma from the sun). */
             printf(",\n \"radiance_kat\": [");

@@ -5,7 +5,10 @@ Imported by tests/ only. Follows:
   arhosekskymodel_radiance, restated in renderer/gpu_kernels/analytic_sky_kernels.cu:16-66):
   per-band model state = 11 x 9 configuration values, 11 radiances, 11 sky emission correction
   factors; the radiance at a wavelength interpolates the two neighbouring 40 nm channels;
-* the sky texture (analytic_sky_kernels.cu:220-276, without the solar disc): texel (x, y) ->
+* the solar disc (arhosekskymodel_sr_internal and _solar_radiance_internal2, restated in
+  analytic_sky_kernels.cu:69-191): the model's piecewise-cubic direct solar radiance at the
+  texel's elevation with limb darkening, from the model's coefficient tables;
+* the sky texture (analytic_sky_kernels.cu:220-276, the solar disc optional): texel (x, y) ->
   polar angles (y from the zenith), the lower hemisphere mirrored, 16 bands weighted by the CIE
   1931 CMF integrals into XYZ, XYZ -> linear sRGB (common/basic_types.h:3000-3010), the HSV
   saturation push towards blue (:257-266 with basic_types.h:3114-3160), and the lower hemisphere
@@ -66,6 +69,49 @@ def sky_radiance(state: dict, theta, gamma, wavelength: float, ang: "Angles | No
     return result
 
 
+def sr_internal(solar: np.ndarray, turbidity_index: int, channel: int, elevation):
+    """arhosekskymodel_sr_internal (analytic_sky_kernels.cu:69-97): the direct solar radiance of one
+    channel and integer turbidity, a cubic in the elevation on 45 pieces spaced cubically in
+    elevation. `solar` = the model's solar tables (11 x 1800)."""
+    pieces, order = 45, 4
+    e = np.asarray(elevation, dtype=np.float64)
+    pos = np.minimum(np.floor(np.power(2.0 * e / math.pi, 1.0 / 3.0) * pieces).astype(np.int64), 44)
+    break_x = np.power(pos / pieces, 3.0) * (math.pi * 0.5)
+    x = e - break_x
+    base = order * pieces * turbidity_index + order * (pos + 1) - 1
+    res = np.zeros_like(e)
+    x_exp = np.ones_like(e)
+    for i in range(order):
+        res = res + x_exp * solar[channel][base - i]
+        x_exp = x_exp * x
+    return res
+
+
+def solar_direct(tables: dict, turbidity: float, wavelength: float, elevation, gamma, solar_radius: float):
+    """arhosekskymodel_solar_radiance_internal2 (analytic_sky_kernels.cu:99-184): the solar
+    radiance interpolated between turbidities and channels, times the limb-darkening polynomial."""
+    turb_low = int(turbidity) - 1
+    turb_frac = turbidity - (turb_low + 1)
+    if turb_low == 9:
+        turb_low, turb_frac = 8, 1.0
+    wl_low = int((wavelength - 320.0) / 40.0)
+    wl_frac = math.fmod(wavelength, 40.0) / 40.0
+    if wl_low == 10:
+        wl_low, wl_frac = 9, 1.0
+    sol = tables["solar"]
+    direct = (1.0 - turb_frac) * ((1.0 - wl_frac) * sr_internal(sol, turb_low, wl_low, elevation) +
+                                  wl_frac * sr_internal(sol, turb_low, wl_low + 1, elevation)) + \
+        turb_frac * ((1.0 - wl_frac) * sr_internal(sol, turb_low + 1, wl_low, elevation) +
+                     wl_frac * sr_internal(sol, turb_low + 1, wl_low + 1, elevation))
+    ld = (1.0 - wl_frac) * tables["limb"][wl_low] + wl_frac * tables["limb"][wl_low + 1]
+    sol_rad_sin = math.sin(solar_radius)
+    ar2 = 1.0 / (sol_rad_sin * sol_rad_sin)
+    sc2 = np.maximum(1.0 - ar2 * np.sin(gamma) ** 2, 0.0)
+    c = np.sqrt(sc2)
+    darkening = ld[0] + ld[1] * c + ld[2] * c ** 2 + ld[3] * c ** 3 + ld[4] * c ** 4 + ld[5] * c ** 5
+    return direct * darkening
+
+
 def _rgb_to_hsv(r, g, b):
     mn = np.minimum(np.minimum(r, g), b)
     mx = np.maximum(np.maximum(r, g), b)
@@ -93,12 +139,17 @@ def _hsv_to_rgb(h, s, v):
     return [np.where(grey, v, o) for o in out]
 
 
-def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, sun_dir) -> np.ndarray:
-    """The sky texture without the solar disc: (height, width, 3) float64."""
+def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, sun_dir, disc: dict | None = None,
+                window: tuple | None = None) -> np.ndarray:
+    """The sky texture: (height, width, 3) float64, without the solar disc unless `disc` =
+    {"tables": the model's tables, "turbidity": t} is given (texels within the solar radius of the
+    sun in the upper hemisphere then add the limb-darkened direct radiance, :238-239). `window` =
+    (y0, y1, x0, x1) evaluates only those rows and columns of the texture."""
     bands = [unpack_state(states[b]) for b in range(BANDS)]
     cmf = np.asarray(cmf, dtype=np.float64)
     xs, ys, zs, centers, integral = cmf[:16], cmf[16:32], cmf[32:48], cmf[48:64], cmf[64]
-    yy, xx = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+    y0, y1, x0, x1 = window if window is not None else (0, height, 0, width)
+    yy, xx = np.meshgrid(np.arange(y0, y1), np.arange(x0, x1), indexing="ij")
     theta = math.pi * (yy + 0.5) / height
     phi = 2 * math.pi * (xx + 0.5) / width
     lower = theta >= 0.5 * math.pi
@@ -113,6 +164,12 @@ def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, su
     for b in range(BANDS):
         wl = min(max(float(centers[b]), 320.0), 720.0)
         v = sky_radiance(bands[b], m_theta, gamma, wl, ang)
+        if disc is not None:
+            in_disc = (gamma < bands[b]["solar_radius"]) & ~lower
+            if in_disc.any():
+                v = v.copy()
+                v[in_disc] += solar_direct(disc["tables"], disc["turbidity"], wl, 0.5 * math.pi - m_theta[in_disc],
+                                           gamma[in_disc], float(bands[b]["solar_radius"]))
         X += xs[b] * v
         Y += ys[b] * v
         Z += zs[b] * v

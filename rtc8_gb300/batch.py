@@ -68,6 +68,9 @@ class SceneBatch:
         return sum(c.width * c.height for c in self.configs) * self.graph_spp
 
     def close(self) -> None:
+        for c in getattr(self, "caches", []):
+            c.finalize()
+        self.caches = []
         for r in self.renderers:
             r.close()
         self.renderers = []
@@ -138,6 +141,42 @@ class SceneBatch:
     def step_uncaptured(self, spp: int) -> None:
         """The same step issued launch by launch (for comparison)."""
         self._issue(spp)
+
+    # ------------------------------------------------------------------ radiance caches
+    def enable_caches(self, settings: dict | None = None) -> None:
+        """Gives every scene its own radiance cache (the volume network of rtc8_nrc.h) with the
+        equal-error comparison's settings (rtc8_gb300.convergence.NRC_SETTINGS)."""
+        from . import convergence, nrc
+
+        st = dict(convergence.NRC_SETTINGS, **(settings or {}))
+        self.nrc_settings = st
+        self.caches = []
+        for r in self.renderers:
+            r.nrc_set_query_density(True)
+            r.nrc_set_termination_factor(st["termination"], st.get("train_termination", 0.0))
+            net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+            net.ema_decay, net.learning_rate = st["ema_decay"], st["learning_rate"]
+            cache = nrc.NeuralRadianceCache()
+            cache.initialize(config=net)
+            self.caches.append(cache)
+
+    def nrc_step(self, spp: int, train_iterations: int | None = None, new_sequence: bool = False) -> None:
+        """One radiance-cache frame of every scene (its own cache's training iterations, then `spp`
+        samples per pixel), each scene on its own stream forked from and joined to the caller's.
+        Not captured in a graph: each frame draws the unbiased-path offsets on the host
+        (renderer_main.cpp:1566)."""
+        import torch
+
+        iters = self.nrc_settings.get("train_iterations", 1) if train_iterations is None else train_iterations
+        origin = torch.cuda.current_stream()
+        for r, s, cache in zip(self.renderers, self.streams, self.caches):
+            s.wait_stream(origin)
+            r.nrc_frame(cache, iters, spp, new_sequence, s.cuda_stream)
+        for s in self.streams:
+            origin.wait_stream(s)
+
+    def nrc_errors(self) -> int:
+        return sum(r.device_errors() | c.device_errors() for r, c in zip(self.renderers, self.caches))
 
     def images(self) -> list[np.ndarray]:
         return [r.image() for r in self.renderers]

@@ -82,6 +82,32 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
     return LIB
 
 
+SKY_TABLES = PKG / "data" / "hosek_tables.bin"
+
+
+def generate_sky_tables(ref: Path, force: bool = False) -> Path | None:
+    """Writes data/hosek_tables.bin (the Hosek-Wilkie 2013 spectral model's coefficient tables)
+    from the model's C source in the reference checkout `ref` (ext/hosek_wilkie_2013), if that
+    checkout is present; the file is generated, not committed. Returns its path or None."""
+    src = ref / "ext" / "hosek_wilkie_2013" / "ArHosekSkyModel.c"
+    if not src.exists():
+        return SKY_TABLES if SKY_TABLES.exists() else None
+    gen = PKG / "data" / "hosek_tables_gen.c"
+    if SKY_TABLES.exists() and not force and SKY_TABLES.stat().st_mtime >= gen.stat().st_mtime:
+        return SKY_TABLES
+    BUILD.mkdir(exist_ok=True)
+    exe = BUILD / "hosek_tables_gen"
+    cc = os.environ.get("CC", "gcc")
+    res = subprocess.run([cc, "-O1", "-w", "-std=gnu99", "-I", str(src.parent), str(gen), str(src), "-lm", "-o",
+                          str(exe)], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"sky table generator failed to build:\n{res.stderr}")
+    tmp = SKY_TABLES.with_suffix(".tmp")
+    subprocess.run([str(exe), str(tmp)], check=True)
+    os.replace(tmp, SKY_TABLES)
+    return SKY_TABLES
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv)
     print(LIB)

@@ -176,17 +176,19 @@ NRC_SETTINGS = {"termination": 1.28, "train_termination": 0.08, "ema_decay": 0.0
                 "spp_per_frame": 128, "train_iterations": 4}
 
 
-def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, time_budget: float) -> dict:
+def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, time_budget: float,
+                 plain_chunk: int = 16, eval_every: int = 1) -> dict:
     """One equal-error comparison on `cfg` (its RNG seed) against the oracle image `ref`."""
     from . import nrc
 
     net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
     net.ema_decay = st["ema_decay"]
     net.learning_rate = st["learning_rate"]
-    plain = plain_curve(cfg, ref, target, time_budget=time_budget)
+    plain = plain_curve(cfg, ref, target, chunk_spp=plain_chunk, time_budget=time_budget)
     cache = nrc_curve(cfg, ref, target, net_config=net, spp_per_frame=st["spp_per_frame"], time_budget=time_budget,
                       termination=st["termination"], train_termination=st.get("train_termination", 0.0),
-                      train_iterations=st.get("train_iterations", 1), max_frames=max(16, 16384 // st["spp_per_frame"]))
+                      train_iterations=st.get("train_iterations", 1), eval_every=eval_every,
+                      max_frames=max(16, 16384 // st["spp_per_frame"]))
     out = {"rng_seed": cfg.rng_seed,
            "plain": {"reached": plain["reached"], "first_below": plain["first_below"],
                      "last": plain["curve"][-1] if plain["curve"] else None},
@@ -212,19 +214,21 @@ def _median(xs):
 
 
 def compare(cfg: SceneConfig, target: float = 1e-3, oracle_spp: int = 16384, time_budget: float = 60.0,
-            settings: dict | None = None, seeds: int = 3, extra_settings: dict | None = None) -> dict:
+            settings: dict | None = None, seeds: int = 3, extra_settings: dict | None = None,
+            plain_chunk: int = 16, eval_every: int = 1) -> dict:
     """Time to reach relMSE <= target (held for SUSTAIN evaluations) for both estimators on `cfg`,
     for `seeds` independent RNG seeds of both estimators; the headline is the median speed-up.
     `extra_settings` ({name: overrides}) repeats the radiance-cache runs with other settings."""
     st = dict(NRC_SETTINGS, **(settings or {}))
     ref = oracle_image(cfg, oracle_spp)
-    runs = [compare_once(cfg.replace(rng_seed=cfg.rng_seed + 7919 * (k + 1)), ref, target, st, time_budget)
-            for k in range(seeds)]
+    runs = [compare_once(cfg.replace(rng_seed=cfg.rng_seed + 7919 * (k + 1)), ref, target, st, time_budget,
+                         plain_chunk, eval_every) for k in range(seeds)]
     out = {"target_rel_mse": target, "sustained_evaluations": SUSTAIN, "oracle_spp": oracle_spp,
            "rel_mse_eps": REL_EPS, "nrc_settings": st, "seeds": seeds,
            "speedup": _median([r["speedup"] for r in runs]),
            "speedup_wall": _median([r["speedup_wall"] for r in runs]),
            "speedups": [r["speedup"] for r in runs], "speedups_wall": [r["speedup_wall"] for r in runs],
+           "plain_chunk_spp": plain_chunk, "nrc_eval_every_frames": eval_every,
            "runs": [{k: v for k, v in r.items() if k != "curves"} for r in runs]}
     for name, over in (extra_settings or {}).items():
         st2 = dict(st, **over)

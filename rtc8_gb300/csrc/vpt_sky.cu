@@ -1,7 +1,10 @@
 // Hosek-Wilkie analytic sky texture (renderer/gpu_kernels/analytic_sky_kernels.cu:16-276,
 // itself a device port of ext/hosek_wilkie_2013/ArHosekSkyModel.c v1.4a). The per-band
 // model states are computed on the host by the published model and passed in as plain
-// floats; this file only evaluates the radiance functions per texel.
+// floats with the model's solar tables; this file evaluates the radiance functions per texel,
+// including the direct solar radiance at each disc texel's own elevation.
+#include <memory>
+
 #include "vpt_ctx.h"
 #include "vpt_scene.cuh"
 
@@ -10,20 +13,26 @@ namespace {
 
 constexpr int kBands = 16;
 constexpr int kStateFloats = 122;  // configs[11][9], radiances[11], ecf_sky[11], solar_radius
-constexpr int kSolarFloats = 7;    // direct solar radiance at the sun's elevation, 6 limb coefficients
+constexpr int kChannels = 11;      // 320, 360, ..., 720 nm
+constexpr int kPieces = 45, kOrder = 4;
+constexpr int kSolarTable = kPieces * kOrder;
 
 struct SkyBand {
     float configs[11][9];
     float radiances[11];
     float ecf_sky[11];
     float solar_radius;
-    float solar_direct;
-    float limb[6];
 };
 struct SkyConst {
     SkyBand band[kBands];
     float xs[kBands], ys[kBands], zs[kBands], center_wl[kBands];
     float integral_cmf;
+    // Solar disc: weight of the upper of the two turbidities around the requested one, the
+    // model's piecewise-cubic direct-radiance tables of both per channel (coefficients of a piece
+    // highest order first, as the model stores them) and its limb-darkening coefficients.
+    float turb_frac;
+    float solar[kChannels][2][kSolarTable];
+    float limb[kChannels][6];
 };
 __constant__ SkyConst c_sky;
 
@@ -52,18 +61,51 @@ __device__ __forceinline__ float sky_radiance(const SkyBand& s, float theta, flo
     return result;
 }
 
-// analytic_sky_kernels.cu:157-191 (limb darkening of the solar disc) with the direct solar
-// radiance taken at the sun's own elevation, plus the in-scattered radiance (:194-214).
-__device__ __forceinline__ float solar_radiance(const SkyBand& s, float theta, float gamma, float wavelength) {
+// analytic_sky_kernels.cu:69-97: the direct solar radiance of one channel at one of the two
+// turbidities (slot 0: lower, 1: upper), a cubic in the elevation on 45 pieces.
+__device__ __forceinline__ float sr_internal(int slot, int wl, float elevation) {
+    int pos = static_cast<int>(powf(2.0f * elevation / kPi, 1.0f / 3.0f) * kPieces);
+    if (pos > kPieces - 1) pos = kPieces - 1;
+    const float break_x = powf(static_cast<float>(pos) / static_cast<float>(kPieces), 3.0f) * (kPi * 0.5f);
+    const float* coefs = &c_sky.solar[wl][slot][kOrder * (pos + 1) - 1];
+    float res = 0.0f;
+    const float x = elevation - break_x;
+    float x_exp = 1.0f;
+    for (int i = 0; i < kOrder; ++i) {
+        res += x_exp * *coefs--;
+        x_exp *= x;
+    }
+    return res;  // times the sun's emission correction, 1 for this model state
+}
+
+// analytic_sky_kernels.cu:99-184: interpolated between turbidities and channels, limb-darkened.
+__device__ __forceinline__ float solar_direct(const SkyBand& s, float wavelength, float elevation, float gamma) {
+    const float tf = c_sky.turb_frac;
+    int wl_low = static_cast<int>((wavelength - 320.0f) / 40.0f);
+    float wl_frac = fmodf(wavelength, 40.0f) / 40.0f;
+    if (wl_low == 10) {
+        wl_low = 9;
+        wl_frac = 1.0f;
+    }
+    const float direct =
+        (1.0f - tf) * ((1.0f - wl_frac) * sr_internal(0, wl_low, elevation) + wl_frac * sr_internal(0, wl_low + 1, elevation)) +
+        tf * ((1.0f - wl_frac) * sr_internal(1, wl_low, elevation) + wl_frac * sr_internal(1, wl_low + 1, elevation));
+    float ld[6];
+    for (int i = 0; i < 6; ++i) ld[i] = (1.0f - wl_frac) * c_sky.limb[wl_low][i] + wl_frac * c_sky.limb[wl_low + 1][i];
     const float sol_rad_sin = sinf(s.solar_radius);
     const float ar2 = 1 / (sol_rad_sin * sol_rad_sin);
     const float singamma = sinf(gamma);
     float sc2 = 1.0f - ar2 * singamma * singamma;
     if (sc2 < 0.0f) sc2 = 0.0f;
-    float c = sqrtf(sc2);
-    float darkening = s.limb[0] + s.limb[1] * c + s.limb[2] * powf(c, 2.0f) + s.limb[3] * powf(c, 3.0f) +
-                      s.limb[4] * powf(c, 4.0f) + s.limb[5] * powf(c, 5.0f);
-    return s.solar_direct * darkening + sky_radiance(s, theta, gamma, wavelength);
+    const float c = sqrtf(sc2);
+    const float darkening = ld[0] + ld[1] * c + ld[2] * powf(c, 2.0f) + ld[3] * powf(c, 3.0f) + ld[4] * powf(c, 4.0f) +
+                            ld[5] * powf(c, 5.0f);
+    return direct * darkening;
+}
+
+// analytic_sky_kernels.cu:194-214: direct radiance at the texel's elevation plus the sky.
+__device__ __forceinline__ float solar_radiance(const SkyBand& s, float theta, float gamma, float wavelength) {
+    return solar_direct(s, wavelength, (kPi / 2.0f) - theta, gamma) + sky_radiance(s, theta, gamma, wavelength);
 }
 
 // basic_types.h:3114-3160 (HSV conversions).
@@ -160,7 +202,8 @@ __global__ void sky_kernel(float4* __restrict__ out, int w, int h, float sx, flo
 
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc) {
-    SkyConst sc;
+    std::unique_ptr<SkyConst> owner(new SkyConst);  // 24 KB: kept off the stack
+    SkyConst& sc = *owner;
     for (int b = 0; b < kBands; ++b) {
         const float* st = states + b * kStateFloats;
         SkyBand& d = sc.band[b];
@@ -169,9 +212,15 @@ int generate_sky_texture(float4* out, int w, int h, const float* states, const f
         for (int i = 0; i < 11; ++i) d.radiances[i] = st[99 + i];
         for (int i = 0; i < 11; ++i) d.ecf_sky[i] = st[110 + i];
         d.solar_radius = st[121];
-        d.solar_direct = solar[b * kSolarFloats];
-        for (int i = 0; i < 6; ++i) d.limb[i] = solar[b * kSolarFloats + 1 + i];
     }
+    sc.turb_frac = solar[0];
+    const float* tables = solar + 1;
+    for (int wl = 0; wl < kChannels; ++wl)
+        for (int t = 0; t < 2; ++t)
+            for (int i = 0; i < kSolarTable; ++i) sc.solar[wl][t][i] = tables[(wl * 2 + t) * kSolarTable + i];
+    const float* limb = tables + kChannels * 2 * kSolarTable;
+    for (int wl = 0; wl < kChannels; ++wl)
+        for (int i = 0; i < 6; ++i) sc.limb[wl][i] = limb[wl * 6 + i];
     for (int b = 0; b < kBands; ++b) {
         sc.xs[b] = cmf[b];
         sc.ys[b] = cmf[16 + b];

@@ -148,8 +148,12 @@ class Renderer:
 
     def generate_sky(self, width: int, height: int, states: np.ndarray, solar: np.ndarray, cmf: np.ndarray,
                      sun_dir, include_solar_disc: bool) -> None:
+        from . import sky as _sky
+
         s = np.ascontiguousarray(states, dtype=np.float32)
         so = np.ascontiguousarray(solar, dtype=np.float32)
+        if s.size != _sky.BANDS * _sky.STATE_FLOATS or so.size != _sky.SOLAR_FLOATS:
+            raise ValueError("generate_sky: states must hold 16 x 122 floats and solar SOLAR_FLOATS floats")
         cm = np.ascontiguousarray(cmf, dtype=np.float32)
         d = np.ascontiguousarray(sun_dir, dtype=np.float32)
         check(self.lib.vpt_generate_sky(self.ctx, width, height, ptr(s, C.c_float), ptr(so, C.c_float),
@@ -367,8 +371,8 @@ def setup_scene(r: Renderer, cfg: SceneConfig, volume: np.ndarray | None = None)
         r._dims = tuple(volume.shape)
     if cfg.sky is not None:
         from . import sky as _sky
-        st = _sky.load_sky_state(cfg.sky, cfg.sun_elevation_deg)
         d = sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg)
+        st = _sky.load_sky_state(cfg.sky, cfg.sun_elevation_deg, d)
         r.generate_sky(cfg.sky.width, cfg.sky.height, st["states"], st["solar"], st["cmf"], d,
                        cfg.sky.include_solar_disc)
     elif cfg.env_constant is not None:

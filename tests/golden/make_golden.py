@@ -10,6 +10,8 @@ It builds oracle/_ref/ with oracle/build_ref.sh and writes
                                       quaternion matrices, 16-band CIE CMF integrals)
   tests/golden/ref_nanovdb.json       NanoVDB 32.3 GridBuilder / SampleFromVoxels<1> / Ray::clip
   tests/golden/ref_hosek_kat.json     Hosek-Wilkie radiance at fixed angles (first sky entry)
+  tests/golden/ref_hosek_states.json  Hosek-Wilkie model states and direct solar radiance at six
+                                      further (elevation, turbidity, albedo) combinations
   tests/golden/nvdb/                  .nvdb files written by NanoVDB 32.3 io::writeGrid(s)
                                       (gzip-compressed when uncoded) and ref_nvdb_files.json,
                                       the reference's own reading of them
@@ -34,6 +36,9 @@ DATA = ROOT / "rtc8_gb300" / "data"
 
 # (solar elevation deg, turbidity, ground albedo; negative = the renderer's per-band ramp)
 SKY_REQUESTS = [(20.0, 3.0, 0.3), (30.0, 4.0, -1.0), (20.0, 4.0, -1.0)]
+# More model states of the library, at other elevations, turbidities and albedos (fixture only).
+SKY_CHECKS = [(5.0, 2.0, 0.1), (45.0, 6.5, -1.0), (70.0, 9.3, 0.8), (1.5, 10.0, 0.5), (88.0, 1.0, -1.0),
+              (12.5, 3.7, 0.3)]
 
 
 def run(name: str, *args: str) -> dict:
@@ -56,6 +61,12 @@ def main() -> int:
     (GOLDEN / "ref_hosek_kat.json").write_text(json.dumps({
         "elevation_deg": first["elevation_deg"], "turbidity": first["turbidity"], "albedo": first["albedo"],
         "band_theta_gamma_radiance": kat}))
+    checks = run("ref_hosek_dump", *[str(x) for req in SKY_CHECKS for x in req])
+    (GOLDEN / "ref_hosek_states.json").write_text(json.dumps(
+        {"entries": [{k: e[k] for k in ("elevation_deg", "turbidity", "albedo", "states", "solar_kat")}
+                     for e in checks["entries"]]}))
+    for e in sky["entries"]:
+        e.pop("solar_kat", None)
     nvdb_dir = GOLDEN / "nvdb"
     nvdb_dir.mkdir(exist_ok=True)
     with tempfile.TemporaryDirectory() as tmp:

@@ -43,8 +43,8 @@ DECISION_PARITY = 0.999
 
 
 def oracle_sky(cfg, width: int, height: int) -> np.ndarray:
-    st = psky.load_sky_state(cfg.sky, cfg.sun_elevation_deg)
     d = sun_direction(cfg.sun_elevation_deg, cfg.sun_azimuth_deg)
+    st = psky.load_sky_state(cfg.sky, cfg.sun_elevation_deg, d)
     return osky.sky_texture(width, height, st["states"], st["cmf"], d.astype(np.float32)).astype(np.float32)
 
 
