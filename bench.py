@@ -281,6 +281,13 @@ def mlp_bench(steps: int, warmup: int) -> dict:
     flop_fwd = 2 * (144 * 64 + 4 * 64 * 64 + 64 * 16)
     t_inf = timed(lambda: cache.infer(s.cuda_stream, q, n_inf, out), max(steps, 10))
     t_tr = timed(lambda: cache.train(s.cuda_stream, q, tgt, n_tr), max(steps, 10))
+    # The training kernel at larger batches (one 128-record tile per CTA), to tell the kernel's
+    # capability from the latency bound of the frame's 16384-record steps.
+    big = {}
+    for nb in (65536, 262144):
+        tgt_b = torch.rand((nb, 3), device="cuda", generator=gen)
+        t_b = timed(lambda: cache.train(s.cuda_stream, q, tgt_b, nb), 10)
+        big[str(nb)] = {"train_step_ms": t_b * 1e3, "train_tflops": nb * 3 * flop_fwd / t_b / 1e12}
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
     inf_tf = n_inf * flop_fwd / t_inf / 1e12
@@ -291,10 +298,10 @@ def mlp_bench(steps: int, warmup: int) -> dict:
             "infer_tflops": inf_tf, "infer_frac_of_peak": inf_tf / peak, "train_step_ms": t_tr * 1e3,
             "train_tflops": tr_tf, "train_frac_of_peak": tr_tf / peak,
             "peak_tflops": peak, "peak_source": "measured bf16_tflops (dense FP16 has the same rate)",
-            "infer_records": n_inf, "train_records": n_tr, "device_errors": errors}
+            "infer_records": n_inf, "train_records": n_tr, "train_larger_batches": big, "device_errors": errors}
 
 
-def nrc_frame_loop(frames: int, warmup: int) -> dict:
+def nrc_frame_loop(frames: int, warmup: int, combined: bool = True) -> dict:
     """The radiance-cache frame loop (train_iterations training iterations + spp_per_frame samples
     per frame, the settings of the equal-error comparison) on the 256x256 dense 64^3 scene; returns
     the mean frame time."""
@@ -309,6 +316,7 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
     setup_scene(r, C1)
     r.nrc_set_query_density(True)
     r.nrc_set_termination_factor(st["termination"], st.get("train_termination", 0.0))
+    r.nrc_set_combined_pass(combined)
     net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
     net.ema_decay, net.learning_rate = st["ema_decay"], st["learning_rate"]
     cache = nrc.NeuralRadianceCache()
@@ -326,7 +334,7 @@ def nrc_frame_loop(frames: int, warmup: int) -> dict:
     b.record(s)
     torch.cuda.synchronize()
     out = {"nrc_frame_ms": a.elapsed_time(b) / frames, "frames": frames, "spp_per_frame": st["spp_per_frame"],
-           "train_iterations_per_frame": iters,
+           "train_iterations_per_frame": iters, "combined_pass": combined,
            "device_errors": r.device_errors() | cache.device_errors()}
     cache.finalize()
     r.close()
@@ -471,6 +479,10 @@ def main():
     ap.add_argument("--nrc-equal-error", default="", choices=["", "c5", "c2"],
                     help="only the radiance-cache vs plain equal-error comparison on the 2048^2 stress scene (c5) "
                          "or the 1024^2 sparse scene (c2), one seed")
+    ap.add_argument("--nrc-separate-passes", action="store_true",
+                    help="with --nrc-frames: first training pass and render samples as two launches")
+    ap.add_argument("--leaf-stage", type=int, default=0,
+                    help="per-warp leaf staging in shared memory when this many lanes share a leaf (0 = off)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the stress-scene and batched-scene figures of the default line")
     args = ap.parse_args()
@@ -508,7 +520,7 @@ def main():
         return
     if args.nrc_frames:
         torch.cuda.set_device(local)
-        print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup)), flush=True)
+        print(json.dumps(nrc_frame_loop(args.nrc_frames, warmup, not args.nrc_separate_passes)), flush=True)
         return
     if args.nrc_equal_error:
         torch.cuda.set_device(local)
@@ -520,6 +532,7 @@ def main():
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg)
     r.set_tracker(1 if args.tracker == "wavefront" else 0)
+    r.set_leaf_staging(args.leaf_stage)
     info = r.volume_info()
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream

@@ -39,6 +39,7 @@ extern "C" {
 #define VPT_DEVERR_STEP_CAP 0x1u      /* a tracking segment hit max_steps_per_segment */
 #define VPT_DEVERR_NONFINITE 0x2u     /* a non-finite sample contribution was dropped */
 #define VPT_DEVERR_TRAIN_FULL 0x4u    /* the training-vertex buffer overflowed */
+#define VPT_DEVERR_STAGE_TIMEOUT 0x8u /* a leaf-staging copy did not complete in time (staging stopped) */
 
 typedef struct VptContext VptContext;
 
@@ -317,6 +318,12 @@ int vpt_synchronize(VptContext* ctx, void* stream);
  * as fit) tune the wavefront. Both trackers draw each path's random numbers in the same order. */
 int vpt_set_tracker(VptContext* ctx, int32_t kind, int32_t slots_per_sm, int32_t pass_steps,
                     int32_t track_ctas_per_sm);
+/* Leaf staging of the persistent tracker (majorant-grid mode on sample-parallel streams, and its
+ * logged form): each warp keeps one 8^3 leaf in shared memory, brought in with one bulk
+ * asynchronous copy (cp.async.bulk) whenever at least `min_lanes` of its lanes look up inside
+ * the same leaf in one tracking step; those lanes read their stencils from it. 0 = off (the
+ * default). Decisions and values are those of the unstaged tracker. */
+int vpt_set_leaf_staging(VptContext* ctx, int32_t min_lanes);
 /* Launch shape of the persistent tracker (CTAs per SM, threads per CTA) and the number of
  * parked lanes of a warp that triggers its joint event phase; 0 = defaults (as many 128-thread
  * CTAs as fit: 7 per SM for the plain tracer on sample-parallel streams; park threshold 20 for
@@ -412,6 +419,9 @@ int vpt_accumulate_inferred_batch(VptContext* ctx, void* stream, uint32_t accum_
  * are inferred after the training steps, with the updated network, as in the reference. */
 int vpt_nrc_frame(VptContext* ctx, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
                   int32_t new_sequence);
+/* 1 (default): the combined training + render launch of vpt_nrc_frame described above; 0: the
+ * first training pass and the batched render pass as two launches (smaller kernels each). */
+int vpt_nrc_set_combined_pass(VptContext* ctx, int32_t on);
 
 #ifdef __cplusplus
 }

@@ -119,6 +119,8 @@ _VPT = {
     "vpt_launch_plain": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vpt_launch_plain_logged": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vpt_launch_plain_noalloc": (C.c_int, [C.POINTER(VptNoAllocTrace), C.c_void_p]),
+    "vpt_set_leaf_staging": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vpt_nrc_set_combined_pass": (C.c_int, [C.c_void_p, C.c_int32]),
     "vpt_tonemap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_uint32, C.c_void_p, C.c_void_p]),
     "vpt_download_image_rgba8": (C.c_int, [C.c_void_p, C.c_float, C.c_uint32, c_u32_p]),
     "vpt_reset_accumulation": (C.c_int, [C.c_void_p]),

@@ -333,6 +333,12 @@ int vpt_accumulate_inferred_batch(VptContext* c, void* stream, uint32_t accum_fr
     return VPT_OK;
 }
 
+int vpt_nrc_set_combined_pass(VptContext* c, int32_t on) {
+    if (!c) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_set_combined_pass: null context");
+    c->nrc_combined_pass = on != 0;
+    return VPT_OK;
+}
+
 int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterations, uint32_t spp,
                   int32_t new_sequence) {
     if (!c || !nrc) return fail(VPT_ERR_INVALID_ARGUMENT, "vpt_nrc_frame: null argument");
@@ -344,12 +350,13 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     const bool batched = c->frame.rng_stream_mode == 1 && spp > 0;
     if (batched && (rc = ensure_render_slots(c, spp))) return rc;
     vpt::NrcBuffers& b = *c->nrc;
+    const bool combo = batched && c->nrc_combined_pass;
     for (uint32_t it = 0; it < train_iterations; ++it) {
         c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
         const uint32_t buf = c->nrc_buf_index;
         const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
         if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
-        if (batched && it == 0) {
+        if (combo && it == 0) {
             // The first training pass and the frame's render samples in one launch: the render
             // paths need the network only at their inference, after the training steps below.
             if ((rc = launch_pass(c, s, vpt::kModeComboNrc, buf, spp, 1, true))) return rc;
@@ -372,7 +379,8 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     }
     if (spp == 0) return VPT_OK;
     if (batched) {
-        if (train_iterations == 0 && (rc = launch_pass(c, s, vpt::kModeRenderNrc, 0, spp, 1, true))) return rc;
+        if ((train_iterations == 0 || !combo) && (rc = launch_pass(c, s, vpt::kModeRenderNrc, 0, spp, 1, true)))
+            return rc;
         // Only the slots whose paths ended with a cache query are inferred (the others are not
         // read by the accumulation).
         if (nrc_infer_indexed(net, stream, b.infer_query, b.infer_index, b.counters + 8, npix * spp, b.inferred))

@@ -398,6 +398,13 @@ int vpt_set_frame_params(VptContext* c, const VptFrameParams* p) {
     return VPT_OK;
 }
 
+int vpt_set_leaf_staging(VptContext* c, int32_t min_lanes) {
+    if (!c || min_lanes < 0 || min_lanes > 32)
+        return set_error(VPT_ERR_INVALID_ARGUMENT, "vpt_set_leaf_staging: min_lanes must lie in [0, 32]");
+    c->leaf_stage_min = min_lanes;
+    return VPT_OK;
+}
+
 int vpt_set_launch_shape(VptContext* c, int32_t ctas_per_sm, int32_t threads, int32_t park_threshold) {
     if (!c || ctas_per_sm < 0 || threads < 0 || (threads && (threads % 32 || threads > 128)) || park_threshold < 0 ||
         park_threshold > 32)
@@ -570,6 +577,9 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         tp.maj_in_smem = 1;
         smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
     }
+    // Leaf staging: majorant-grid tracker on sample-parallel streams (and its logged form).
+    const bool stage = c->leaf_stage_min > 0 && grid_maj && (dlog != nullptr || tp.stream_mode == 1);
+    tp.leaf_stage_min = stage ? c->leaf_stage_min : 0;
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
     if (c->tracker == 1 && capture == cudaStreamCaptureStatusNone) {
@@ -583,8 +593,10 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         rc3 = vpt::wf_run(c, tp, grid_maj, smem, s);
         if (rc3) return rc3;
     } else {
-        int ctas = vpt::persistent_grid(c, threads, vpt::plain_kernel_ptr(grid_maj, dlog != nullptr, tp.stream_mode == 1), smem);
-        vpt::launch_plain(tp, grid_maj, ctas, threads, smem, s);
+        const size_t launch_smem = vpt::plain_smem_bytes(smem, stage, threads);
+        const void* kernel = vpt::plain_kernel_ptr(grid_maj, dlog != nullptr, tp.stream_mode == 1, stage);
+        int ctas = vpt::persistent_grid(c, threads, kernel, launch_smem);
+        vpt::launch_plain(tp, grid_maj, ctas, threads, launch_smem, s);
     }
     if (tp.stream_mode == 1)
         vpt::launch_finalize_mean_dev(c->d_sum, c->d_mean, static_cast<uint32_t>(3 * npix), c->d_frame, spp, s);

@@ -44,6 +44,8 @@ struct VptContextImpl {
     int32_t width = 0, height = 0;
     int device = 0, num_sms = 0;
     int32_t ctas_per_sm = 0, threads = 0, park_threshold = 0;
+    int32_t leaf_stage_min = 0;         // > 0: per-warp leaf staging (vpt_set_leaf_staging)
+    bool nrc_combined_pass = true;      // frame: first training pass and render samples in one launch
 
     // per pixel (renderer_main.cpp:80-129)
     uint64_t* d_rng = nullptr;
@@ -117,7 +119,7 @@ int nrc_reseed_train_rng(VptContextImpl* c);
 int upload_sample_jumps(VptContextImpl* c, uint32_t count, cudaStream_t s);
 int generate_sky_texture(float4* out, int w, int h, const float* states, const float* solar, const float* cmf,
                          const float sun_dir[3], int include_disc);
-const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel);
+const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel, bool leaf_stage);
 // Wavefront plain tracer: runs the passes of one launch on `s` (vpt_wavefront.cu).
 int wf_run(VptContextImpl* c, const TraceParams& tp, bool grid_majorant, size_t smem, cudaStream_t s);
 int wf_ensure(VptContextImpl* c, uint32_t slots);

@@ -265,6 +265,120 @@ __device__ __forceinline__ float sample_trilinear(const Grid& g, V3 xyz, LeafCac
     return stencil_lerp(s, v);
 }
 
+// ------------------------------------------------------------------------------ leaf staging
+// Per-warp copy of one 8^3 leaf (2 KB) in shared memory. When at least `min_lanes` lanes of a
+// warp look up inside the same leaf in one tracking step, the leaf is brought in with one bulk
+// asynchronous copy (cp.async.bulk, global -> shared, completion counted in bytes on the warp's
+// mbarrier), and the lanes of that leaf read their eight stencil values from shared memory
+// (the same bits as from global memory, so the decisions do not change).
+constexpr uint32_t kLeafBytes = 512 * sizeof(float);
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+
+struct LeafStage {
+    float* values;    // this warp's buffer (16-byte aligned)
+    uint64_t* bar;    // this warp's mbarrier
+    int32_t key;      // staged leaf's table index; -1 = none, -2 = staging switched off (timeout)
+    int32_t slot;     // its slot (-1: an empty leaf, every value 0)
+    uint32_t phase;   // parity of the next completion of `bar`
+};
+
+__device__ __forceinline__ uint32_t smem_addr32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void stage_bar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Issued by one lane: the previous contents were read by the generic proxy, hence the proxy fence.
+__device__ __forceinline__ void stage_copy(float* dst, const float* src, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(smem_addr32(bar)), "r"(kLeafBytes)
+                 : "memory");
+    (void)state;
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr32(dst)),
+                 "l"(src), "r"(kLeafBytes), "r"(smem_addr32(bar))
+                 : "memory");
+}
+// Bounded wait for the copy's completion (false after kStageWaitLimit polls).
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t phase) {
+    for (uint32_t i = 0; i < kStageWaitLimit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(smem_addr32(bar)), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// sample_trilinear with the warp's staged leaf. Called by all 32 lanes together; `need` says
+// whether this lane wants a value at `xyz`. Sets `timed_out` if a copy did not complete (the
+// warp then stops staging; see the tracker's exit).
+__device__ __forceinline__ float sample_trilinear_staged(const Grid& g, bool need, V3 xyz, LeafCache& cache,
+                                                         LeafStage& st, int min_lanes, bool& timed_out) {
+    const uint32_t lane = threadIdx.x & 31;
+    const Stencil s = stencil_at(g, xyz);
+    const bool cand = need && s.fast;
+    const int key = cand ? s.key : -1 - static_cast<int>(lane);  // non-candidates in groups of one
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const uint32_t score = cand ? (static_cast<uint32_t>(__popc(peers)) << 5) | lane : 0u;
+    const uint32_t best = __reduce_max_sync(0xffffffffu, score);
+    if (st.key != -2 && static_cast<int>(best >> 5) >= min_lanes) {
+        const int best_lane = static_cast<int>(best & 31);
+        const int leaf = __shfl_sync(0xffffffffu, key, best_lane);
+        if (leaf != st.key) {
+            int32_t slot = 0;
+            if (static_cast<int>(lane) == best_lane) slot = stencil_slot(g, s, cache);
+            slot = __shfl_sync(0xffffffffu, slot, best_lane);
+            if (slot >= 0) {
+                __syncwarp();  // every lane's reads of the previous leaf are complete
+                if (lane == 0) stage_copy(st.values, g.leaf_values + static_cast<int64_t>(slot) * 512, st.bar);
+                const bool ok = __all_sync(0xffffffffu, stage_wait(st.bar, st.phase));
+                st.phase ^= 1u;
+                if (ok) {
+                    st.key = leaf;
+                    st.slot = slot;
+                } else {
+                    st.key = -2;
+                    timed_out = true;
+                }
+            } else {
+                st.key = leaf;
+                st.slot = -1;
+            }
+        }
+    }
+    if (!need) return 0.0f;
+    float v[8];
+    if (s.fast && s.key == st.key) {
+        if (st.slot < 0) return 0.0f;
+        const float* p = st.values + (((s.i & 7) << 6) | ((s.j & 7) << 3) | (s.k & 7));
+        v[0] = p[0];
+        v[1] = p[1];
+        v[2] = p[8];
+        v[3] = p[9];
+        v[4] = p[64];
+        v[5] = p[65];
+        v[6] = p[72];
+        v[7] = p[73];
+    } else if (s.fast) {
+        const int32_t slot = stencil_slot(g, s, cache);
+        if (slot < 0) return 0.0f;
+        stencil_load_fast(g, s, slot, v);
+    } else {
+        stencil_load_slow(g, s, v);
+    }
+    return stencil_lerp(s, v);
+}
+
 // util/Ray.h:343-363 + :512-520 (slab test, clipped to the ray's [tmin, tmax]).
 __device__ __forceinline__ bool clip_ray(V3 bmin, V3 bmax, V3 eye, V3 dir, float tmin, float tmax, float* t0o,
                                          float* t1o) {

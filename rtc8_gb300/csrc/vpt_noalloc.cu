@@ -220,7 +220,7 @@ extern "C" int vpt_launch_plain_noalloc(const VptNoAllocTrace* a, void* stream) 
     int dev = 0, sms = 0, occ = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return ctx_set_error(VPT_ERR_CUDA, "vpt_launch_plain_noalloc: device query failed");
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, plain_kernel_ptr(grid_maj, false, tp.stream_mode == 1), threads, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, plain_kernel_ptr(grid_maj, false, tp.stream_mode == 1, false), threads, smem) != cudaSuccess ||
         occ <= 0)
         occ = 1;
     launch_plain(tp, grid_maj, sms * occ, threads, smem, s);

@@ -210,13 +210,15 @@ __device__ __forceinline__ void train_item_to_pixel(uint32_t item, uint32_t w, u
 // from the register allocation.
 constexpr int kStreamsPerPixel = 0, kStreamsSampleParallel = 1, kStreamsRuntime = 2;
 
-template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime>
+// kStage: per-warp leaf staging in shared memory (sample_trilinear_staged; TraceParams::
+// leaf_stage_min lanes in one leaf trigger a bulk copy of that leaf).
+template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime, bool kStage = false>
 __global__ void __launch_bounds__(128, kMode != kModePlain                    ? kNrcCtasPerSm
                                        : kStreams == kStreamsSampleParallel ? kPlainCtasPerSm
                                                                             : kPlainPerPixelCtasPerSm)
     plain_trace_kernel(const TraceParams P) {
     const bool sample_parallel = kStreams == kStreamsRuntime ? P.stream_mode == 1 : kStreams == kStreamsSampleParallel;
-    extern __shared__ float s_maj[];
+    extern __shared__ __align__(128) float s_maj[];
     const Grid& g = P.grid;
     const float* maj_grid = g.maj;
     if constexpr (kGridMajorant) {
@@ -226,6 +228,18 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
             __syncthreads();
             maj_grid = s_maj;
         }
+    }
+    LeafStage stage{nullptr, nullptr, -1, -1, 0u};
+    bool stage_timed_out = false;
+    if constexpr (kStage) {
+        // After the staged majorant grid: the warps' leaf buffers, then their mbarriers.
+        const size_t maj_bytes = P.maj_in_smem ? static_cast<size_t>(g.mx) * g.my * g.mz * sizeof(float) : 0;
+        unsigned char* area = reinterpret_cast<unsigned char*>(s_maj) + (maj_bytes + 127) / 128 * 128;
+        const int warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+        stage.values = reinterpret_cast<float*>(area + static_cast<size_t>(warp) * kLeafBytes);
+        stage.bar = reinterpret_cast<uint64_t*>(area + static_cast<size_t>(warps) * kLeafBytes) + warp;
+        if ((threadIdx.x & 31) == 0) stage_bar_init(stage.bar);
+        __syncwarp();
     }
     const uint32_t num_pixels = static_cast<uint32_t>(P.width) * static_cast<uint32_t>(P.height);
     const float global_maj = P.density_coeff * g.global_majorant;
@@ -802,7 +816,12 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
 
         // ---------------------------------------------------------------- converged lookups
         float density = 0.0f;
-        if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos), leaf_cache);
+        if constexpr (kStage) {
+            density = P.density_coeff * sample_trilinear_staged(g, need_lookup, world_to_index(g, lookup_pos), leaf_cache,
+                                                                 stage, P.leaf_stage_min, stage_timed_out);
+        } else {
+            if (need_lookup) density = P.density_coeff * sample_trilinear(g, world_to_index(g, lookup_pos), leaf_cache);
+        }
 
         // Outcome of one lookup at the lane's current tentative collision (majorant `maj`).
         auto resolve = [&](float dens) {
@@ -837,6 +856,15 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
             }
         };
         if (need_lookup) resolve(density);
+    }
+
+    if constexpr (kStage) {
+        if (stage_timed_out) {
+            // A copy that did not complete may still land in this warp's buffer: wait for it
+            // (again bounded) before the CTA's shared memory is released.
+            err |= VPT_DEVERR_STAGE_TIMEOUT;
+            stage_wait(stage.bar, stage.phase ^ 1u);
+        }
     }
 
     // warp-reduce the work counters
@@ -958,9 +986,20 @@ void pool_majorants(const float* fine, int lx, int ly, int lz, float* out, int m
     pool_majorants_kernel<<<(n + 255) / 256, 256, 0, s>>>(fine, lx, ly, lz, out, mx, my, mz, factor);
 }
 
+size_t plain_smem_bytes(size_t maj_bytes, bool leaf_stage, int threads) {
+    if (!leaf_stage) return maj_bytes;
+    const size_t warps = static_cast<size_t>(threads) / 32;
+    return (maj_bytes + 127) / 128 * 128 + warps * (kLeafBytes + sizeof(uint64_t));
+}
+
 // Logged launches (decision records for the parity tests) follow the stream layout at run time;
-// the production launches use a kernel compiled for their layout.
-const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel) {
+// the production launches use a kernel compiled for their layout. Leaf staging exists for the
+// majorant-grid tracker on sample-parallel streams and for its logged form.
+const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel, bool leaf_stage) {
+    if (leaf_stage && grid_majorant)
+        return logged ? reinterpret_cast<const void*>(plain_trace_kernel<true, true, kModePlain, kStreamsRuntime, true>)
+                      : reinterpret_cast<const void*>(
+                            plain_trace_kernel<true, false, kModePlain, kStreamsSampleParallel, true>);
     if (logged) return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, true, kModePlain>)
                                      : reinterpret_cast<const void*>(plain_trace_kernel<false, true, kModePlain>);
     if (sample_parallel)
@@ -974,7 +1013,12 @@ const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parall
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s) {
     dim3 grid(grid_ctas), block(threads);
     const size_t sm = grid_majorant ? smem : 0;
-    if (p.dlog) {
+    if (p.leaf_stage_min > 0 && grid_majorant && (p.dlog || p.stream_mode == 1)) {
+        if (p.dlog)
+            plain_trace_kernel<true, true, kModePlain, kStreamsRuntime, true><<<grid, block, sm, s>>>(p);
+        else
+            plain_trace_kernel<true, false, kModePlain, kStreamsSampleParallel, true><<<grid, block, sm, s>>>(p);
+    } else if (p.dlog) {
         if (grid_majorant)
             plain_trace_kernel<true, true, kModePlain><<<grid, block, sm, s>>>(p);
         else

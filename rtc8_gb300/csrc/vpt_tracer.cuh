@@ -46,6 +46,7 @@ struct TraceParams {
     const ulonglong2* sample_jumps;  // sample-parallel mode: LCG jump (A, C) of sample stream_base + i
     int32_t maj_in_smem;      // majorant grid staged in dynamic shared memory
     int32_t park_threshold;   // parked lanes that trigger a warp's event phase (0 = default)
+    int32_t leaf_stage_min;   // > 0: per-warp leaf staging when this many lanes look up in one leaf
 
     uint64_t* rng;            // per pixel
     double* sum_rgb;          // 3 per pixel
@@ -68,6 +69,10 @@ struct TraceParams {
 constexpr int kMajSmemCells = 8192;
 
 void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
+// Dynamic shared memory of a plain launch: the staged majorant grid (`maj_bytes`, 0 if not
+// staged) and, with leaf staging, one 2 KB leaf buffer and one mbarrier per warp.
+size_t plain_smem_bytes(size_t maj_bytes, bool leaf_stage, int threads);
+const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel, bool leaf_stage);
 // Radiance-cache render (kModeRenderNrc) or training (kModeTrainNrc) pass.
 void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
                      cudaStream_t s);

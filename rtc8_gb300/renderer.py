@@ -183,6 +183,10 @@ class Renderer:
         """0 = persistent megakernel (default), 1 = wavefront; see vpt_set_tracker."""
         check(self.lib.vpt_set_tracker(self.ctx, kind, slots_per_sm, pass_steps, track_ctas_per_sm), "vpt_set_tracker")
 
+    def set_leaf_staging(self, min_lanes: int) -> None:
+        """Per-warp leaf staging in shared memory (0 = off); see vpt_set_leaf_staging."""
+        check(self.lib.vpt_set_leaf_staging(self.ctx, min_lanes), "vpt_set_leaf_staging")
+
     def set_launch_shape(self, ctas_per_sm: int = 0, threads: int = 0, park_threshold: int = 0) -> None:
         check(self.lib.vpt_set_launch_shape(self.ctx, ctas_per_sm, threads, park_threshold), "vpt_set_launch_shape")
 
@@ -281,6 +285,9 @@ class Renderer:
     def nrc_set_termination_factor(self, render_factor: float, train_factor: float = 0.0) -> None:
         check(self.lib.vpt_nrc_set_termination_factor(self.ctx, render_factor, train_factor),
               "vpt_nrc_set_termination_factor")
+
+    def nrc_set_combined_pass(self, on: bool) -> None:
+        check(self.lib.vpt_nrc_set_combined_pass(self.ctx, int(on)), "vpt_nrc_set_combined_pass")
 
     def nrc_set_query_density(self, on: bool) -> None:
         check(self.lib.vpt_nrc_set_query_density(self.ctx, int(on)), "vpt_nrc_set_query_density")

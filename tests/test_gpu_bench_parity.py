@@ -62,12 +62,13 @@ def add_sun_disc(env: np.ndarray, sun_dir, radius_deg: float, radiance: float) -
     return out
 
 
-def run_pair(cfg, vox, env, spp: int, device_volume: bool = False) -> dict:
-    """Logged GPU launch and the oracle on the same scene; returns both results and the
-    per-sample decision agreement."""
+def run_pair(cfg, vox, env, spp: int, device_volume: bool = False, stage: int = 0) -> dict:
+    """Logged GPU launch (with per-warp leaf staging when `stage` > 0) and the oracle on the same
+    scene; returns both results and the per-sample decision agreement."""
     import torch
 
     r = Renderer(cfg.width, cfg.height)
+    r.set_leaf_staging(stage)
     if device_volume:
         setup_scene(r, cfg)                       # the product's own fBm generator
         got_vox = r.download_volume()
@@ -127,6 +128,14 @@ def test_sparse512_workload_parameters(cuda_device, c2_volume, c2_sky):
     o = res["oracle"]["log"]
     # the workload's features are exercised: long paths, shadow rays, the bounce cap is reachable
     assert o[..., 2].sum() > 0 and np.mean(o[..., 0] >= 10) > 0.05
+
+
+def test_sparse512_workload_leaf_staging(cuda_device, c2_volume, c2_sky):
+    """The same scene traced with per-warp leaf staging."""
+    cfg = C2.replace(width=128, height=128)
+    spp = 4
+    res = run_pair(cfg, c2_volume, c2_sky, spp, stage=6)
+    check_parity(cfg, res, spp, min_vertices=20)
 
 
 def test_sparse512_workload_reference_streams(cuda_device, c2_volume, c2_sky):

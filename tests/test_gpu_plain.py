@@ -20,12 +20,13 @@ pytestmark = pytest.mark.gpu
 DECISION_PARITY = 0.999
 
 
-def _gpu_logged(cfg, vox, env, spp, tracker=0, **tracker_kw):
+def _gpu_logged(cfg, vox, env, spp, tracker=0, stage=0, **tracker_kw):
     import torch
 
     r = Renderer(cfg.width, cfg.height)
     setup_scene(r, cfg, volume=vox)
     r.set_tracker(tracker, **tracker_kw)
+    r.set_leaf_staging(stage)
     if env is not None and cfg.sky is None:
         r.set_environment_rgb(env)
     log = torch.zeros(cfg.width * cfg.height * spp * 4, dtype=torch.int32, device="cuda")
@@ -211,4 +212,18 @@ def test_wavefront_tracker_matches_megakernel(cuda_device, kind):
     np.testing.assert_array_equal(a["rng"], b["rng"])
     np.testing.assert_array_equal(a["sum"], b["sum"])
     np.testing.assert_array_equal(a["mean"], b["mean"])
+    assert a["counters"] == b["counters"] and a["errors"] == b["errors"] == 0
+
+
+@pytest.mark.parametrize("min_lanes", [1, 6])
+def test_leaf_staging_keeps_every_decision(cuda_device, min_lanes):
+    """Per-warp leaf staging (cp.async.bulk copies of shared leaves into shared memory) reads the
+    same values as the unstaged tracker: identical decision logs, lookups and images."""
+    cfg = small_config_mode(size=48, n=40, g=0.8, majorant_mode=1)
+    vox = volume_for(cfg)
+    env = constant_environment(cfg.env_constant)
+    a = _gpu_logged(cfg, vox, env, 4)
+    b = _gpu_logged(cfg, vox, env, 4, stage=min_lanes)
+    np.testing.assert_array_equal(a["log"], b["log"])
+    np.testing.assert_allclose(a["sum"], b["sum"], rtol=1e-12, atol=1e-15)   # FP64 atomics in launch order
     assert a["counters"] == b["counters"] and a["errors"] == b["errors"] == 0
