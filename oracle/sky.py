@@ -140,11 +140,16 @@ def _hsv_to_rgb(h, s, v):
 
 
 def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, sun_dir, disc: dict | None = None,
-                window: tuple | None = None) -> np.ndarray:
+                window: tuple | None = None, cos_gamma_ulps: int | None = None) -> np.ndarray:
     """The sky texture: (height, width, 3) float64, without the solar disc unless `disc` =
     {"tables": the model's tables, "turbidity": t} is given (texels within the solar radius of the
     sun in the upper hemisphere then add the limb-darkened direct radiance, :238-239). `window` =
-    (y0, y1, x0, x1) evaluates only those rows and columns of the texture."""
+    (y0, y1, x0, x1) evaluates only those rows and columns of the texture. With `cos_gamma_ulps`
+    = k the cosine of the view-sun angle is rounded to float32 and moved by k float32 steps before
+    the arccos: the renderer takes that angle as acos of a float32 dot product
+    (analytic_sky_kernels.cu:237), and within the disc (1 - cos < 1e-5) a float32 cosine takes
+    only a few dozen values, so its rounding moves the limb-darkened radiance by percents; a test
+    brackets the float32 result between evaluations at neighbouring cosines."""
     bands = [unpack_state(states[b]) for b in range(BANDS)]
     cmf = np.asarray(cmf, dtype=np.float64)
     xs, ys, zs, centers, integral = cmf[:16], cmf[16:32], cmf[32:48], cmf[48:64], cmf[64]
@@ -156,7 +161,14 @@ def sky_texture(width: int, height: int, states: np.ndarray, cmf: np.ndarray, su
     m_theta = np.where(lower, math.pi - theta, theta)
     view = np.stack([-np.sin(phi) * np.sin(m_theta), np.cos(m_theta), np.cos(phi) * np.sin(m_theta)], axis=-1)
     sd = np.asarray(sun_dir, dtype=np.float64)
-    gamma = np.arccos(np.clip(view @ sd, -1.0, 1.0))
+    cos_gamma = view @ sd
+    if cos_gamma_ulps is not None:
+        c32 = np.clip(cos_gamma, -1.0, 1.0).astype(np.float32)
+        step = np.float32(np.inf) if cos_gamma_ulps > 0 else np.float32(-np.inf)
+        for _ in range(abs(int(cos_gamma_ulps))):
+            c32 = np.nextafter(c32, step)
+        cos_gamma = c32.astype(np.float64)
+    gamma = np.arccos(np.clip(cos_gamma, -1.0, 1.0))
     X = np.zeros_like(theta)
     Y = np.zeros_like(theta)
     Z = np.zeros_like(theta)

@@ -60,9 +60,21 @@ def test_solar_disc_matches_oracle(cuda_device, elevation, turbidity):
     phi = math.atan2(-float(d[0]), float(d[2])) % (2 * math.pi)
     cy, cx = int(theta / math.pi * h), int(phi / (2 * math.pi) * w)
     win = (cy - 12, cy + 12, cx - 12, cx + 12)
-    ref = osky.sky_texture(w, h, st["states"], st["cmf"], d.astype(np.float32),
-                           disc={"tables": sky._coefficients(), "turbidity": turbidity}, window=win)
+    disc = {"tables": sky._coefficients(), "turbidity": turbidity}
+    ref = osky.sky_texture(w, h, st["states"], st["cmf"], d.astype(np.float32), disc=disc, window=win)
     sub = got[win[0]:win[1], win[2]:win[3]]
     lum = sub @ np.array([0.2126729, 0.7151522, 0.0721750])
     assert (lum > 50 * np.median(lum)).sum() >= 8          # the disc is there and bright
-    np.testing.assert_allclose(sub, ref, rtol=2e-3, atol=1e-6)
+    # The renderer takes the view-sun angle as acos of a float32 dot product; inside the disc that
+    # cosine takes only a few dozen float32 values, and one step of it moves the limb-darkened
+    # radiance by percents. Every texel lies within 2e-3 of the oracle evaluated at the float32
+    # cosine or at most 2 float32 steps away from it, and most texels match the rounded cosine.
+    near32 = osky.sky_texture(w, h, st["states"], st["cmf"], d.astype(np.float32), disc=disc, window=win,
+                              cos_gamma_ulps=0)
+    shifted = [osky.sky_texture(w, h, st["states"], st["cmf"], d.astype(np.float32), disc=disc, window=win,
+                                cos_gamma_ulps=k) for k in (-2, -1, 1, 2)]
+    lo = np.minimum.reduce([ref, near32] + shifted)
+    hi = np.maximum.reduce([ref, near32] + shifted)
+    assert np.all(sub >= lo * (1 - 2e-3) - 1e-6) and np.all(sub <= hi * (1 + 2e-3) + 1e-6)
+    near = np.isclose(sub, near32, rtol=2e-3, atol=1e-6).all(axis=-1)
+    assert near.mean() >= 0.97, f"texels within 2e-3 of the float32-cosine oracle: {near.mean():.4f}"
