@@ -165,14 +165,15 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
             "device_errors": errors, "image": img}
 
 
-# Radiance-cache settings of the equal-error comparison, from sweeps on the 64^3 cloud with five
-# RNG seeds that the comparison itself does not use, judged by the sustained criterion: the volume
-# cache of rtc8_nrc.h with Adam lr 5e-3 and the raw weights for inference (an EMA of the weights
-# lagged behind: decay 0.9 -> 0.85x median, 0.99 -> 0.2x); render paths end at path-spread factor
-# 1.28 and biased training suffixes at 0.08; 128 samples per pixel per frame with four training
-# iterations (generate, propagate, shuffle, 4 x 16384-record steps) per frame. Render paths use the
-# configuration's shadow-ray roulette; the training suffixes do not.
-NRC_SETTINGS = {"termination": 1.28, "train_termination": 0.08, "ema_decay": 0.0, "learning_rate": 5e-3,
+# Radiance-cache settings of the equal-error comparison, from sweeps on the 64^3 cloud with RNG
+# seeds that the comparison itself does not use, judged by the sustained criterion: the volume
+# cache of rtc8_nrc.h with Adam lr 5e-3; render paths end at path-spread factor 1.28 and biased
+# training suffixes at 0.08; 128 samples per pixel per frame with four training iterations
+# (generate, propagate, shuffle, 4 x 16384-record steps) per frame; inference with an EMA of the
+# weights at decay 0.8 (over six seeds: median 1.84x, worst 1.55x; raw weights 1.82x, worst 1.34x;
+# decay 0.9 -> 0.85x median, 0.99 -> 0.2x, the average lagging behind the young cache). Render
+# paths use the configuration's shadow-ray roulette; the training suffixes do not.
+NRC_SETTINGS = {"termination": 1.28, "train_termination": 0.08, "ema_decay": 0.8, "learning_rate": 5e-3,
                 "spp_per_frame": 128, "train_iterations": 4}
 
 
