@@ -40,6 +40,7 @@ extern "C" {
 #define VPT_DEVERR_NONFINITE 0x2u     /* a non-finite sample contribution was dropped */
 #define VPT_DEVERR_TRAIN_FULL 0x4u    /* the training-vertex buffer overflowed */
 #define VPT_DEVERR_STAGE_TIMEOUT 0x8u /* a leaf-staging copy did not complete in time (staging stopped) */
+#define VPT_DEVERR_BVH_STACK 0x10u    /* a surface BVH traversal ran out of stack (nodes skipped) */
 
 typedef struct VptContext VptContext;
 
@@ -185,6 +186,71 @@ int vpt_set_volume_nanovdb(VptContext* ctx, const void* grid, uint64_t bytes);
  * renderer/renderer_scene.cpp:2468. A ZIP or BLOSC grid is refused with an error naming the
  * codec: inflate its payload on the host and call vpt_set_volume_nanovdb. */
 int vpt_set_volume_nvdb_file(VptContext* ctx, const char* path, uint64_t grid_index);
+
+/* ---- surfaces ----------------------------------------------------------------------- */
+/* Triangle meshes around and inside the volume: the reference's surface path without OptiX
+ * (closest and any hits through a BVH built on the host, renderer_kernel_common.h:72-294 and
+ * optix_pathtracing_kernels.cu:84-96, 176-195, 216-239, 268-275, 340-356).
+ *
+ * Scene structure as in renderer/renderer_scene.h: a geometry instance is a triangle mesh
+ * with one material; a geometry group is a contiguous range of geometry instances; an
+ * instance places a group with a 3x4 transform (several instances may share a group).
+ *
+ * Materials hold the immediate values of the reference's 1x1 textures: colours in [0, 1] are
+ * stored as 8-bit values (truncated, renderer_scene.cpp:860-900) and read back sRGB-decoded;
+ * roughness and metallic are 8-bit values read back linearly; emittance is an HDR float RGB
+ * (zero = not an emitter). SIMPLE_PBR is what the reference creates for every loaded mesh and
+ * rectangle (renderer_scene.cpp:1202-1255, 1411-1414, 1561-1563): SimplePBR_BRDF with
+ * reflectance 0.5 and smoothness min(1 - roughness, 0.999) (common_renderer_types.h:1924-1985);
+ * LAMBERT is its forceLambertBRDF alternative (:1483-1541). Image textures, normal maps and
+ * opacity are not supported. */
+#define VPT_MATERIAL_SIMPLE_PBR 0
+#define VPT_MATERIAL_LAMBERT 1
+typedef struct VptSurfaceMaterial {
+    int32_t kind;           /* VPT_MATERIAL_* */
+    float base_color[3];    /* SIMPLE_PBR base colour / LAMBERT reflectance (sRGB-encoded) */
+    float roughness;        /* SIMPLE_PBR: occlusion_roughness_metallic.y (default 0.5) */
+    float metallic;         /* SIMPLE_PBR: occlusion_roughness_metallic.z */
+    float emittance[3];     /* linear HDR emittance; all zero = no emitter */
+} VptSurfaceMaterial;
+/* One geometry instance: object-space vertices (9 floats each: position, shading normal,
+ * tangent) and triangles (3 vertex indices each). */
+typedef struct VptSurfaceGeometry {
+    const float* vertices;
+    uint32_t num_vertices;
+    const uint32_t* triangles;
+    uint32_t num_triangles;
+    uint32_t material;
+} VptSurfaceGeometry;
+/* One instance: the group [first_geometry, first_geometry + num_geometries) placed by the
+ * row-major 3x4 object-to-world transform. The light distribution over instances weighs each
+ * by the squared length of the transform's first column (compute_light_probs.cu:88-99); the
+ * density of reaching an emitter uses uniform_scale, the instance's own scale without the
+ * mesh's static transform (Instance::uniformScale, renderer_scene.h:885-898). Normally both
+ * are the same number. */
+typedef struct VptSurfaceInstance {
+    uint32_t first_geometry;
+    uint32_t num_geometries;
+    float transform[12];
+    float uniform_scale;
+} VptSurfaceInstance;
+/* Replaces the context's surfaces (all three arrays HOST memory; num_instances = 0 removes
+ * them). Transforms the vertices to world space, builds the BVH and the light distributions
+ * of the emitting triangles (per triangle luminance(emittance) x object-space area, per
+ * geometry instance, per instance the group's total x scale^2: compute_light_probs.cu:19-137,
+ * renderer_scene.cpp:353-468) and widens the world box (compute_light_probs.cu:139-157).
+ * Plain launches of a context with surfaces run the surface tracer (reference and
+ * configuration modes, either stream layout; not the wavefront tracer, not leaf staging, not
+ * the radiance-cache passes). With surfaces a volume is optional (vpt_clear_volume). */
+int vpt_set_surfaces(VptContext* ctx, const VptSurfaceMaterial* materials, uint32_t num_materials,
+                     const VptSurfaceGeometry* geometries, uint32_t num_geometries,
+                     const VptSurfaceInstance* instances, uint32_t num_instances);
+/* Counts of the current surfaces: world triangles, BVH nodes, emitting triangles, and the
+ * world box (6 floats: min, max) the launches use. Any pointer may be NULL. */
+int vpt_get_surface_info(VptContext* ctx, uint32_t* triangles, uint32_t* bvh_nodes, uint32_t* emitters,
+                         float* world_box);
+/* Removes the density volume (a surface-only scene: the reference without a density grid). */
+int vpt_clear_volume(VptContext* ctx);
 
 /* Image-based environment from an RGB float image (row-major, rows = polar angle from +y).
  * Builds the hierarchical importance map on the device (compute_light_probs.cu:161-211). */
