@@ -88,6 +88,33 @@ class VptNanoVdbInfo(C.Structure):
     ]
 
 
+class VptSurfaceMaterial(C.Structure):
+    """Mirror of ``VptSurfaceMaterial`` (include/rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("kind", C.c_int32), ("base_color", C.c_float * 3), ("roughness", C.c_float), ("metallic", C.c_float),
+        ("emittance", C.c_float * 3),
+    ]
+
+
+class VptSurfaceGeometry(C.Structure):
+    """Mirror of ``VptSurfaceGeometry`` (include/rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("vertices", c_float_p), ("num_vertices", C.c_uint32),
+        ("triangles", C.POINTER(C.c_uint32)), ("num_triangles", C.c_uint32), ("material", C.c_uint32),
+    ]
+
+
+class VptSurfaceInstance(C.Structure):
+    """Mirror of ``VptSurfaceInstance`` (include/rtc8_vpt.h)."""
+
+    _fields_ = [
+        ("first_geometry", C.c_uint32), ("num_geometries", C.c_uint32), ("transform", C.c_float * 12),
+        ("uniform_scale", C.c_float),
+    ]
+
+
 # name -> (restype, argtypes)
 _VPT = {
     "vpt_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -109,6 +136,12 @@ _VPT = {
     "vpt_nanovdb_decode_leaves": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64, c_i32_p, c_float_p, c_i64_p]),
     "vpt_set_volume_nanovdb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "vpt_set_volume_nvdb_file": (C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64]),
+    "vpt_set_surfaces": (C.c_int, [C.c_void_p, C.POINTER(VptSurfaceMaterial), C.c_uint32,
+                                   C.POINTER(VptSurfaceGeometry), C.c_uint32, C.POINTER(VptSurfaceInstance),
+                                   C.c_uint32]),
+    "vpt_get_surface_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                       C.POINTER(C.c_uint32), c_float_p]),
+    "vpt_clear_volume": (C.c_int, [C.c_void_p]),
     "vpt_set_environment_rgb": (C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32]),
     "vpt_get_importance_map_info": (C.c_int, [C.c_void_p, c_i32_p, c_i32_p, c_i32_p, c_i64_p, c_float_p]),
     "vpt_download_importance_map": (C.c_int, [C.c_void_p, c_float_p]),

@@ -131,6 +131,8 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
 // paths also list the slots of the queries they write (infer_index, counters[8]).
 int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
                 bool index_queries = false) {
+    if (c->surf || !c->has_volume)
+        return fail(VPT_ERR_INVALID_ARGUMENT, "the radiance-cache passes need a volume and no surfaces");
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;

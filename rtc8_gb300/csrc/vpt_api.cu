@@ -102,6 +102,7 @@ int vpt_destroy(VptContext* c) {
     if (!c) return VPT_OK;
     c->release_nrc();
     c->release_wf();
+    c->release_surfaces();
     dev_free(&c->d_rng);
     dev_free(&c->d_sum);
     dev_free(&c->d_mean);
@@ -196,18 +197,12 @@ static int build_grid_from_dense(VptContext* c, const float* d_dense, int nx, in
     c->inv_voxel_size = static_cast<float>(1.0 / static_cast<double>(voxel_size));
     for (int a = 0; a < 3; ++a) c->origin[a] = origin[a];
     int n[3] = {nx, ny, nz};
-    float center[3];
-    float r2 = 0;
     for (int a = 0; a < 3; ++a) {
         c->bbox_min[a] = origin[a];
         c->bbox_max[a] = static_cast<float>(origin[a] + static_cast<double>(n[a]) * voxel_size);
-        center[a] = (c->bbox_min[a] + c->bbox_max[a]) * 0.5f;
-        float d = c->bbox_max[a] - center[a];
-        r2 += d * d;
     }
-    // compute_light_probs.cu:139-157: world AABB = grid box (no meshes), radius = |max - centre|.
-    c->world_radius = std::sqrt(r2);
     c->has_volume = true;
+    c->update_world_box();
     c->maj_shift = 0;  // the pooled majorant grid is rebuilt at the next launch
     VPT_CUDA(cudaDeviceSynchronize());
     return VPT_OK;
@@ -467,11 +462,16 @@ static int ensure_majorant_grid(VptContextImpl* c) {
 }
 
 int fill_trace_params(VptContextImpl* c, TraceParams* tp) {
-    if (!c->has_volume || !c->has_frame) return set_error(VPT_ERR_NOT_READY, "volume or frame parameters missing");
-    int rc = ensure_majorant_grid(c);
-    if (rc) return rc;
+    if ((!c->has_volume && !c->surf) || !c->has_frame)
+        return set_error(VPT_ERR_NOT_READY, "volume (or surfaces) or frame parameters missing");
+    if (c->has_volume) {
+        int rc = ensure_majorant_grid(c);
+        if (rc) return rc;
+    }
     const VptFrameParams& f = c->frame;
     std::memset(tp, 0, sizeof(*tp));
+    tp->volume_enabled = c->has_volume ? 1 : 0;
+    if (c->surf) tp->surf = *c->surf;
     Grid& g = tp->grid;
     g.leaf_table = c->d_leaf_table;
     g.leaf_values = c->d_leaf_values;
@@ -571,18 +571,23 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     }
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     int threads = c->threads > 0 ? c->threads : 128;
-    bool grid_maj = c->frame.majorant_mode == 1;
+    bool grid_maj = c->frame.majorant_mode == 1 && c->has_volume;
     size_t smem = 0;
     if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {
         tp.maj_in_smem = 1;
         smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
     }
     // Leaf staging: majorant-grid tracker on sample-parallel streams (and its logged form).
-    const bool stage = c->leaf_stage_min > 0 && grid_maj && (dlog != nullptr || tp.stream_mode == 1);
+    const bool stage = c->leaf_stage_min > 0 && grid_maj && (dlog != nullptr || tp.stream_mode == 1) && !c->surf;
     tp.leaf_stage_min = stage ? c->leaf_stage_min : 0;
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
-    if (c->tracker == 1 && capture == cudaStreamCaptureStatusNone) {
+    if (c->surf) {
+        // Scenes with triangles: the surface form of the persistent tracker.
+        const void* kernel = vpt::surface_kernel_ptr(grid_maj, dlog != nullptr);
+        int ctas = vpt::persistent_grid(c, threads, kernel, smem);
+        vpt::launch_surface(tp, grid_maj, ctas, threads, smem, s);
+    } else if (c->tracker == 1 && capture == cudaStreamCaptureStatusNone) {
         // Wavefront tracer: its passes are issued from the host until every slot retired (not
         // capturable; a stream being captured gets the persistent megakernel below).
         const uint64_t items = tp.stream_mode == 1 ? npix * spp : npix;
@@ -726,18 +731,13 @@ int upload_sparse_grid(VptContextImpl* c, const std::vector<int32_t>& table, int
     // float map (NanoVDB.h:2029-2032, applyInverseMapF).
     c->voxel_size = info.map_mat_f[0];
     c->inv_voxel_size = info.map_inv_mat_f[0];
-    float center[3];
-    float r2 = 0;
     for (int a = 0; a < 3; ++a) {
         c->origin[a] = static_cast<float>(info.map_vec_d[a] + static_cast<double>(lo[a]) * info.map_mat_d[4 * a]);
         c->bbox_min[a] = static_cast<float>(info.world_min[a]);
         c->bbox_max[a] = static_cast<float>(info.world_max[a]);
-        center[a] = (c->bbox_min[a] + c->bbox_max[a]) * 0.5f;
-        float d = c->bbox_max[a] - center[a];
-        r2 += d * d;
     }
-    c->world_radius = std::sqrt(r2);
     c->has_volume = true;
+    c->update_world_box();
     c->maj_shift = 0;  // the pooled majorant grid is rebuilt at the next launch
     VPT_CUDA(cudaDeviceSynchronize());
     return VPT_OK;

@@ -13,6 +13,7 @@ namespace vpt {
 
 struct TraceParams;
 struct NrcBuffers;
+struct Surfaces;
 
 // Per-slot path state of the wavefront tracer (vpt_wavefront.cu), structure of arrays.
 struct WfBuffers {
@@ -97,6 +98,16 @@ struct VptContextImpl {
     uint32_t* wf_pinned = nullptr;
     cudaEvent_t wf_events[8] = {};
     void release_wf();
+
+    // surfaces (vpt_set_surfaces, vpt_surface.cu); device arrays owned through `surf_mem`
+    Surfaces* surf = nullptr;            // host copy of the device view, nullptr = no surfaces
+    std::vector<void*> surf_mem;
+    uint32_t surf_nodes = 0, surf_emitters = 0;
+    float surf_box_min[3] = {0, 0, 0}, surf_box_max[3] = {0, 0, 0};
+    void release_surfaces();
+    // World box and radius from the volume's box and the surfaces' box (compute_light_probs.cu:139-157).
+    void update_world_box();
+    float world_min[3] = {0, 0, 0}, world_max[3] = {0, 0, 0};
 
     NrcBuffers* nrc = nullptr;
     int32_t nrc_query_density = 0;

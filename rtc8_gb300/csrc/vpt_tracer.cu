@@ -27,6 +27,7 @@ enum : uint32_t {
     ST_ESCAPE,       // primary segment left the grid
     ST_END_SAMPLE,   // accumulate, next sample or next item
     ST_DONE,
+    ST_SURFACE,      // surface scenes: the primary segment ended on a triangle
 };
 
 enum : uint32_t {
@@ -64,6 +65,8 @@ constexpr int kNrcParkThreshold = 24;
 constexpr int kPlainCtasPerSm = 7;
 constexpr int kPlainPerPixelCtasPerSm = 5;
 constexpr int kNrcCtasPerSm = 7;
+// The surface tracer carries the hit, the light sample's geometry and a BVH stack per lane.
+constexpr int kSurfCtasPerSm = 4;
 
 struct DdaState {
     int cell[3];
@@ -212,11 +215,19 @@ constexpr int kStreamsPerPixel = 0, kStreamsSampleParallel = 1, kStreamsRuntime 
 
 // kStage: per-warp leaf staging in shared memory (sample_trilinear_staged; TraceParams::
 // leaf_stage_min lanes in one leaf trigger a bulk copy of that leaf).
-template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime, bool kStage = false>
-__global__ void __launch_bounds__(128, kMode != kModePlain                    ? kNrcCtasPerSm
+// kSurfaces: the scene has triangle meshes (TraceParams::surf): every primary segment first
+// finds its closest triangle, volume tracking stops there, surface vertices scatter by their
+// BSDF, NEE also samples the emitting triangles and shadow rays test the triangles for
+// visibility (optix_pathtracing_kernels.cu:84-96, 176-195, 216-239, 268-275, 340-356;
+// renderer_kernel_common.h:72-124, 146-403). Plain mode only.
+template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime, bool kStage = false,
+          bool kSurfaces = false>
+__global__ void __launch_bounds__(128, kSurfaces                              ? kSurfCtasPerSm
+                                       : kMode != kModePlain                  ? kNrcCtasPerSm
                                        : kStreams == kStreamsSampleParallel ? kPlainCtasPerSm
                                                                             : kPlainPerPixelCtasPerSm)
     plain_trace_kernel(const TraceParams P) {
+    static_assert(!kSurfaces || (kMode == kModePlain && !kStage), "surfaces: plain mode without leaf staging");
     const bool sample_parallel = kStreams == kStreamsRuntime ? P.stream_mode == 1 : kStreams == kStreamsSampleParallel;
     extern __shared__ __align__(128) float s_maj[];
     const Grid& g = P.grid;
@@ -281,6 +292,15 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     float area_pdf = 1.0f, vis = 1.0f;
     bool pick_sun = false;
 
+    // Surface scenes: the current primary segment's closest triangle (~0u = none), whether the
+    // current vertex is on a surface, and the shadow ray of a light sample (its origin, the
+    // light-side cosine over the length and the squared distance; 1 and 1 for the environment).
+    uint32_t hit_tri = ~0u;
+    float hit_b1 = 0.0f, hit_b2 = 0.0f;
+    bool at_surface = false;
+    V3 shadow_eye = v3(0, 0, 0);
+    float nee_lp_cos = 1.0f, nee_dist2 = 1.0f;
+
     // Per-lane work counters (32-bit: a lane does far fewer than 2^32 steps in a launch), summed
     // over the warp in 64 bits at the end.
     uint32_t n_lookups = 0, n_vertices = 0, n_samples = 0, n_cells = 0;
@@ -316,6 +336,123 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
     uint32_t prev_vertex = kInvalidVertex;
     RGB nee_value = rgb(0, 0, 0);
     bool unbiased = false, terminal_written = false;
+
+    // NEE set-up of a surface scene at the vertex `origin` (renderer_kernel_common.h:297-358):
+    // the environment group (image or sky, and the sun) against the emitting triangles with
+    // probToSampleEnvLight, the light sample, the triangles' visibility test from the light
+    // towards the vertex, then the shadow segment through the volume.
+    auto surf_nee_setup = [&]() {
+        float u_light = rng.uniform();
+        const float u0 = rng.uniform();
+        const float u1 = rng.uniform();
+        pick_sun = false;
+        const bool areas = P.surf.inst_integral > 0.0f;
+        const bool env_group = P.env_enabled || P.sun.enabled;
+        bool select_env = false;
+        float type_prob = 1.0f;
+        if (env_group) {
+            if (areas) {
+                if (u_light < kProbEnvLight) {
+                    type_prob = kProbEnvLight;
+                    u_light /= type_prob;
+                    select_env = true;
+                } else {
+                    type_prob = 1.0f - kProbEnvLight;
+                    u_light = (u_light - kProbEnvLight) / type_prob;
+                }
+            } else {
+                select_env = true;
+            }
+        }
+        vis = 0.0f;
+        nee_lp_cos = 1.0f;
+        nee_dist2 = 1.0f;
+        bool have_light = env_group || areas;
+        V3 sdir = v3(0, 0, 1);
+        float trace_length = trace_len;
+        if (have_light && select_env) {
+            float light_prob = 1.0f;
+            if (P.sun.enabled && P.env_enabled) {
+                if (u_light < P.sun.select_prob) {
+                    pick_sun = true;
+                    light_prob = P.sun.select_prob;
+                } else {
+                    light_prob = 1.0f - P.sun.select_prob;
+                }
+            } else if (P.sun.enabled) {
+                pick_sun = true;
+            }
+            if (pick_sun) {
+                light_dir = v3(P.sun.dir[0], P.sun.dir[1], P.sun.dir[2]);
+                emittance = rgb(P.sun.irradiance[0], P.sun.irradiance[1], P.sun.irradiance[2]);
+                area_pdf = light_prob;
+            } else {
+                float pdf;
+                const RGB radiance = env_sample(P.env, u0, u1, &light_dir, &pdf);
+                emittance = kPi * radiance;
+                area_pdf = pdf;
+                if (area_pdf == 0.0f) have_light = false;
+                area_pdf *= light_prob;
+            }
+            if (have_light) {
+                area_pdf *= type_prob;
+                sdir = -light_dir;
+                nee_lp_cos = dot(sdir, -light_dir);
+                if (nee_lp_cos <= 0.0f) have_light = false;
+                shadow_eye = origin + trace_len * light_dir;
+            }
+        } else if (have_light) {
+            const AreaSample as = sample_area_light(P.surf, u_light, u0, u1);
+            if (as.area_pdf == 0.0f) {
+                have_light = false;
+            } else {
+                area_pdf = as.area_pdf * type_prob;
+                emittance = as.emittance;
+                sdir = origin - as.pos;
+                const float lp_cos = dot(sdir, as.normal);
+                if (lp_cos <= 0.0f) {
+                    have_light = false;
+                } else {
+                    shadow_eye = offset_ray_origin(as.pos, as.normal);
+                    sdir = origin - shadow_eye;
+                    nee_dist2 = dot(sdir, sdir);
+                    trace_length = sqrtf(nee_dist2);
+                    sdir = sdir * (1.0f / trace_length);
+                    nee_lp_cos = lp_cos / trace_length;
+                    light_dir = -sdir;
+                }
+            }
+        }
+        if (!have_light) {
+            st = ST_NEE_DONE;  // vis = 0: no contribution
+            return;
+        }
+        bool overflow = false;
+        const bool blocked = bvh_any(P.surf, shadow_eye, sdir, 0.0f, trace_length * 0.9999f, &overflow);
+        if (overflow) err |= VPT_DEVERR_BVH_STACK;
+        if (blocked) {
+            st = ST_NEE_DONE;
+            return;
+        }
+        vis = 1.0f;
+        float a, b;
+        if (P.volume_enabled && clip_ray(bmin, bmax, shadow_eye, sdir, 0.0f, trace_length, &a, &b)) {
+            shadow = true;
+            t = fmaxf(0.0f, a);
+            t1 = b;
+            seg_steps = 0;
+            if constexpr (kGridMajorant) {
+                dda_init(g, shadow_eye, sdir, t, &dda);
+                texit = fminf(fminf(dda.tnext[0], dda.tnext[1]), fminf(dda.tnext[2], t1));
+                maj = P.density_coeff * cell_maj(maj_grid, g, dda);
+            } else {
+                maj = global_maj;
+            }
+            st = ST_STEP;
+        } else {
+            st = ST_NEE_DONE;
+        }
+    };
 
     while (true) {
         // Warp-level event batching: lanes whose path reached an event (segment end, collision,
@@ -454,8 +591,21 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     st = ST_END_SAMPLE;
                     break;
                 }
+                // optix_pathtracing_kernels.cu:84-96: the closest triangle bounds the segment.
+                float seg_max = 1e10f;
+                bool in_volume = true;
+                if constexpr (kSurfaces) {
+                    bool overflow = false;
+                    const SurfHit h = bvh_closest(P.surf, origin, dir, 0.0f, 1e10f, &overflow);
+                    if (overflow) err |= VPT_DEVERR_BVH_STACK;
+                    hit_tri = h.tri;
+                    hit_b1 = h.b1;
+                    hit_b2 = h.b2;
+                    if (h.tri != ~0u) seg_max = h.t;
+                    in_volume = P.volume_enabled != 0;
+                }
                 float a, b;
-                if (clip_ray(bmin, bmax, origin, dir, 0.0f, 1e10f, &a, &b)) {
+                if (in_volume && clip_ray(bmin, bmax, origin, dir, 0.0f, seg_max, &a, &b)) {
                     shadow = false;
                     t = fmaxf(0.0f, a);
                     t1 = b;
@@ -469,7 +619,7 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     }
                     st = ST_STEP;
                 } else {
-                    st = ST_ESCAPE;
+                    st = (kSurfaces && hit_tri != ~0u) ? ST_SURFACE : ST_ESCAPE;
                 }
                 break;
             }
@@ -479,11 +629,15 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                 const int r = track_pass<kGridMajorant, kCells>(g, maj_grid, P.density_coeff, t1, seg_dir, rng, t, texit,
                                                                 maj, dda, n_cells);
                 if (r == PASS_LOOKUP) {
-                    const V3 seg_eye = shadow ? origin + trace_len * light_dir : origin;
+                    V3 seg_eye;
+                    if constexpr (kSurfaces)
+                        seg_eye = shadow ? shadow_eye : origin;
+                    else
+                        seg_eye = shadow ? origin + trace_len * light_dir : origin;
                     lookup_pos = seg_eye + seg_dir * t;
                     need_lookup = true;
                 } else if (r == PASS_END) {
-                    st = shadow ? ST_NEE_DONE : ST_ESCAPE;
+                    st = shadow ? ST_NEE_DONE : ((kSurfaces && hit_tri != ~0u) ? ST_SURFACE : ST_ESCAPE);
                 } else {
                     yield = true;  // let the warp's lookups run before crossing more cells
                 }
@@ -496,7 +650,13 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     RGB radiance = env_evaluate(P.env, dir, &hyp_pdf);
                     float mis = 1.0f;
                     if (path_length > 1) {
-                        float light_pdf = (P.sun.enabled ? (1.0f - P.sun.select_prob) : 1.0f) * hyp_pdf;
+                        float sel = P.sun.enabled ? (1.0f - P.sun.select_prob) : 1.0f;
+                        // :140-142: with emitting triangles the environment is picked with
+                        // probToSampleEnvLight.
+                        if constexpr (kSurfaces) {
+                            if (P.surf.inst_integral > 0.0f) sel = P.sun.enabled ? kProbEnvLight * sel : kProbEnvLight;
+                        }
+                        float light_pdf = sel * hyp_pdf;
                         float bsdf_pdf = dir_pdf;
                         mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                     }
@@ -589,6 +749,11 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     }
                 }
                 throughput = rdiv(throughput, continue_prob);
+                if constexpr (kSurfaces) {
+                    at_surface = false;
+                    surf_nee_setup();
+                    break;
+                }
 
                 float u_light = rng.uniform();
                 float u0 = rng.uniform();
@@ -654,7 +819,99 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                 }
                 break;
             }
+            case ST_SURFACE: {
+                if constexpr (kSurfaces) {
+                    // A triangle hit (optix_pathtracing_kernels.cu:176-195): the surface point,
+                    // its emission weighted against area-light sampling (:216-239), Russian
+                    // roulette (:254-268), NEE set-up.
+                    const SurfPoint sp = surface_point(P.surf, hit_tri, hit_b1, hit_b2, P.env_enabled != 0);
+                    const V3 ray_origin = origin;
+                    origin = sp.pos;
+                    const V3 vout_local = to_local(sp.sf, -dir);
+                    const SurfMaterial& mt = P.surf.mats[sp.material];
+                    if (vout_local.z > 0 && mt.emissive) {
+                        const RGB em = rgb(mt.emittance[0], mt.emittance[1], mt.emittance[2]);
+                        float mis = 1.0f;
+                        if (path_length > 1) {
+                            const V3 dv = ray_origin - origin;
+                            const float dist2 = dot(dv, dv);
+                            const float light_pdf = sp.hyp_area_pdf * dist2 / vout_local.z;
+                            const float bsdf_pdf = dir_pdf;
+                            mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+                        }
+                        contribution = contribution + throughput * (em * (mis / kPi));
+                    }
+                    float continue_prob = 1.0f;
+                    if (static_cast<int32_t>(path_length) >= P.rr_start) {
+                        continue_prob = fminf(luminance(throughput) / init_importance, 1.0f);
+                        if (rng.uniform() >= continue_prob) {
+                            end_code = END_RR;
+                            st = ST_END_SAMPLE;
+                            break;
+                        }
+                    }
+                    throughput = rdiv(throughput, continue_prob);
+                    at_surface = true;
+                    surf_nee_setup();
+                } else {
+                    st = ST_ESCAPE;
+                }
+                break;
+            }
             case ST_NEE_DONE: {
+                if constexpr (kSurfaces) {
+                    if (at_surface) {
+                        // renderer_kernel_common.h:385-402 with the surface's BSDF, then BSDF
+                        // sampling and the offset origin of the next ray
+                        // (optix_pathtracing_kernels.cu:340-356).
+                        const SurfPoint sp = surface_point(P.surf, hit_tri, hit_b1, hit_b2, P.env_enabled != 0);
+                        const Bsdf f = make_bsdf(P.surf.mats[sp.material]);
+                        const V3 q = to_local(sp.sf, -dir);
+                        if (vis > 0.0f) {
+                            const V3 sdir = -light_dir;
+                            const V3 vin = to_local(sp.sf, -sdir);
+                            const RGB fs = bsdf_eval(f, q, vin);
+                            const float sp_cos = fabsf(dot(sdir, sp.gn));
+                            RGB nee;
+                            if (pick_sun) {
+                                nee = fs * emittance * (vis * sp_cos / area_pdf);
+                            } else {
+                                float bpdf = bsdf_pdf(f, q, vin) * nee_lp_cos / nee_dist2;
+                                if (!isfinite(bpdf)) bpdf = 0.0f;
+                                const float light_pdf = area_pdf;
+                                const float mis = (light_pdf * light_pdf) / ((bpdf * bpdf) + (light_pdf * light_pdf));
+                                const RGB le = rdiv(emittance, kPi);
+                                const float gterm = nee_lp_cos * sp_cos / nee_dist2;
+                                nee = fs * le * (vis * mis * gterm / area_pdf);
+                            }
+                            contribution = contribution + throughput * nee;
+                        }
+                        if (P.max_bounces > 0 && static_cast<int32_t>(path_length) >= P.max_bounces) {
+                            end_code = END_MAX_BOUNCES;
+                            st = ST_END_SAMPLE;
+                            break;
+                        }
+                        const float u0 = rng.uniform();
+                        const float u1 = rng.uniform();
+                        V3 local;
+                        float pdf;
+                        const RGB fs = bsdf_sample(f, q, u0, u1, &local, &pdf);
+                        if (pdf == 0.0f) {
+                            end_code = END_PDF_ZERO;
+                            st = ST_END_SAMPLE;
+                            break;
+                        }
+                        dir = from_local(sp.sf, local);
+                        const float dot_sgn = dot(dir, sp.gn);
+                        const RGB local_tp = fs * (fabsf(dot_sgn) / pdf);
+                        throughput = throughput * local_tp;
+                        origin = offset_ray_origin(sp.pos, (dot_sgn > 0.0f ? 1.0f : -1.0f) * sp.gn);
+                        dir_pdf = pdf;
+                        at_surface = false;
+                        st = ST_SEGMENT;
+                        break;
+                    }
+                }
                 // renderer_kernel_common.h:385-402, then phase sampling (:341-356).
                 nee_value = rgb(0, 0, 0);
                 if (vis > 0.0f) {
@@ -667,13 +924,16 @@ __global__ void __launch_bounds__(128, kMode != kModePlain                    ? 
                     if (pick_sun) {
                         nee = fs * emittance * (vis / area_pdf);
                     } else {
-                        float lp_cos = dot(sdir, -light_dir);
-                        float bsdf_pdf = pf * lp_cos / 1.0f;
+                        // Surface scenes keep the light-side cosine over the distance and the
+                        // squared distance of an area-light sample (1 for the environment).
+                        float lp_cos = kSurfaces ? nee_lp_cos : dot(sdir, -light_dir);
+                        const float dist2 = kSurfaces ? nee_dist2 : 1.0f;
+                        float bsdf_pdf = pf * lp_cos / dist2;
                         if (!isfinite(bsdf_pdf)) bsdf_pdf = 0.0f;
                         float light_pdf = area_pdf;
                         float mis = (light_pdf * light_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                         RGB le = rdiv(emittance, kPi);
-                        float gterm = lp_cos * 1.0f / 1.0f;
+                        float gterm = lp_cos * 1.0f / dist2;
                         nee = fs * le * (vis * mis * gterm / area_pdf);
                     }
                     if (!(kMayTrain && is_train)) contribution = contribution + throughput * nee;
@@ -1034,6 +1294,24 @@ void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int t
         else
             plain_trace_kernel<false, false, kModePlain, kStreamsPerPixel><<<grid, block, sm, s>>>(p);
     }
+}
+
+template <bool kGridMajorant>
+static const void* surface_kernel_for(bool logged) {
+    return logged ? reinterpret_cast<const void*>(
+                        plain_trace_kernel<kGridMajorant, true, kModePlain, kStreamsRuntime, false, true>)
+                  : reinterpret_cast<const void*>(
+                        plain_trace_kernel<kGridMajorant, false, kModePlain, kStreamsRuntime, false, true>);
+}
+
+const void* surface_kernel_ptr(bool grid_majorant, bool logged) {
+    return grid_majorant ? surface_kernel_for<true>(logged) : surface_kernel_for<false>(logged);
+}
+
+void launch_surface(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s) {
+    const size_t sm = grid_majorant ? smem : 0;
+    void* args[] = {const_cast<TraceParams*>(&p)};
+    cudaLaunchKernel(surface_kernel_ptr(grid_majorant, p.dlog != nullptr), dim3(grid_ctas), dim3(threads), args, sm, s);
 }
 
 const void* nrc_kernel_ptr(int mode, bool grid_majorant) {

@@ -3,6 +3,7 @@
 
 #include "nrc_buffers.cuh"
 #include "vpt_device.cuh"
+#include "vpt_surface.cuh"
 #include "../../include/rtc8_vpt.h"
 
 namespace vpt {
@@ -56,6 +57,10 @@ struct TraceParams {
     unsigned long long* counters;  // lookups, vertices, samples
     unsigned int* error_flags;
 
+    // Surface scenes only (plain_trace_kernel<..., kSurfaces = true>).
+    Surfaces surf;
+    int32_t volume_enabled;   // 0: surfaces without a density grid (no tracking, no draws)
+
     // Radiance-cache passes only.
     NrcBuffers nrc;
     uint32_t nrc_buf;           // training buffer of this frame (nrcBufferIndex)
@@ -73,6 +78,9 @@ void launch_plain(const TraceParams& p, bool grid_majorant, int grid_ctas, int t
 // staged) and, with leaf staging, one 2 KB leaf buffer and one mbarrier per warp.
 size_t plain_smem_bytes(size_t maj_bytes, bool leaf_stage, int threads);
 const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parallel, bool leaf_stage);
+// Plain tracer of scenes with surfaces (either stream layout, logged or not).
+const void* surface_kernel_ptr(bool grid_majorant, bool logged);
+void launch_surface(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
 // Radiance-cache render (kModeRenderNrc) or training (kModeTrainNrc) pass.
 void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
                      cudaStream_t s);
