@@ -37,7 +37,23 @@ class OrcScene(C.Structure):
         ("width", C.c_int32), ("height", C.c_int32),
         ("max_bounces", C.c_int32), ("rr_start", C.c_int32), ("majorant_mode", C.c_int32), ("max_steps", C.c_int32),
         ("stream_mode", C.c_int32), ("maj_shift", C.c_int32), ("shadow_rr", C.c_float),
+        ("surfaces", C.c_void_p), ("volume_disabled", C.c_int32),
     ]
+
+
+class OrcSurfMaterial(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("base_color", C.c_float * 3), ("roughness", C.c_float),
+                ("metallic", C.c_float), ("emittance", C.c_float * 3)]
+
+
+class OrcSurfGeometry(C.Structure):
+    _fields_ = [("vertices", f32p), ("num_vertices", C.c_uint32), ("triangles", u32p), ("num_triangles", C.c_uint32),
+                ("material", C.c_uint32)]
+
+
+class OrcSurfInstance(C.Structure):
+    _fields_ = [("first_geometry", C.c_uint32), ("num_geometries", C.c_uint32), ("transform", C.c_float * 12),
+                ("uniform_scale", C.c_float)]
 
 
 _FUNCS = {
@@ -54,6 +70,13 @@ _FUNCS = {
     "orc_env_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p, f32p]),
     "orc_env_evaluate": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p, f32p]),
     "orc_imp_sample": (None, [C.POINTER(OrcScene), f32p, C.c_int32, f32p]),
+    "orc_surfaces_create": (C.c_void_p, [C.POINTER(OrcSurfMaterial), C.c_uint32, C.POINTER(OrcSurfGeometry),
+                                         C.c_uint32, C.POINTER(OrcSurfInstance), C.c_uint32, f32p]),
+    "orc_surfaces_destroy": (None, [C.c_void_p]),
+    "orc_surface_closest": (None, [C.c_void_p, f32p, f32p, C.c_int32, C.c_float, i32p, f32p]),
+    "orc_surface_any": (None, [C.c_void_p, f32p, f32p, f32p, C.c_int32, i32p]),
+    "orc_bsdf_eval": (None, [C.POINTER(OrcSurfMaterial), f32p, f32p, C.c_int32, f32p, f32p]),
+    "orc_bsdf_sample": (None, [C.POINTER(OrcSurfMaterial), f32p, f32p, C.c_int32, f32p]),
     "orc_phase_sample": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p, f32p]),
     "orc_phase_eval": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p]),
     "orc_polar_yup": (None, [f32p, C.c_int32, f32p]),
@@ -259,6 +282,101 @@ def scene_from_config(cfg, voxels: np.ndarray, env_rgb: np.ndarray | None, **ove
               shadow_rr=cfg.shadow_rr_threshold)
     kw.update(over)
     return make_scene(**kw)
+
+
+def _material(m) -> OrcSurfMaterial:
+    o = OrcSurfMaterial()
+    o.kind = m.kind
+    o.base_color[:] = [float(x) for x in m.base_color]
+    o.roughness, o.metallic = float(m.roughness), float(m.metallic)
+    o.emittance[:] = [float(x) for x in m.emittance]
+    return o
+
+
+class OracleSurfaces:
+    """The oracle's prepared copy of a rtc8_gb300.surfaces.SurfaceScene (freed on close)."""
+
+    def __init__(self, scene):
+        L = lib()
+        mats = (OrcSurfMaterial * len(scene.materials))(*[_material(m) for m in scene.materials])
+        self.keep = []
+        geoms = (OrcSurfGeometry * len(scene.meshes))()
+        for g, mesh in zip(geoms, scene.meshes):
+            v = np.ascontiguousarray(mesh.vertices, dtype=np.float32)
+            t = np.ascontiguousarray(mesh.triangles, dtype=np.uint32)
+            self.keep += [v, t]
+            g.vertices, g.num_vertices = p(v, C.c_float), len(v)
+            g.triangles, g.num_triangles, g.material = p(t, C.c_uint32), len(t), mesh.material
+        insts = (OrcSurfInstance * len(scene.instances))()
+        for d, src in zip(insts, scene.instances):
+            d.first_geometry, d.num_geometries = src.first_geometry, src.num_geometries
+            d.transform[:] = [float(x) for x in np.asarray(src.transform, dtype=np.float32).reshape(12)]
+            d.uniform_scale = float(src.uniform_scale)
+        box = np.zeros(6, dtype=np.float32)
+        self.handle = L.orc_surfaces_create(mats, len(mats), geoms, len(geoms), insts, len(insts), p(box, C.c_float))
+        if not self.handle:
+            raise ValueError("orc_surfaces_create rejected the scene")
+        self.box = box
+
+    def closest(self, org: np.ndarray, d: np.ndarray, tmax: float = 1e10):
+        org = np.ascontiguousarray(org, dtype=np.float32)
+        d = np.ascontiguousarray(d, dtype=np.float32)
+        n = len(org)
+        tri = np.zeros(n, dtype=np.int32)
+        tb = np.zeros((n, 3), dtype=np.float32)
+        lib().orc_surface_closest(self.handle, p(org, C.c_float), p(d, C.c_float), n, tmax, p(tri, C.c_int32),
+                                  p(tb, C.c_float))
+        return tri, tb
+
+    def close(self):
+        if self.handle:
+            lib().orc_surfaces_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+def attach_surfaces(sc: OracleScene, scene, volume_enabled: bool = True) -> OracleSurfaces:
+    """Adds a surface scene to an oracle scene and widens its world box to the union of the
+    volume's box (unless disabled) and the instances' boxes (compute_light_probs.cu:139-157)."""
+    surf = OracleSurfaces(scene)
+    s = sc.scene
+    s.surfaces = surf.handle
+    s.volume_disabled = 0 if volume_enabled else 1
+    lo = surf.box[:3].copy()
+    hi = surf.box[3:].copy()
+    if volume_enabled:
+        lo = np.minimum(lo, np.array(s.bbox_min[:], dtype=np.float32))
+        hi = np.maximum(hi, np.array(s.bbox_max[:], dtype=np.float32))
+    center = (lo + hi) * np.float32(0.5)
+    d = (hi - center).astype(np.float32)
+    r2 = np.float32(0)
+    for a in range(3):
+        r2 = np.float32(r2 + np.float32(d[a] * d[a]))
+        s.world_min[a] = float(lo[a])
+        s.world_max[a] = float(hi[a])
+    s.world_radius = float(np.sqrt(r2))
+    sc.keep.append(surf)
+    return surf
+
+
+def bsdf_eval(material, q: np.ndarray, v: np.ndarray):
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    v = np.ascontiguousarray(v, dtype=np.float32)
+    val = np.zeros((len(q), 3), dtype=np.float32)
+    pdf = np.zeros(len(q), dtype=np.float32)
+    lib().orc_bsdf_eval(C.byref(_material(material)), p(q, C.c_float), p(v, C.c_float), len(q), p(val, C.c_float),
+                        p(pdf, C.c_float))
+    return val, pdf
+
+
+def bsdf_sample(material, q: np.ndarray, u: np.ndarray) -> np.ndarray:
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.zeros((len(q), 7), dtype=np.float32)
+    lib().orc_bsdf_sample(C.byref(_material(material)), p(q, C.c_float), p(u, C.c_float), len(q), p(out, C.c_float))
+    return out
 
 
 def render_plain(sc: OracleScene, rng: np.ndarray, spp: int, accum_base: int = 0, rows=None, threads: int = 0,

@@ -576,6 +576,564 @@ inline RGB next_event(const OrcScene& s, Pcg32& rng, V3 pos, const Frame& fr, fl
     return ret;
 }
 
+}  // namespace
+
+// ------------------------------------------------------------------------------ surfaces
+// The reference's surface path (renderer_kernel_common.h:72-403, common_renderer_types.h:
+// 1265-1307, 1483-1985, compute_light_probs.cu:19-157) restated over prepared world triangles.
+struct OrcSurfaces {
+    struct Mat {
+        int kind;
+        float diffuse[3], specular[3], roughness;
+        float emit[3];
+        bool emissive;
+    };
+    struct Inst {
+        float m[12], nm[9];
+        float uniform_scale;
+        uint32_t first_geom, num_geoms, first_world_tri_of_geom0;
+        std::vector<float> group_w, group_cdf;
+        float group_integral;
+    };
+    struct Geom {
+        uint32_t num_tris, material;
+        std::vector<float> w, cdf;
+        float integral;
+        std::vector<float> nrm, tan;   // object space, 3 per vertex
+        std::vector<uint32_t> tri;     // 3 per triangle
+    };
+    std::vector<Mat> mats;
+    std::vector<Geom> geoms;
+    std::vector<Inst> insts;
+    std::vector<float> inst_w, inst_cdf;
+    float inst_integral = 0;
+    // World triangles: 9 floats each, and their (instance, geometry, primitive).
+    std::vector<float> pos;
+    std::vector<uint32_t> owner_inst, owner_geom, owner_prim;
+    std::vector<uint32_t> inst_geom_first_tri;   // per (instance, geometry of its group): first world triangle
+};
+
+namespace {
+
+float orc_unorm8(float v) {
+    const float sc = 255.0f * v;
+    const uint32_t q = std::min<uint32_t>(sc > 0.0f ? static_cast<uint32_t>(sc) : 0u, 255u);
+    return static_cast<float>(q);
+}
+// sRGB decode of an 8-bit immediate texel (renderer_scene.cpp:1171-1200 read mode NormalizedFloat_sRGB).
+float orc_srgb8(float v) {
+    const double c = orc_unorm8(v) / 255.0;
+    return static_cast<float>(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+}
+
+// The BSDF parameters setupBSDFBody derives from a material's immediate textures
+// (common_renderer_types.h:1524-1541 Lambert; 1924-1933 and 1962-1985 SimplePBR with
+// reflectance 0.5 and smoothness min(1 - roughness, 0.999)).
+OrcSurfaces::Mat decode_material(const OrcSurfMaterial& m) {
+    OrcSurfaces::Mat d{};
+    d.kind = m.kind;
+    float base[3];
+    for (int a = 0; a < 3; ++a) base[a] = orc_srgb8(m.base_color[a]);
+    if (m.kind == 1) {
+        for (int a = 0; a < 3; ++a) {
+            d.diffuse[a] = base[a];
+            d.specular[a] = 0.0f;
+        }
+        d.roughness = 1.0f;
+    } else {
+        const float rough = orc_unorm8(m.roughness) / 255.0f, metal = orc_unorm8(m.metallic) / 255.0f;
+        const float smooth = std::min(1.0f - rough, 0.999f);
+        for (int a = 0; a < 3; ++a) {
+            d.diffuse[a] = base[a] * (1 - metal);
+            d.specular[a] = 0.16f * (0.5f * 0.5f) * (1 - metal) + base[a] * metal;
+        }
+        d.roughness = 1 - smooth;
+    }
+    d.emissive = m.emittance[0] != 0.0f || m.emittance[1] != 0.0f || m.emittance[2] != 0.0f;
+    for (int a = 0; a < 3; ++a) d.emit[a] = m.emittance[a];
+    return d;
+}
+
+V3 cross3(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+float excl_cdf(const std::vector<float>& w, std::vector<float>* cdf) {
+    cdf->resize(w.size());
+    float acc = 0.0f;
+    for (size_t i = 0; i < w.size(); ++i) {
+        (*cdf)[i] = acc;
+        acc = acc + w[i];
+    }
+    return w.empty() ? 0.0f : (*cdf)[w.size() - 1] + w.back();
+}
+
+// DiscreteDistribution1D::sample (common_renderer_types.h:165-188).
+uint32_t dist_sample(const std::vector<float>& w, const std::vector<float>& cdf, float integral, float u, float* prob,
+                     float* remapped) {
+    const uint32_t n = static_cast<uint32_t>(w.size());
+    u *= integral;
+    int idx = 0;
+    uint32_t p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (int d = static_cast<int>(p2 >> 1); d >= 1; d >>= 1) {
+        if (idx + d >= static_cast<int>(n)) continue;
+        if (cdf[idx + d] <= u) idx += d;
+    }
+    const float lc = cdf[idx];
+    const float rc = idx < static_cast<int>(n) - 1 ? cdf[idx + 1] : integral;
+    *remapped = (u - lc) / (rc - lc);
+    *prob = w[idx] / integral;
+    return static_cast<uint32_t>(idx);
+}
+
+V3 xf_point(const float* m, const float* p) {
+    return v3(m[0] * p[0] + m[1] * p[1] + m[2] * p[2] + m[3] * 1.0f, m[4] * p[0] + m[5] * p[1] + m[6] * p[2] + m[7] * 1.0f,
+              m[8] * p[0] + m[9] * p[1] + m[10] * p[2] + m[11] * 1.0f);
+}
+V3 xf_vector(const float* m, V3 v) {
+    return v3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z, m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+V3 xf_normal(const float* nm, V3 n) {
+    return v3(nm[0] * n.x + nm[1] * n.y + nm[2] * n.z, nm[3] * n.x + nm[4] * n.y + nm[5] * n.z,
+              nm[6] * n.x + nm[7] * n.y + nm[8] * n.z);
+}
+V3 tri_vertex(const OrcSurfaces& S, uint32_t t, int k) {
+    const float* q = &S.pos[9 * static_cast<size_t>(t) + 3 * k];
+    return v3(q[0], q[1], q[2]);
+}
+
+// Möller-Trumbore in the order of renderer_kernel_common.h:236-248; two-sided, t in [tmin, tmax].
+bool tri_hit(V3 o, V3 d, V3 p0, V3 p1, V3 p2, float tmin, float tmax, float* t, float* b1, float* b2) {
+    const V3 e1 = p1 - p0, e2 = p2 - p0;
+    const V3 pv = cross3(d, e2);
+    const float det = dot(e1, pv);
+    if (det == 0.0f) return false;
+    const float rdet = 1.0f / det;
+    const V3 tv = o - p0;
+    const float u = dot(tv, pv) * rdet;
+    if (!(u >= 0.0f && u <= 1.0f)) return false;
+    const V3 qv = cross3(tv, e1);
+    const float v = dot(d, qv) * rdet;
+    if (!(v >= 0.0f && u + v <= 1.0f)) return false;
+    const float tt = dot(e2, qv) * rdet;
+    if (!(tt >= tmin && tt <= tmax)) return false;
+    *t = tt;
+    *b1 = u;
+    *b2 = v;
+    return true;
+}
+
+// Closest triangle by exhaustive search; equal distances go to the lower triangle index.
+int32_t closest_hit(const OrcSurfaces& S, V3 o, V3 d, float tmax, float* tout, float* b1o, float* b2o) {
+    int32_t best = -1;
+    float bt = tmax;
+    const uint32_t n = static_cast<uint32_t>(S.owner_inst.size());
+    for (uint32_t t = 0; t < n; ++t) {
+        float tt, b1, b2;
+        if (tri_hit(o, d, tri_vertex(S, t, 0), tri_vertex(S, t, 1), tri_vertex(S, t, 2), 0.0f, bt, &tt, &b1, &b2) &&
+            (best < 0 || tt < bt)) {
+            best = static_cast<int32_t>(t);
+            bt = tt;
+            *b1o = b1;
+            *b2o = b2;
+        }
+    }
+    *tout = bt;
+    return best;
+}
+
+bool any_hit(const OrcSurfaces& S, V3 o, V3 d, float tmax) {
+    const uint32_t n = static_cast<uint32_t>(S.owner_inst.size());
+    for (uint32_t t = 0; t < n; ++t) {
+        float tt, b1, b2;
+        if (tri_hit(o, d, tri_vertex(S, t, 0), tri_vertex(S, t, 1), tri_vertex(S, t, 2), 0.0f, tmax, &tt, &b1, &b2))
+            return true;
+    }
+    return false;
+}
+
+struct SurfPt {
+    V3 pos, gn;
+    Frame sf;
+    float hyp_area_pdf;
+    uint32_t material;
+};
+
+// computeSurfacePoint (renderer_kernel_common.h:72-124).
+SurfPt surface_point(const OrcSurfaces& S, uint32_t tri, float b1, float b2, bool env_enabled) {
+    const OrcSurfaces::Inst& in = S.insts[S.owner_inst[tri]];
+    const OrcSurfaces::Geom& ge = S.geoms[S.owner_geom[tri]];
+    const uint32_t prim = S.owner_prim[tri];
+    const V3 p0 = tri_vertex(S, tri, 0), p1 = tri_vertex(S, tri, 1), p2 = tri_vertex(S, tri, 2);
+    const float b0 = 1 - (b1 + b2);
+    SurfPt sp;
+    sp.pos = b0 * p0 + b1 * p1 + b2 * p2;
+    const V3 gn = cross3(p1 - p0, p2 - p0);
+    const float area = 0.5f * std::sqrt(gn.x * gn.x + gn.y * gn.y + gn.z * gn.z);
+    sp.gn = gn * (1.0f / (2 * area));
+    const uint32_t* vi = &ge.tri[3 * static_cast<size_t>(prim)];
+    auto at = [](const std::vector<float>& a, uint32_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); };
+    const V3 ln = b0 * at(ge.nrm, vi[0]) + b1 * at(ge.nrm, vi[1]) + b2 * at(ge.nrm, vi[2]);
+    const V3 lt = b0 * at(ge.tan, vi[0]) + b1 * at(ge.tan, vi[1]) + b2 * at(ge.tan, vi[2]);
+    sp.sf.n = normalize(xf_normal(in.nm, ln));
+    sp.sf.t = normalize(xf_vector(in.m, lt));
+    sp.sf.b = cross3(sp.sf.n, sp.sf.t);
+    sp.material = ge.material;
+    float light_prob = 1.0f;
+    if (env_enabled) light_prob *= (1 - 0.25f);
+    const float inst_imp = (in.uniform_scale * in.uniform_scale) * in.group_integral;
+    sp.hyp_area_pdf = 0.0f;
+    if (S.inst_integral > 0.0f) {
+        const float inst_prob = inst_imp / S.inst_integral;
+        if (inst_prob != 0.0f) {
+            light_prob *= inst_prob;
+            const float geom_prob = ge.integral / in.group_integral;
+            if (geom_prob != 0.0f) {
+                light_prob *= geom_prob;
+                light_prob *= ge.integral == 0.0f ? 0.0f : ge.w[prim] / ge.integral;
+                sp.hyp_area_pdf = light_prob / area;
+            }
+        }
+    }
+    return sp;
+}
+
+// cosineSampleHemisphere over concentricSampleDisk (common_renderer_types.h:1265-1307).
+V3 cos_hemisphere(float u0, float u1) {
+    const float sx = 2 * u0 - 1, sy = 2 * u1 - 1;
+    float x = 0.0f, y = 0.0f;
+    if (!(sx == 0 && sy == 0)) {
+        float r, th;
+        if (sx >= -sy) {
+            if (sx > sy) {
+                r = sx;
+                th = sy / sx;
+            } else {
+                r = sy;
+                th = 2 - sx / sy;
+            }
+        } else if (sx > sy) {
+            r = -sy;
+            th = 6 + sx / sy;
+        } else {
+            r = -sx;
+            th = 4 + sy / sx;
+        }
+        th *= kPi / 4;
+        x = r * std::cos(th);
+        y = r * std::sin(th);
+    }
+    return v3(x, y, std::sqrt(std::fmax(0.0f, 1.0f - x * x - y * y)));
+}
+
+inline float p5(float x) {
+    const float x2 = x * x;
+    return x * (x2 * x2);
+}
+inline float lerp1(float a, float b, float t) { return (1 - t) * a + t * b; }
+
+// GGX of the dichromatic BRDF (common_renderer_types.h:1595-1650).
+float g_d(float ag, V3 m) {
+    if (m.z <= 0.0f) return 0.0f;
+    const float tmp = m.x * m.x + m.y * m.y + (m.z * ag) * (m.z * ag);
+    return (ag * ag) / (kPi * (tmp * tmp));
+}
+float g_g1(float ag, V3 v, V3 m) {
+    if (dot(v, m) * v.z <= 0) return 0.0f;
+    const float tmp = (ag * ag) * (v.x * v.x + v.y * v.y) / (v.z * v.z);
+    return 2 / (1 + std::sqrt(1 + tmp));
+}
+float g_hc(float ag, V3 v1, V3 v2, V3 m) {
+    const float a1 = (ag * ag) * (v1.x * v1.x + v1.y * v1.y) / (v1.z * v1.z);
+    const float a2 = (ag * ag) * (v2.x * v2.x + v2.y * v2.y) / (v2.z * v2.z);
+    const float l1 = (-1 + std::sqrt(1 + a1)) / 2;
+    const float l2 = (-1 + std::sqrt(1 + a2)) / 2;
+    const float c1 = (dot(v1, m) / v1.z) > 0 ? 1.0f : 0.0f;
+    const float c2 = (dot(v2, m) / v2.z) > 0 ? 1.0f : 0.0f;
+    return c1 * c2 / (1 + l1 + l2);
+}
+float g_pdf(float ag, V3 v, V3 m) { return g_g1(ag, v, m) * std::fabs(dot(v, m)) * g_d(ag, m) / std::fabs(v.z); }
+float g_sample(float ag, V3 v, float u0, float u1, V3* m, float* mpdf) {
+    const V3 sv = normalize(v3(ag * v.x, ag * v.y, v.z));
+    const float d2 = std::sqrt(sv.x * sv.x + sv.y * sv.y);
+    const float rd = 1.0f / d2;
+    const V3 T1 = (sv.z < 0.9999f) ? v3(sv.y * rd, -sv.x * rd, 0) : v3(1, 0, 0);
+    const V3 T2 = v3(T1.y * sv.z, -T1.x * sv.z, d2);
+    const float a = 1.0f / (1.0f + sv.z);
+    const float r = std::sqrt(u0);
+    const float phi = kPi * ((u1 < a) ? u1 / a : 1 + (u1 - a) / (1.0f - a));
+    const float sp = std::sin(phi), cp = std::cos(phi);
+    const float P1 = r * cp;
+    const float P2 = r * sp * ((u1 < a) ? 1.0f : sv.z);
+    V3 mm = P1 * T1 + P2 * T2 + std::sqrt(1.0f - P1 * P1 - P2 * P2) * sv;
+    mm = normalize(v3(ag * mm.x, ag * mm.y, mm.z));
+    *m = mm;
+    const float D = g_d(ag, mm);
+    *mpdf = g_g1(ag, v, mm) * std::fabs(dot(v, mm)) * D / std::fabs(v.z);
+    return D;
+}
+
+struct Brdf {
+    RGB diff, spec;
+    float rough;
+    int kind;
+};
+Brdf brdf_of(const OrcSurfaces::Mat& m) {
+    return Brdf{rgb(m.diffuse[0], m.diffuse[1], m.diffuse[2]), rgb(m.specular[0], m.specular[1], m.specular[2]), m.roughness,
+                m.kind};
+}
+// Lobe selection weights (:1690-1705, non-fitted).
+void lobe_weights(const Brdf& f, float qz, float vz, float* wd, float* ws) {
+    const float vn5 = p5(1 - vz);
+    const float fd90 = 0.5f * f.rough + 2 * f.rough * qz * qz;
+    const float edf = lerp1(1.0f, fd90, vn5);
+    *wd = luminance(f.diff) * (edf * edf) * lerp1(1.0f, 1.0f / 1.51f, f.rough);
+    *ws = lerp1(luminance(f.spec), 1.0f, p5(1 - vz));
+}
+RGB dichro_value(const Brdf& f, float ag, V3 L, V3 V, V3 m, float lh, float D) {
+    const float G = g_hc(ag, L, V, m);
+    const float w = p5(1 - lh);
+    const RGB F = (1 - w) * f.spec + w * rgb(1.0f, 1.0f, 1.0f);
+    RGB spec = F * ((D * G) / (4 * L.z * V.z));
+    if (G == 0) spec = rgb(0, 0, 0);
+    const float fd90 = 0.5f * f.rough + 2 * f.rough * lh * lh;
+    const float fo = lerp1(1.0f, fd90, p5(1 - V.z));
+    const float fi = lerp1(1.0f, fd90, p5(1 - L.z));
+    return f.diff * (fo * fi * lerp1(1.0f, 1.0f / 1.51f, f.rough) / kPi) + spec;
+}
+// sampleF (Lambert :1497-1505, dichromatic :1680-1790).
+RGB brdf_sample(const Brdf& f, V3 q, float u0, float u1, V3* out, float* pdf) {
+    if (f.kind == 1) {
+        V3 d = cos_hemisphere(u0, u1);
+        *pdf = d.z / kPi;
+        if (q.z <= 0.0f) d.z *= -1;
+        *out = d;
+        return div(f.diff, kPi);
+    }
+    const float ag = f.rough * f.rough;
+    const bool entering = q.z >= 0.0f;
+    const V3 V = entering ? q : -q;
+    float wd, ws;
+    lobe_weights(f, q.z, V.z, &wd, &ws);
+    const float sum = wd + ws;
+    if (sum == 0.0f) {
+        *pdf = 0.0f;
+        return rgb(0, 0, 0);
+    }
+    float pd, ps, lh, D;
+    V3 L, m;
+    if (sum * u1 < wd) {
+        const float ud1 = (sum * u1 - 0) / wd;
+        L = cos_hemisphere(u0, ud1);
+        pd = L.z / kPi;
+        m = normalize(L + V);
+        lh = std::fmin(dot(L, m), 1.0f);
+        ps = (1.0f / (4 * lh)) * g_pdf(ag, V, m);
+        D = g_d(ag, m);
+    } else {
+        const float ud1 = (sum * u1 - wd) / ws;
+        float mp;
+        D = g_sample(ag, V, u0, ud1, &m, &mp);
+        const float vh = std::fmin(dot(V, m), 1.0f);
+        lh = vh;
+        L = (2 * vh) * m - V;
+        if (L.z * V.z <= 0) {
+            *pdf = 0.0f;
+            return rgb(0, 0, 0);
+        }
+        ps = (1.0f / (4 * lh)) * mp;
+        pd = L.z / kPi;
+    }
+    const RGB val = dichro_value(f, ag, L, V, m, lh, D);
+    *out = entering ? L : -L;
+    *pdf = (pd * wd + ps * ws) / sum;
+    return val;
+}
+// evaluateF and evaluatePDF (Lambert :1506-1517, dichromatic :1792-1875).
+RGB brdf_eval(const Brdf& f, V3 q, V3 s) {
+    if (f.kind == 1) return (q.z * s.z > 0) ? div(f.diff, kPi) : rgb(0, 0, 0);
+    if (s.z * q.z <= 0) return rgb(0, 0, 0);
+    const float ag = f.rough * f.rough;
+    const bool entering = q.z >= 0.0f;
+    const V3 V = entering ? q : -q, L = entering ? s : -s;
+    const V3 m = normalize(L + V);
+    return dichro_value(f, ag, L, V, m, dot(L, m), g_d(ag, m));
+}
+float brdf_pdf(const Brdf& f, V3 q, V3 s) {
+    if (f.kind == 1) return (q.z * s.z > 0) ? std::fabs(s.z) / kPi : 0.0f;
+    const float ag = f.rough * f.rough;
+    const bool entering = q.z >= 0.0f;
+    const V3 V = entering ? q : -q, L = entering ? s : -s;
+    const V3 m = normalize(L + V);
+    const float common = 1.0f / (4 * dot(L, m));
+    float wd, ws;
+    lobe_weights(f, q.z, V.z, &wd, &ws);
+    const float sum = wd + ws;
+    if (sum == 0.0f) return 0.0f;
+    return ((L.z / kPi) * wd + (common * g_pdf(ag, V, m)) * ws) / sum;
+}
+
+// offsetRayOrigin (common_renderer_types.h:1324-1349).
+float offset1(float p, float n) {
+    const int32_t oi = static_cast<int32_t>(256.0f * n);
+    int32_t bits;
+    std::memcpy(&bits, &p, 4);
+    bits += (p < 0 ? -oi : oi);
+    float p1;
+    std::memcpy(&p1, &bits, 4);
+    const float p2 = p + (1.0f / 65536.0f) * n;
+    return std::fabs(p) < (1.0f / 32.0f) ? p2 : p1;
+}
+V3 offset_origin(V3 p, V3 n) { return v3(offset1(p.x, n.x), offset1(p.y, n.y), offset1(p.z, n.z)); }
+
+// sampleLight<false> over the emitting triangles (renderer_kernel_common.h:146-290).
+bool sample_area(const OrcSurfaces& S, float ul, float u0, float u1, V3* pos, V3* nrm, RGB* emit, float* area_pdf) {
+    float light_prob = 1.0f;
+    float inst_prob, ug;
+    const uint32_t ii = dist_sample(S.inst_w, S.inst_cdf, S.inst_integral, ul, &inst_prob, &ug);
+    light_prob *= inst_prob;
+    if (inst_prob == 0.0f) return false;
+    const OrcSurfaces::Inst& in = S.insts[ii];
+    float geom_prob, up;
+    const uint32_t gi = dist_sample(in.group_w, in.group_cdf, in.group_integral, ug, &geom_prob, &up);
+    light_prob *= geom_prob;
+    if (geom_prob == 0.0f) return false;
+    const OrcSurfaces::Geom& ge = S.geoms[in.first_geom + gi];
+    float prim_prob, unused;
+    const uint32_t prim = dist_sample(ge.w, ge.cdf, ge.integral, up, &prim_prob, &unused);
+    light_prob *= prim_prob;
+    const uint32_t tri = S.inst_geom_first_tri[in.first_world_tri_of_geom0 + gi] + prim;
+    const V3 p0 = tri_vertex(S, tri, 0), p1 = tri_vertex(S, tri, 1), p2 = tri_vertex(S, tri, 2);
+    const V3 gnv = cross3(p1 - p0, p2 - p0);
+    float t0 = 0.5f * u0, t1 = 0.5f * u1;
+    const float off = t1 - t0;
+    if (off > 0)
+        t1 += off;
+    else
+        t0 -= off;
+    const float t2 = 1 - (t0 + t1);
+    *area_pdf = light_prob * (2.0f / std::sqrt(gnv.x * gnv.x + gnv.y * gnv.y + gnv.z * gnv.z));
+    *pos = t0 * p0 + t1 * p1 + t2 * p2;
+    const uint32_t* vi = &ge.tri[3 * static_cast<size_t>(prim)];
+    auto at = [](const std::vector<float>& a, uint32_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); };
+    *nrm = normalize(xf_normal(in.nm, t0 * at(ge.nrm, vi[0]) + t1 * at(ge.nrm, vi[1]) + t2 * at(ge.nrm, vi[2])));
+    const OrcSurfaces::Mat& mt = S.mats[ge.material];
+    *emit = mt.emissive ? rgb(mt.emit[0], mt.emit[1], mt.emit[2]) : rgb(0, 0, 0);
+    return true;
+}
+
+// performNextEventEstimation (renderer_kernel_common.h:297-403) in a scene with surfaces: the
+// environment (with the sun of the configuration mode) against the emitting triangles with
+// probToSampleEnvLight, triangle visibility, then ratio tracking through the volume. At a
+// medium vertex `surf` is null and `fr` is the phase frame; at a surface vertex `surf` holds the
+// point and `f`, `q` its BSDF and query direction.
+RGB next_event_surf(const OrcScene& s, Pcg32& rng, V3 pos, const Frame& fr, const SurfPt* surf, const Brdf* f, V3 q,
+                    uint32_t* shadow_steps, int64_t* lookups, bool* capped) {
+    const OrcSurfaces& S = *s.surfaces;
+    float u_light = rng.uniform();
+    const float u0 = rng.uniform();
+    const float u1 = rng.uniform();
+    const bool areas = S.inst_integral > 0.0f;
+    const bool env_group = s.env_enabled || s.sun_enabled;
+    if (!env_group && !areas) return rgb(0, 0, 0);
+    bool select_env = false;
+    float type_prob = 1.0f;
+    if (env_group) {
+        if (areas) {
+            if (u_light < 0.25f) {
+                type_prob = 0.25f;
+                u_light /= type_prob;
+                select_env = true;
+            } else {
+                type_prob = 1.0f - 0.25f;
+                u_light = (u_light - 0.25f) / type_prob;
+            }
+        } else {
+            select_env = true;
+        }
+    }
+    bool pick_sun = false;
+    RGB emittance;
+    float area_pdf, lp_cos, dist2 = 1.0f, trace_length = 2 * s.world_radius;
+    V3 light_point, sdir;
+    if (select_env) {
+        float light_prob = 1.0f;
+        if (s.sun_enabled && s.env_enabled) {
+            if (u_light < s.sun_prob) {
+                pick_sun = true;
+                light_prob = s.sun_prob;
+            } else {
+                light_prob = 1.0f - s.sun_prob;
+            }
+        } else if (s.sun_enabled) {
+            pick_sun = true;
+        }
+        V3 light_dir;
+        if (pick_sun) {
+            light_dir = v3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]);
+            emittance = rgb(s.sun_irradiance[0], s.sun_irradiance[1], s.sun_irradiance[2]);
+            area_pdf = light_prob;
+        } else {
+            float dp;
+            const RGB radiance = env_sample(s, u0, u1, &light_dir, &dp);
+            emittance = kPi * radiance;
+            area_pdf = dp;
+            if (area_pdf == 0.0f) return rgb(0, 0, 0);
+            area_pdf *= light_prob;
+        }
+        area_pdf *= type_prob;
+        sdir = -light_dir;
+        lp_cos = dot(sdir, -light_dir);
+        if (lp_cos <= 0.0f) return rgb(0, 0, 0);
+        light_point = pos + trace_length * light_dir;
+    } else {
+        V3 lp, ln;
+        if (!sample_area(S, u_light, u0, u1, &lp, &ln, &emittance, &area_pdf)) return rgb(0, 0, 0);
+        if (area_pdf == 0.0f) return rgb(0, 0, 0);
+        area_pdf *= type_prob;
+        sdir = pos - lp;
+        lp_cos = dot(sdir, ln);
+        if (lp_cos <= 0.0f) return rgb(0, 0, 0);
+        light_point = offset_origin(lp, ln);
+        sdir = pos - light_point;
+        dist2 = dot(sdir, sdir);
+        trace_length = std::sqrt(dist2);
+        sdir = sdir * (1.0f / trace_length);
+        lp_cos /= trace_length;
+    }
+    if (any_hit(S, light_point, sdir, trace_length * 0.9999f)) return rgb(0, 0, 0);
+    float vis = 1.0f;
+    float t0, t1;
+    if (!s.volume_disabled && clip_ray(s.bbox_min, s.bbox_max, light_point, sdir, 0.0f, trace_length, &t0, &t1)) {
+        float t = std::fmax(0.0f, t0);
+        if (track(s, rng, light_point, sdir, &t, t1, true, &vis, shadow_steps, lookups) == SEG_CAP) {
+            *capped = true;
+            return rgb(0, 0, 0);
+        }
+    }
+    if (!(vis > 0.0f)) return rgb(0, 0, 0);
+    RGB fs;
+    float bsdf_pdf, sp_cos;
+    if (surf) {
+        const V3 vin = to_local(surf->sf, -sdir);
+        fs = brdf_eval(*f, q, vin);
+        bsdf_pdf = brdf_pdf(*f, q, vin);
+        sp_cos = std::fabs(dot(sdir, surf->gn));
+    } else {
+        const V3 vin = to_local(fr, -sdir);
+        const float pf = phase_pdf(s.phase_kind, s.phase_param, vin);
+        fs = rgb(s.albedo, s.albedo, s.albedo) * pf;
+        bsdf_pdf = pf;
+        sp_cos = 1.0f;
+    }
+    if (pick_sun) return fs * emittance * (surf ? vis * sp_cos / area_pdf : vis / area_pdf);
+    float bp = bsdf_pdf * lp_cos / dist2;
+    if (!std::isfinite(bp)) bp = 0.0f;
+    const float mis = (area_pdf * area_pdf) / ((bp * bp) + (area_pdf * area_pdf));
+    const RGB le = div(emittance, kPi);
+    const float g = surf ? lp_cos * sp_cos / dist2 : lp_cos * 1.0f / dist2;
+    return fs * le * (vis * mis * g / area_pdf);
+}
+
 // RadianceQuery of an in-medium vertex (optix_pathtracing_kernels.cu:14-29; the medium's
 // surface parameters are common_renderer_types.h:2133-2140): position in the world box,
 // normal = vOut (polar angles, slots in the reference's order), roughness 0 (or the local
@@ -646,8 +1204,16 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
         }
         bool collided = false;
         float hit_dist = 1e10f;
+        // optix_pathtracing_kernels.cu:84-96: the closest triangle bounds the segment.
+        int32_t hit_tri = -1;
+        float hb1 = 0.0f, hb2 = 0.0f;
+        if (s.surfaces) {
+            float th;
+            hit_tri = closest_hit(*s.surfaces, origin, dir, 1e10f, &th, &hb1, &hb2);
+            if (hit_tri >= 0) hit_dist = th;
+        }
         float t0, t1;
-        if (clip_ray(s.bbox_min, s.bbox_max, origin, dir, 0.0f, hit_dist, &t0, &t1)) {
+        if (!s.volume_disabled && clip_ray(s.bbox_min, s.bbox_max, origin, dir, 0.0f, hit_dist, &t0, &t1)) {
             float t = std::fmax(0.0f, t0);
             float unused = 1.0f;
             SegEnd e = track(s, rng, origin, dir, &t, t1, false, &unused, &rec[1], lookups);
@@ -660,6 +1226,62 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                 hit_dist = t;
             }
         }
+        if (!collided && hit_tri >= 0) {
+            // A triangle hit: surface point, emission against area-light sampling (:216-239),
+            // Russian roulette, NEE, BSDF sampling and the offset origin (:254-356).
+            const OrcSurfaces& S = *s.surfaces;
+            const SurfPt sp = surface_point(S, static_cast<uint32_t>(hit_tri), hb1, hb2, s.env_enabled != 0);
+            const V3 ray_origin = origin;
+            const V3 q = to_local(sp.sf, -dir);
+            const OrcSurfaces::Mat& mt = S.mats[sp.material];
+            if (q.z > 0 && mt.emissive) {
+                float mis = 1.0f;
+                if (path_length > 1) {
+                    const V3 dv = ray_origin - sp.pos;
+                    const float dist2 = dot(dv, dv);
+                    const float light_pdf = sp.hyp_area_pdf * dist2 / q.z;
+                    const float bsdf_pdf = dir_pdf;
+                    mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
+                }
+                contribution = contribution + throughput * (rgb(mt.emit[0], mt.emit[1], mt.emit[2]) * (mis / kPi));
+            }
+            float continue_prob = 1.0f;
+            if (static_cast<int32_t>(path_length) >= s.rr_start) {
+                continue_prob = std::fmin(luminance(throughput) / init_importance, 1.0f);
+                if (rng.uniform() >= continue_prob) {
+                    end_code = ORC_END_RR;
+                    break;
+                }
+            }
+            throughput = div(throughput, continue_prob);
+            const Brdf f = brdf_of(mt);
+            bool capped = false;
+            const RGB nee = next_event_surf(s, rng, sp.pos, sp.sf, &sp, &f, q, &rec[2], lookups, &capped);
+            if (capped) {
+                end_code = ORC_END_STEP_CAP;
+                break;
+            }
+            contribution = contribution + throughput * nee;
+            if (s.max_bounces > 0 && static_cast<int32_t>(path_length) >= s.max_bounces) {
+                end_code = ORC_END_MAX_BOUNCES;
+                break;
+            }
+            const float u0 = rng.uniform();
+            const float u1 = rng.uniform();
+            V3 local;
+            float pdf;
+            const RGB fs = brdf_sample(f, q, u0, u1, &local, &pdf);
+            if (pdf == 0.0f) {
+                end_code = ORC_END_PDF_ZERO;
+                break;
+            }
+            dir = from_local(sp.sf, local);
+            const float dot_sgn = dot(dir, sp.gn);
+            throughput = throughput * (fs * (std::fabs(dot_sgn) / pdf));
+            origin = offset_origin(sp.pos, (dot_sgn > 0.0f ? 1.0f : -1.0f) * sp.gn);
+            dir_pdf = pdf;
+            continue;
+        }
         if (!collided) {
             // optix_pathtracing_kernels.cu:130-174 (environment hit with MIS).
             if (s.env_enabled) {
@@ -667,7 +1289,10 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                 RGB radiance = env_evaluate(s, dir, &hyp_pdf);
                 float mis = 1.0f;
                 if (path_length > 1) {
-                    float light_pdf = (s.sun_enabled ? (1.0f - s.sun_prob) : 1.0f) * hyp_pdf;
+                    float sel = s.sun_enabled ? (1.0f - s.sun_prob) : 1.0f;
+                    // :140-142: with emitting triangles the environment is picked with probToSampleEnvLight.
+                    if (s.surfaces && s.surfaces->inst_integral > 0.0f) sel = s.sun_enabled ? 0.25f * sel : 0.25f;
+                    float light_pdf = sel * hyp_pdf;
                     float bsdf_pdf = dir_pdf;
                     mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                 }
@@ -744,7 +1369,8 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
         // cache's targets.
         OrcScene s_nee = s;
         if (train) s_nee.shadow_rr = 0.0f;
-        RGB nee = next_event(s_nee, rng, pos, fr, &vis, &rec[2], lookups, &capped);
+        RGB nee = s.surfaces ? next_event_surf(s_nee, rng, pos, fr, nullptr, nullptr, v3(0, 0, 1), &rec[2], lookups, &capped)
+                             : next_event(s_nee, rng, pos, fr, &vis, &rec[2], lookups, &capped);
         if (capped) {
             end_code = ORC_END_STEP_CAP;
             break;
@@ -1051,6 +1677,173 @@ void orc_quat_to_matrix(const float* q, float* m9) {
     M3 m = quat_to_m3(q);
     float vals[9] = {m.c0.x, m.c0.y, m.c0.z, m.c1.x, m.c1.y, m.c1.z, m.c2.x, m.c2.y, m.c2.z};
     std::memcpy(m9, vals, sizeof(vals));
+}
+
+OrcSurfaces* orc_surfaces_create(const OrcSurfMaterial* mats, uint32_t nmat, const OrcSurfGeometry* geoms, uint32_t ngeom,
+                                 const OrcSurfInstance* insts, uint32_t ninst, float* box_out) {
+    if (!mats || !geoms || !insts || nmat == 0 || ngeom == 0 || ninst == 0) return nullptr;
+    auto* S = new OrcSurfaces();
+    for (uint32_t k = 0; k < nmat; ++k) {
+        const OrcSurfaces::Mat d = decode_material(mats[k]);
+        S->mats.push_back(d);
+    }
+    std::vector<float> glo(3 * static_cast<size_t>(ngeom), INFINITY), ghi(3 * static_cast<size_t>(ngeom), -INFINITY);
+    for (uint32_t g = 0; g < ngeom; ++g) {
+        const OrcSurfGeometry& G = geoms[g];
+        if (G.material >= nmat) {
+            delete S;
+            return nullptr;
+        }
+        OrcSurfaces::Geom d;
+        d.num_tris = G.num_triangles;
+        d.material = G.material;
+        for (uint32_t v = 0; v < G.num_vertices; ++v) {
+            const float* a = G.vertices + 9 * static_cast<size_t>(v);
+            for (int k = 0; k < 3; ++k) {
+                glo[3 * g + k] = std::min(glo[3 * g + k], a[k]);
+                ghi[3 * g + k] = std::max(ghi[3 * g + k], a[k]);
+                d.nrm.push_back(a[3 + k]);
+                d.tan.push_back(a[6 + k]);
+            }
+        }
+        const OrcSurfaces::Mat& mt = S->mats[G.material];
+        for (uint32_t t = 0; t < G.num_triangles; ++t) {
+            const uint32_t* ix = G.triangles + 3 * static_cast<size_t>(t);
+            d.tri.insert(d.tri.end(), ix, ix + 3);
+            // computeTriangleImportance (compute_light_probs.cu:19-50), object-space area.
+            const float* p0 = G.vertices + 9 * static_cast<size_t>(ix[0]);
+            const float* p1 = G.vertices + 9 * static_cast<size_t>(ix[1]);
+            const float* p2 = G.vertices + 9 * static_cast<size_t>(ix[2]);
+            const V3 n = cross3(v3(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]), v3(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]));
+            const float area = 0.5f * std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+            RGB est = rgb(0, 0, 0);
+            if (mt.emissive) {
+                const RGB e = rgb(mt.emit[0], mt.emit[1], mt.emit[2]);
+                est = est + e;
+                est = est + e;
+                est = est + e;
+                est = est * (1.0f / 3);
+            }
+            d.w.push_back(luminance(est) * area);
+        }
+        d.integral = excl_cdf(d.w, &d.cdf);
+        S->geoms.push_back(std::move(d));
+    }
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < ninst; ++i) {
+        const OrcSurfInstance& I = insts[i];
+        if (I.num_geometries == 0 || static_cast<uint64_t>(I.first_geometry) + I.num_geometries > ngeom) {
+            delete S;
+            return nullptr;
+        }
+        OrcSurfaces::Inst d;
+        std::memcpy(d.m, I.transform, sizeof(d.m));
+        // Normals go through the inverse transpose (common_renderer_types.h:1080-1085), the
+        // inverse taken in double.
+        const double a = I.transform[0], b = I.transform[1], c = I.transform[2], dd = I.transform[4],
+                     e = I.transform[5], f = I.transform[6], g = I.transform[8], h = I.transform[9],
+                     k = I.transform[10];
+        const double A = e * k - f * h, B = -(dd * k - f * g), Cc = dd * h - e * g;
+        const double r = 1.0 / (a * A + b * B + c * Cc);
+        const double inv[9] = {A * r, -(b * k - c * h) * r, (b * f - c * e) * r, B * r, (a * k - c * g) * r,
+                               -(a * f - c * dd) * r, Cc * r, -(a * h - b * g) * r, (a * e - b * dd) * r};
+        for (int row = 0; row < 3; ++row)
+            for (int col = 0; col < 3; ++col) d.nm[3 * row + col] = static_cast<float>(inv[3 * col + row]);
+        d.uniform_scale = I.uniform_scale;
+        d.first_geom = I.first_geometry;
+        d.num_geoms = I.num_geometries;
+        d.first_world_tri_of_geom0 = static_cast<uint32_t>(S->inst_geom_first_tri.size());
+        for (uint32_t q = 0; q < I.num_geometries; ++q) d.group_w.push_back(S->geoms[I.first_geometry + q].integral);
+        d.group_integral = excl_cdf(d.group_w, &d.group_cdf);
+        const float* M = I.transform;
+        const float col0 = std::sqrt(M[0] * M[0] + M[4] * M[4] + M[8] * M[8]);
+        S->inst_w.push_back((col0 * col0) * d.group_integral);
+        // World box: the group's object box transformed corner by corner (basic_types.h:2876-2888).
+        float gl[3] = {INFINITY, INFINITY, INFINITY}, gh[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t q = 0; q < I.num_geometries; ++q)
+            for (int ax = 0; ax < 3; ++ax) {
+                gl[ax] = std::min(gl[ax], glo[3 * (I.first_geometry + q) + ax]);
+                gh[ax] = std::max(gh[ax], ghi[3 * (I.first_geometry + q) + ax]);
+            }
+        for (int corner = 0; corner < 8; ++corner) {
+            const float pc[3] = {(corner & 1) ? gh[0] : gl[0], (corner & 2) ? gh[1] : gl[1], (corner & 4) ? gh[2] : gl[2]};
+            const V3 w = xf_point(M, pc);
+            const float wa[3] = {w.x, w.y, w.z};
+            for (int ax = 0; ax < 3; ++ax) {
+                lo[ax] = std::min(lo[ax], wa[ax]);
+                hi[ax] = std::max(hi[ax], wa[ax]);
+            }
+        }
+        for (uint32_t q = 0; q < I.num_geometries; ++q) {
+            const uint32_t gidx = I.first_geometry + q;
+            const OrcSurfGeometry& G = geoms[gidx];
+            S->inst_geom_first_tri.push_back(static_cast<uint32_t>(S->owner_inst.size()));
+            for (uint32_t t = 0; t < G.num_triangles; ++t) {
+                for (int v = 0; v < 3; ++v) {
+                    const V3 w = xf_point(M, G.vertices + 9 * static_cast<size_t>(G.triangles[3 * static_cast<size_t>(t) + v]));
+                    S->pos.push_back(w.x);
+                    S->pos.push_back(w.y);
+                    S->pos.push_back(w.z);
+                }
+                S->owner_inst.push_back(i);
+                S->owner_geom.push_back(gidx);
+                S->owner_prim.push_back(t);
+            }
+        }
+        S->insts.push_back(std::move(d));
+    }
+    S->inst_integral = excl_cdf(S->inst_w, &S->inst_cdf);
+    if (box_out)
+        for (int ax = 0; ax < 3; ++ax) {
+            box_out[ax] = lo[ax];
+            box_out[3 + ax] = hi[ax];
+        }
+    return S;
+}
+
+void orc_surfaces_destroy(OrcSurfaces* s) { delete s; }
+
+void orc_surface_closest(const OrcSurfaces* S, const float* org, const float* dir, int32_t n, float tmax, int32_t* tri,
+                         float* tb) {
+    for (int32_t i = 0; i < n; ++i) {
+        float t = 0, b1 = 0, b2 = 0;
+        tri[i] = closest_hit(*S, v3(org[3 * i], org[3 * i + 1], org[3 * i + 2]), v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]),
+                             tmax, &t, &b1, &b2);
+        tb[3 * i] = t;
+        tb[3 * i + 1] = b1;
+        tb[3 * i + 2] = b2;
+    }
+}
+
+void orc_surface_any(const OrcSurfaces* S, const float* org, const float* dir, const float* tmax, int32_t n, int32_t* hit) {
+    for (int32_t i = 0; i < n; ++i)
+        hit[i] = any_hit(*S, v3(org[3 * i], org[3 * i + 1], org[3 * i + 2]), v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]),
+                         tmax[i]) ? 1 : 0;
+}
+
+static Brdf decoded_brdf(const OrcSurfMaterial* m) { return brdf_of(decode_material(*m)); }
+
+void orc_bsdf_eval(const OrcSurfMaterial* m, const float* q, const float* v, int32_t n, float* val, float* pdf) {
+    const Brdf f = decoded_brdf(m);
+    for (int32_t i = 0; i < n; ++i) {
+        const V3 qq = v3(q[3 * i], q[3 * i + 1], q[3 * i + 2]), vv = v3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+        const RGB c = brdf_eval(f, qq, vv);
+        val[3 * i] = c.r;
+        val[3 * i + 1] = c.g;
+        val[3 * i + 2] = c.b;
+        pdf[i] = brdf_pdf(f, qq, vv);
+    }
+}
+
+void orc_bsdf_sample(const OrcSurfMaterial* m, const float* q, const float* u, int32_t n, float* out7) {
+    const Brdf f = decoded_brdf(m);
+    for (int32_t i = 0; i < n; ++i) {
+        V3 d;
+        float pdf;
+        const RGB c = brdf_sample(f, v3(q[3 * i], q[3 * i + 1], q[3 * i + 2]), u[2 * i], u[2 * i + 1], &d, &pdf);
+        const float o[7] = {d.x, d.y, d.z, c.r, c.g, c.b, pdf};
+        std::memcpy(out7 + 7 * i, o, sizeof(o));
+    }
 }
 
 int64_t orc_render_plain(const OrcScene* sc, uint64_t* rng_states, int32_t accum_base, int32_t spp,

@@ -67,7 +67,33 @@ typedef struct OrcScene {
     int32_t stream_mode;       /* 0 = per-pixel sequential streams, 1 = sample s jumped by s * 2^40 */
     int32_t maj_shift;         /* majorant cells of 2^maj_shift voxels (cell_majorant has cx*cy*cz) */
     float shadow_rr;           /* Russian-roulette threshold of shadow-ray visibility, 0 = off */
+    /* Triangle meshes (orc_surfaces_create), NULL = volume-only scene; plain passes only. */
+    const struct OrcSurfaces* surfaces;
+    int32_t volume_disabled;   /* 1: no density grid (surfaces only) */
 } OrcScene;
+
+/* Surface scene inputs, laid out like the product's VptSurface* structs: materials with the
+ * immediate texture values, geometry instances with object-space vertices (position, normal,
+ * tangent) and triangles, instances with a row-major 3x4 transform over a geometry range. */
+typedef struct OrcSurfMaterial {
+    int32_t kind;              /* 0 = SimplePBR, 1 = Lambert */
+    float base_color[3];
+    float roughness, metallic;
+    float emittance[3];
+} OrcSurfMaterial;
+typedef struct OrcSurfGeometry {
+    const float* vertices;
+    uint32_t num_vertices;
+    const uint32_t* triangles;
+    uint32_t num_triangles;
+    uint32_t material;
+} OrcSurfGeometry;
+typedef struct OrcSurfInstance {
+    uint32_t first_geometry, num_geometries;
+    float transform[12];
+    float uniform_scale;
+} OrcSurfInstance;
+typedef struct OrcSurfaces OrcSurfaces;
 
 /* Per-sample decision record: vertices, primary lookups, shadow lookups, end code. */
 enum {
@@ -132,6 +158,21 @@ void orc_env_sample(const OrcScene* sc, const float* u, int32_t n, float* dir, f
                     float* rgb);
 void orc_env_evaluate(const OrcScene* sc, const float* dir, int32_t n, float* pdf, float* rgb);
 void orc_imp_sample(const OrcScene* sc, const float* u, int32_t n, float* out5);
+/* Prepared surfaces (world triangles, light distributions) from the raw inputs; box_out gets
+ * the union of the instances' transformed boxes (min, max). NULL for invalid input. */
+OrcSurfaces* orc_surfaces_create(const OrcSurfMaterial* materials, uint32_t num_materials,
+                                 const OrcSurfGeometry* geometries, uint32_t num_geometries,
+                                 const OrcSurfInstance* instances, uint32_t num_instances, float* box_out);
+void orc_surfaces_destroy(OrcSurfaces* s);
+/* Closest hits (tri index or -1, t, b1, b2 per ray) and any-hit tests of n rays. */
+void orc_surface_closest(const OrcSurfaces* s, const float* org, const float* dir, int32_t n, float tmax,
+                         int32_t* tri, float* tb);
+void orc_surface_any(const OrcSurfaces* s, const float* org, const float* dir, const float* tmax, int32_t n,
+                     int32_t* hit);
+/* BSDF of a material (kind, decoded parameters) evaluated for n (query, sampled) direction
+ * pairs in the shading frame: value (3), pdf (1); and sampled: direction (3), value (3), pdf. */
+void orc_bsdf_eval(const OrcSurfMaterial* m, const float* q, const float* v, int32_t n, float* val, float* pdf);
+void orc_bsdf_sample(const OrcSurfMaterial* m, const float* q, const float* u, int32_t n, float* out7);
 void orc_phase_sample(int32_t kind, float param, const float* u, int32_t n, float* dir_local,
                       float* pdf);
 void orc_phase_eval(int32_t kind, float param, const float* dir_local, int32_t n, float* pdf);

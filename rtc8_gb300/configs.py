@@ -70,6 +70,10 @@ class SceneConfig:
     cam_distance_diagonals: float = 2.5
     cam_direction: tuple = (0.55, 0.3, 1.0)   # from the grid centre towards the camera
     rng_seed: int = REFERENCE_RNG_SEED
+    # Triangle meshes around the volume: the name of a procedural scene of
+    # rtc8_gb300.surfaces ("room"), or None; volume_enabled = False renders the surfaces alone.
+    surfaces: str | None = None
+    volume_enabled: bool = True
 
     def replace(self, **kw) -> "SceneConfig":
         return dataclasses.replace(self, **kw)
@@ -108,7 +112,17 @@ C5 = SceneConfig(name="c5_sparse1024_2048px", width=2048, height=2048, spp=16,
                  sky=SkySpec(turbidity=3.0, ground_albedo=0.3), max_bounces=1024, rr_start_vertex=9,
                  majorant_cell_log2=6)
 
-CONFIGS = {c.name: c for c in (C1, C1_REFERENCE_MODE, C2, C5)}
+# Mixed surface + volume workload (the reference's scenes put clouds among meshes): the dense
+# 64^3 cloud of C1 inside an open room with coloured Lambert walls, a glossy and a metallic
+# SimplePBR block and a rectangle light under the ceiling, 512^2, seen from the open side.
+C_ROOM = C1.replace(name="room_cloud64_512px", width=512, height=512, surfaces="room", cam_direction=(0.0, 0.12, 1.0),
+                    cam_distance_diagonals=1.55, fov_deg=48.0)
+# The same with the reference's own path rules.
+C_ROOM_REFERENCE_MODE = C_ROOM.replace(name="room_reference_mode", phase_kind=0, phase_param=0.0,
+                                       sun_elevation_deg=None, max_bounces=0, rr_start_vertex=1, majorant_mode=0,
+                                       rng_stream_mode=0, shadow_rr_threshold=0.0)
+
+CONFIGS = {c.name: c for c in (C1, C1_REFERENCE_MODE, C2, C5, C_ROOM, C_ROOM_REFERENCE_MODE)}
 
 
 # ------------------------------------------------------------------------------ geometry

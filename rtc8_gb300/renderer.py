@@ -141,6 +141,51 @@ class Renderer:
         self.set_environment_rgb(rgb)
         return rgb
 
+    def set_surfaces(self, scene) -> None:
+        """Uploads a rtc8_gb300.surfaces.SurfaceScene (None removes the surfaces): the BVH and
+        the emitters' light distributions are built on the host by vpt_set_surfaces."""
+        from . import _lib as L
+
+        if scene is None or not scene.instances:
+            check(self.lib.vpt_set_surfaces(self.ctx, None, 0, None, 0, None, 0), "vpt_set_surfaces")
+            return
+        mats = (L.VptSurfaceMaterial * len(scene.materials))()
+        for m, src in zip(mats, scene.materials):
+            m.kind = src.kind
+            m.base_color[:] = [float(x) for x in src.base_color]
+            m.roughness, m.metallic = float(src.roughness), float(src.metallic)
+            m.emittance[:] = [float(x) for x in src.emittance]
+        keep = []
+        geoms = (L.VptSurfaceGeometry * len(scene.meshes))()
+        for g, mesh in zip(geoms, scene.meshes):
+            v = np.ascontiguousarray(mesh.vertices, dtype=np.float32)
+            t = np.ascontiguousarray(mesh.triangles, dtype=np.uint32)
+            if v.ndim != 2 or v.shape[1] != 9 or t.ndim != 2 or t.shape[1] != 3:
+                raise ValueError("set_surfaces: vertices must be (n, 9) and triangles (m, 3)")
+            keep += [v, t]
+            g.vertices = ptr(v, C.c_float)
+            g.num_vertices = len(v)
+            g.triangles = ptr(t, C.c_uint32)
+            g.num_triangles = len(t)
+            g.material = mesh.material
+        insts = (L.VptSurfaceInstance * len(scene.instances))()
+        for d, src in zip(insts, scene.instances):
+            d.first_geometry, d.num_geometries = src.first_geometry, src.num_geometries
+            d.transform[:] = [float(x) for x in np.asarray(src.transform, dtype=np.float32).reshape(12)]
+            d.uniform_scale = float(src.uniform_scale)
+        check(self.lib.vpt_set_surfaces(self.ctx, mats, len(mats), geoms, len(geoms), insts, len(insts)),
+              "vpt_set_surfaces")
+
+    def surface_info(self) -> dict:
+        tri, nodes, em = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        box = (C.c_float * 6)()
+        check(self.lib.vpt_get_surface_info(self.ctx, C.byref(tri), C.byref(nodes), C.byref(em), box),
+              "vpt_get_surface_info")
+        return {"triangles": tri.value, "bvh_nodes": nodes.value, "emitters": em.value, "world_box": list(box)}
+
+    def clear_volume(self) -> None:
+        check(self.lib.vpt_clear_volume(self.ctx), "vpt_clear_volume")
+
     def set_environment_rgb(self, rgb: np.ndarray) -> None:
         img = np.ascontiguousarray(rgb, dtype=np.float32)
         h, w, _ = img.shape
@@ -384,5 +429,12 @@ def setup_scene(r: Renderer, cfg: SceneConfig, volume: np.ndarray | None = None)
                        cfg.sky.include_solar_disc)
     elif cfg.env_constant is not None:
         r.set_environment_rgb(constant_environment(cfg.env_constant))
+    if cfg.surfaces is not None:
+        from . import surfaces as _surf
+        if cfg.surfaces != "room":
+            raise ValueError(f"unknown surface scene {cfg.surfaces!r}")
+        r.set_surfaces(_surf.room_scene())
+    if not cfg.volume_enabled:
+        r.clear_volume()
     r.set_frame(frame_params(cfg))
     r.seed_rng(cfg.rng_seed)
