@@ -112,8 +112,8 @@ class ClockSampler:
 
 
 def _cfg(name):
-    from rtc8_gb300.configs import C1, C2, C5
-    return {"c1": C1, "c2": C2, "c5": C5}[name]
+    from rtc8_gb300.configs import C1, C2, C5, C_ROOM
+    return {"c1": C1, "c2": C2, "c5": C5, "room": C_ROOM}[name]
 
 
 def _mlp_tensor_pipe():
@@ -389,6 +389,41 @@ def stress_plain(steps: int = 3, warmup: int = 2) -> dict:
     return out
 
 
+def surface_plain(steps: int = 3, warmup: int = 2, cfg_name: str = "room_cloud64_512px") -> dict:
+    """The surface tracer on the mixed scene (the 64^3 cloud inside an open room of Lambert walls,
+    two SimplePBR blocks and a rectangle light, 512^2), STEP_SPP per launch, device-timed; with the
+    room's BVH and emitter counts and the work counters (lookups per path)."""
+    import torch
+
+    from rtc8_gb300.configs import CONFIGS
+    from rtc8_gb300.renderer import Renderer, setup_scene
+
+    cfg = CONFIGS[cfg_name]
+    r = Renderer(cfg.width, cfg.height)
+    setup_scene(r, cfg)
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        r.launch_plain(STEP_SPP, s.cuda_stream)
+    torch.cuda.synchronize()
+    r.reset_counters()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(steps):
+        r.launch_plain(STEP_SPP, s.cuda_stream)
+    b.record(s)
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    c = r.counters()
+    out = {"workload": f"{cfg.name}: {cfg.width}x{cfg.height}, {STEP_SPP} spp per launch, fBm {cfg.volume.n}^3 "
+                       f"cloud in a room of {r.surface_info()['triangles']} triangles (Lambert walls, SimplePBR "
+                       "blocks, rectangle light), sun + constant environment through the open side",
+           "ms_per_launch": ms, "paths_per_s": cfg.width * cfg.height * STEP_SPP / (ms / 1e3), "launches": steps,
+           "surfaces": r.surface_info(), "vertices_per_path": c["vertices"] / max(c["samples"], 1),
+           "lookups_per_path": c["lookups"] / max(c["samples"], 1), "device_errors": r.device_errors()}
+    r.close()
+    return out
+
+
 def batch_bench(steps: int, warmup: int, spp: int = 4) -> dict:
     """The batched workload: 16 seeded scenes of uneven resolution and grid size, one batch
     step = `spp` samples per pixel of every scene as one CUDA-graph launch, launch shapes picked by
@@ -464,7 +499,7 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4", "c5", "room"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--image", type=int, default=0, help="override the image side (profiling runs)")
     ap.add_argument("--no-flush", action="store_true", help="skip the L2 flush between steps (profiling runs)")
@@ -643,6 +678,7 @@ def main():
     if rank == 0 and not args.no_extras and args.config == "c2":
         extras = {}
         for key, fn in (("stress_2048px_1024cube_plain", lambda: stress_plain()),
+                        ("room_512px_surfaces_cloud64", lambda: surface_plain()),
                         ("batched_16_scenes", lambda: batch_bench(3, 2))):
             try:
                 extras[key] = fn()

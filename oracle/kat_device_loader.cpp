@@ -473,6 +473,43 @@ void run_nrc() {
 
 }  // namespace
 
+// Surface BSDFs: bsdf.params holds 6 floats per material (kind, linear base colour, smoothness,
+// metallic); every material gets the same query directions, variates and second directions.
+void run_bsdf() {
+    auto params = read_vec<float>("bsdf.params");
+    auto q = read_vec<float>("bsdf.q");
+    auto u = read_vec<float>("bsdf.u");
+    auto v = read_vec<float>("bsdf.v");
+    uint32_t n = static_cast<uint32_t>(q.size() / 3);
+    if (u.size() != 2 * static_cast<size_t>(n) || v.size() != 3 * static_cast<size_t>(n) || params.size() % 6)
+        die("bsdf inputs have inconsistent sizes");
+    Dev dq(4 * q.size()), du(4 * u.size()), dv(4 * v.size()), dout(4 * 11 * static_cast<size_t>(n));
+    dq.put(q);
+    du.put(u);
+    dv.put(v);
+    std::vector<float> all;
+    for (size_t m = 0; m < params.size() / 6; ++m) {
+        int32_t kind = static_cast<int32_t>(params[6 * m]);
+        float br = params[6 * m + 1], bg = params[6 * m + 2], bb = params[6 * m + 3];
+        float sm = params[6 * m + 4], me = params[6 * m + 5];
+        void *a = dq.p, *b = du.p, *c = dv.p, *o = dout.p;
+        launch("kat_bsdf", blocks(n, 64), 1, 64, {&kind, &br, &bg, &bb, &sm, &me, &a, &b, &c, &n, &o});
+        auto r = dout.get<float>(11 * static_cast<size_t>(n));
+        all.insert(all.end(), r.begin(), r.end());
+    }
+    write_vec("bsdf.out", all);
+}
+
+void run_offset() {
+    auto pn = read_vec<float>("offset.pn");
+    uint32_t n = static_cast<uint32_t>(pn.size() / 6);
+    Dev dp(4 * pn.size()), dout(4 * 3 * static_cast<size_t>(n));
+    dp.put(pn);
+    void *a = dp.p, *o = dout.p;
+    launch("kat_offset", blocks(n, 64), 1, 64, {&a, &n, &o});
+    write_vec("offset.out", dout.get<float>(3 * static_cast<size_t>(n)));
+}
+
 int main(int argc, char** argv) {
     if (argc != 3) die("usage: kat_device_loader <ptx> <dir>");
     g_dir = argv[2];
@@ -486,6 +523,8 @@ int main(int argc, char** argv) {
     run_schlick();
     run_env();
     run_nrc();
+    run_bsdf();
+    run_offset();
     std::printf("ok\n");
     return 0;
 }

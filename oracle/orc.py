@@ -77,6 +77,7 @@ _FUNCS = {
     "orc_surface_any": (None, [C.c_void_p, f32p, f32p, f32p, C.c_int32, i32p]),
     "orc_bsdf_eval": (None, [C.POINTER(OrcSurfMaterial), f32p, f32p, C.c_int32, f32p, f32p]),
     "orc_bsdf_sample": (None, [C.POINTER(OrcSurfMaterial), f32p, f32p, C.c_int32, f32p]),
+    "orc_offset_origin": (None, [f32p, C.c_int32, f32p]),
     "orc_phase_sample": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p, f32p]),
     "orc_phase_eval": (None, [C.c_int32, C.c_float, f32p, C.c_int32, f32p]),
     "orc_polar_yup": (None, [f32p, C.c_int32, f32p]),
@@ -376,6 +377,13 @@ def bsdf_sample(material, q: np.ndarray, u: np.ndarray) -> np.ndarray:
     u = np.ascontiguousarray(u, dtype=np.float32)
     out = np.zeros((len(q), 7), dtype=np.float32)
     lib().orc_bsdf_sample(C.byref(_material(material)), p(q, C.c_float), p(u, C.c_float), len(q), p(out, C.c_float))
+    return out
+
+
+def offset_origin(pn: np.ndarray) -> np.ndarray:
+    pn = np.ascontiguousarray(pn, dtype=np.float32)
+    out = np.zeros((len(pn), 3), dtype=np.float32)
+    lib().orc_offset_origin(p(pn, C.c_float), len(pn), p(out, C.c_float))
     return out
 
 

@@ -238,3 +238,55 @@ extern "C" __global__ void kat_read_minmax(const RGBSpectrumAsOrderedInt* mn, co
     out[4] = b.g;
     out[5] = b.b;
 }
+
+// ------------------------------------------------------------------------------ surface BSDFs
+// The reference's LambertBRDF and SimplePBR_BRDF (a DichromaticBRDF) built from decoded material
+// values; per input: sampleF's direction (3), value (3) and density, then evaluateF (3) and
+// evaluatePDF at the second direction v (11 floats).
+extern "C" __global__ void kat_bsdf(int32_t kind, float br, float bg, float bb, float smoothness, float metallic,
+                                    const float* q, const float* u, const float* v, uint32_t n, float* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vector3D ql(q[3 * i], q[3 * i + 1], q[3 * i + 2]);
+    const Vector3D vl(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    const BSDFQuery query(ql, Normal3D(0, 0, 1));
+    const BSDFSample smp(u[2 * i], u[2 * i + 1]);
+    BSDFQueryResult res;
+    RGBSpectrum f, fe;
+    float pe;
+    if (kind == 1) {
+        const LambertBRDF b(RGBSpectrum(br, bg, bb));
+        f = b.sampleF(query, smp, &res);
+        fe = b.evaluateF(query, vl);
+        pe = b.evaluatePDF(query, vl);
+    } else {
+        SimplePBR_BRDF b(RGBSpectrum(br, bg, bb), 0.5f, smoothness, metallic);
+        f = b.sampleF(query, smp, &res);
+        fe = b.evaluateF(query, vl);
+        pe = b.evaluatePDF(query, vl);
+    }
+    float* o = out + 11 * i;
+    o[0] = res.dirLocal.x;
+    o[1] = res.dirLocal.y;
+    o[2] = res.dirLocal.z;
+    o[3] = f.r;
+    o[4] = f.g;
+    o[5] = f.b;
+    o[6] = res.dirPDensity;
+    o[7] = fe.r;
+    o[8] = fe.g;
+    o[9] = fe.b;
+    o[10] = pe;
+}
+
+// offsetRayOrigin (common_renderer_types.h:1326-1349) for n (point, normal) pairs.
+extern "C" __global__ void kat_offset(const float* pn, uint32_t n, float* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Point3D p(pn[6 * i], pn[6 * i + 1], pn[6 * i + 2]);
+    const Normal3D nn(pn[6 * i + 3], pn[6 * i + 4], pn[6 * i + 5]);
+    const Point3D r = offsetRayOrigin(p, nn);
+    out[3 * i] = r.x;
+    out[3 * i + 1] = r.y;
+    out[3 * i + 2] = r.z;
+}

@@ -1821,6 +1821,15 @@ void orc_surface_any(const OrcSurfaces* S, const float* org, const float* dir, c
                          tmax[i]) ? 1 : 0;
 }
 
+void orc_offset_origin(const float* pn, int32_t n, float* out) {
+    for (int32_t i = 0; i < n; ++i) {
+        const V3 r = offset_origin(v3(pn[6 * i], pn[6 * i + 1], pn[6 * i + 2]), v3(pn[6 * i + 3], pn[6 * i + 4], pn[6 * i + 5]));
+        out[3 * i] = r.x;
+        out[3 * i + 1] = r.y;
+        out[3 * i + 2] = r.z;
+    }
+}
+
 static Brdf decoded_brdf(const OrcSurfMaterial* m) { return brdf_of(decode_material(*m)); }
 
 void orc_bsdf_eval(const OrcSurfMaterial* m, const float* q, const float* v, int32_t n, float* val, float* pdf) {

@@ -173,6 +173,8 @@ void orc_surface_any(const OrcSurfaces* s, const float* org, const float* dir, c
  * pairs in the shading frame: value (3), pdf (1); and sampled: direction (3), value (3), pdf. */
 void orc_bsdf_eval(const OrcSurfMaterial* m, const float* q, const float* v, int32_t n, float* val, float* pdf);
 void orc_bsdf_sample(const OrcSurfMaterial* m, const float* q, const float* u, int32_t n, float* out7);
+/* offsetRayOrigin of n (point, normal) pairs (6 floats each). */
+void orc_offset_origin(const float* pn, int32_t n, float* out);
 void orc_phase_sample(int32_t kind, float param, const float* u, int32_t n, float* dir_local,
                       float* pdf);
 void orc_phase_eval(int32_t kind, float param, const float* dir_local, int32_t n, float* pdf);

@@ -116,7 +116,7 @@ C5 = SceneConfig(name="c5_sparse1024_2048px", width=2048, height=2048, spp=16,
 # 64^3 cloud of C1 inside an open room with coloured Lambert walls, a glossy and a metallic
 # SimplePBR block and a rectangle light under the ceiling, 512^2, seen from the open side.
 C_ROOM = C1.replace(name="room_cloud64_512px", width=512, height=512, surfaces="room", cam_direction=(0.0, 0.12, 1.0),
-                    cam_distance_diagonals=1.55, fov_deg=48.0)
+                    cam_distance_diagonals=1.55, fov_deg=48.0, sun_azimuth_deg=20.0)
 # The same with the reference's own path rules.
 C_ROOM_REFERENCE_MODE = C_ROOM.replace(name="room_reference_mode", phase_kind=0, phase_param=0.0,
                                        sun_elevation_deg=None, max_bounces=0, rr_start_vertex=1, majorant_mode=0,

@@ -2,7 +2,8 @@
 
 oracle/build_ref.sh (in a checkout with the reference next to it) compiles oracle/ref_kat_device.cu
 — known-answer kernels around the reference's PCG32RNG, SchlickPhaseFunction,
-HierarchicalImportanceMap and ImageBasedEnvironmentalLight, plus the reference's own
+HierarchicalImportanceMap, ImageBasedEnvironmentalLight, LambertBRDF, SimplePBR_BRDF and
+offsetRayOrigin, plus the reference's own
 importance-map kernels (renderer/gpu_kernels/compute_light_probs.cu) and radiance-cache set-up
 kernels (renderer/gpu_kernels/nrc_set_up_kernels.cu) — to oracle/_ref/ref_kat_device.ptx. On a
 GPU host this script builds oracle/kat_device_loader.cpp, feeds it seeded inputs and writes the
@@ -123,7 +124,51 @@ def make_inputs(rng) -> dict:
     d["acc.inferred"] = (rng.standard_normal((npix, 3)) * 2).astype(np.float32)
     d["acc.query"] = queries(rng, npix)
     d["acc.prev"] = rng.random((npix, 3)).astype(np.float32)
+    # Surface BSDFs (drawn after everything above, so the earlier inputs keep their values): the
+    # materials' decoded values (8-bit sRGB base colour, 8-bit roughness / metallic), query
+    # directions over both hemispheres including grazing ones, variates, second directions.
+    raw = surface_materials()
+    d["bsdf.raw"] = raw
+    d["bsdf.params"] = decoded_bsdf_params(raw)
+    nb = 512
+    qd = rng.standard_normal((nb, 3))
+    qd[:8, 2] = np.abs(qd[:8, 2]) * 1e-3
+    d["bsdf.q"] = (qd / np.linalg.norm(qd, axis=1, keepdims=True)).astype(np.float32)
+    ub = rng.random((nb, 2)).astype(np.float32)
+    ub[:3] = [[0.0, 0.0], [0.5, 0.5], [0.999999, 0.999999]]
+    d["bsdf.u"] = ub
+    vd = rng.standard_normal((nb, 3))
+    d["bsdf.v"] = (vd / np.linalg.norm(vd, axis=1, keepdims=True)).astype(np.float32)
+    # offsetRayOrigin: points near and far from the origin, unit normals.
+    npts = 256
+    pts = (rng.standard_normal((npts, 3)) * np.where(rng.random((npts, 1)) < 0.3, 0.01, 10.0)).astype(np.float32)
+    nrm = rng.standard_normal((npts, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d["offset.pn"] = np.concatenate([pts, nrm.astype(np.float32)], axis=1)
     return d
+
+
+def surface_materials() -> np.ndarray:
+    """Raw materials (kind, base colour, roughness, metallic; the immediate values a scene gives):
+    SimplePBR dielectrics from rough to smooth, metals, and Lambert."""
+    return np.array([[0, 0.8, 0.8, 0.8, 0.5, 0.0], [0, 0.55, 0.6, 0.8, 0.3, 0.0], [0, 0.95, 0.75, 0.45, 0.2, 1.0],
+                     [0, 0.2, 0.9, 0.3, 0.02, 0.0], [0, 0.9, 0.9, 0.9, 1.0, 0.5], [1, 0.75, 0.15, 0.12, 0.0, 0.0]],
+                    np.float32)
+
+
+def decoded_bsdf_params(raw: np.ndarray) -> np.ndarray:
+    """The values the reference's 1x1 textures return: 8-bit truncation, sRGB decode of the colour
+    (renderer_scene.cpp:860-900, 1202-1255), smoothness = min(1 - roughness, 0.999) (:1978)."""
+    def unorm8(v):
+        return np.minimum(np.floor(np.float32(255.0) * np.float32(v)), 255.0)
+
+    out = []
+    for kind, r, g, b, rough, metal in raw:
+        c = unorm8(np.array([r, g, b])) / 255.0
+        lin = np.where(c <= 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4).astype(np.float32)
+        smooth = np.float32(min(np.float32(1.0) - np.float32(unorm8(rough) / 255.0), np.float32(0.999)))
+        out.append([kind, *lin, smooth, np.float32(unorm8(metal) / 255.0)])
+    return np.array(out, np.float32)
 
 
 OUTPUTS = {
@@ -131,7 +176,8 @@ OUTPUTS = {
     "env.out": np.float32, "env.integral": np.float32, "env.mips": np.float32,
     "prep.out": np.uint32, "prep.minmax": np.float32, "prep.avg": np.float32, "prep.term": np.uint32,
     "prop.target_out": np.float32, "shuf.query1": np.float32, "shuf.target1": np.float32,
-    "shuf.minmax": np.float32, "shuf.avg": np.float32, "acc.out": np.float32,
+    "shuf.minmax": np.float32, "shuf.avg": np.float32, "acc.out": np.float32, "bsdf.out": np.float32,
+    "offset.out": np.float32,
 }
 
 
