@@ -197,7 +197,7 @@ struct SurfHit {
 // Closest hit in [tmin, tmax]; ties in t go to the lower world-triangle index (the oracle's
 // brute-force search applies the same rule). Sets *overflow if the traversal stack overflowed
 // (the builder bounds the depth below the stack size, so trees it built never do).
-__device__ __forceinline__ SurfHit bvh_closest(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
+static __device__ __noinline__ SurfHit bvh_closest(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
     SurfHit h{~0u, tmax, 0.0f, 0.0f};
     const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     uint32_t stack[kBvhStack];
@@ -255,7 +255,7 @@ __device__ __forceinline__ SurfHit bvh_closest(const Surfaces& S, V3 o, V3 d, fl
 }
 
 // Any hit in [tmin, tmax] (the visibility ray's any-hit program, optix_pathtracing_kernels.cu:7-10).
-__device__ __forceinline__ bool bvh_any(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
+static __device__ __noinline__ bool bvh_any(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
     const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     uint32_t stack[kBvhStack];
     int sp = 0;
@@ -296,7 +296,7 @@ struct SurfPoint {
 
 // computeSurfacePoint (renderer_kernel_common.h:72-124) for world triangle `tri` at (b1, b2).
 // `env_enabled`: the environment takes probToSampleEnvLight of the light selection.
-__device__ __forceinline__ SurfPoint surface_point(const Surfaces& S, uint32_t tri, float b1, float b2,
+static __device__ __noinline__ SurfPoint surface_point(const Surfaces& S, uint32_t tri, float b1, float b2,
                                                    bool env_enabled) {
     const float4 q0 = S.tri_pos[3 * tri];
     const V3 p0 = ld3(q0), p1 = ld3(S.tri_pos[3 * tri + 1]), p2 = ld3(S.tri_pos[3 * tri + 2]);
@@ -462,7 +462,7 @@ __device__ __forceinline__ RGB dichromatic_value(const Bsdf& f, float ag, V3 L, 
 
 // BSDF::sampleF (Lambert :1497-1505, dichromatic :1680-1790). `q` = the query direction (vOut)
 // in the shading frame. Returns the value; *pdf = 0 marks a failed sample.
-__device__ __forceinline__ RGB bsdf_sample(const Bsdf& f, V3 q, float u0, float u1, V3* out, float* pdf) {
+static __device__ __noinline__ RGB bsdf_sample(const Bsdf& f, V3 q, float u0, float u1, V3* out, float* pdf) {
     if (f.kind == kMatLambert) {
         V3 d = cosine_sample_hemisphere(u0, u1);
         *pdf = d.z / kPi;
@@ -527,6 +527,10 @@ __device__ __forceinline__ RGB bsdf_eval(const Bsdf& f, V3 q, V3 s) {
     return dichromatic_value(f, ag, L, V, m, dot_lh, ggx_d(ag, m));
 }
 
+// evaluateF and evaluatePDF of one direction together (NEE needs both), out of line.
+__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 q, V3 s);
+static __device__ __noinline__ RGB bsdf_eval_pdf(const Bsdf& f, V3 q, V3 s, float* pdf);
+
 // BSDF::evaluatePDF (Lambert :1512-1517, dichromatic :1830-1875).
 __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 q, V3 s) {
     if (f.kind == kMatLambert) return (q.z * s.z > 0) ? fabsf(s.z) / kPi : 0.0f;
@@ -556,7 +560,7 @@ struct AreaSample {
 // sampleLight<false> for the area lights (renderer_kernel_common.h:146-290): instance, geometry
 // of its group, triangle (each a CDF search that remaps the variate for the next level), then a
 // uniform point by the low-distortion triangle map.
-__device__ __forceinline__ AreaSample sample_area_light(const Surfaces& S, float ul, float u0, float u1) {
+static __device__ __noinline__ AreaSample sample_area_light(const Surfaces& S, float ul, float u0, float u1) {
     AreaSample a;
     a.area_pdf = 0.0f;
     a.emittance = rgb(0, 0, 0);
@@ -599,6 +603,11 @@ __device__ __forceinline__ AreaSample sample_area_light(const Surfaces& S, float
     const SurfMaterial& mt = S.mats[ge.material];
     if (mt.emissive) a.emittance = rgb(mt.emittance[0], mt.emittance[1], mt.emittance[2]);
     return a;
+}
+
+static __device__ __noinline__ RGB bsdf_eval_pdf(const Bsdf& f, V3 q, V3 s, float* pdf) {
+    *pdf = bsdf_pdf(f, q, s);
+    return bsdf_eval(f, q, s);
 }
 
 }  // namespace vpt

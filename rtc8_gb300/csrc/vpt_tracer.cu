@@ -28,6 +28,7 @@ enum : uint32_t {
     ST_END_SAMPLE,   // accumulate, next sample or next item
     ST_DONE,
     ST_SURFACE,      // surface scenes: the primary segment ended on a triangle
+    ST_NEE_SETUP,    // surface scenes: light sample and shadow ray of the current vertex
 };
 
 enum : uint32_t {
@@ -65,8 +66,11 @@ constexpr int kNrcParkThreshold = 24;
 constexpr int kPlainCtasPerSm = 7;
 constexpr int kPlainPerPixelCtasPerSm = 5;
 constexpr int kNrcCtasPerSm = 7;
-// The surface tracer carries the hit, the light sample's geometry and a BVH stack per lane.
-constexpr int kSurfCtasPerSm = 4;
+// The surface tracer carries the hit, the light sample's geometry and a BVH stack per lane; it
+// is latency-bound (every vertex traverses the BVH twice with divergent loops), and occupancy wins
+// over register spills: room scene 512^2 x 16 spp, 4 / 6 / 8 / 10 / 12 / 16 CTAs per SM ->
+// 176 / 151 / 137 / 132 / 128 / 121 ms per launch.
+constexpr int kSurfCtasPerSm = 16;
 
 struct DdaState {
     int cell[3];
@@ -751,7 +755,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                 throughput = rdiv(throughput, continue_prob);
                 if constexpr (kSurfaces) {
                     at_surface = false;
-                    surf_nee_setup();
+                    st = ST_NEE_SETUP;
                     break;
                 }
 
@@ -852,10 +856,16 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                     }
                     throughput = rdiv(throughput, continue_prob);
                     at_surface = true;
-                    surf_nee_setup();
+                    st = ST_NEE_SETUP;
                 } else {
                     st = ST_ESCAPE;
                 }
+                break;
+            }
+            case ST_NEE_SETUP: {
+                // One call site for medium and surface vertices keeps the kernel's code small
+                // (the surface passes are bound by instruction fetch otherwise).
+                if constexpr (kSurfaces) surf_nee_setup();
                 break;
             }
             case ST_NEE_DONE: {
@@ -870,13 +880,14 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         if (vis > 0.0f) {
                             const V3 sdir = -light_dir;
                             const V3 vin = to_local(sp.sf, -sdir);
-                            const RGB fs = bsdf_eval(f, q, vin);
+                            float bpdf0;
+                            const RGB fs = bsdf_eval_pdf(f, q, vin, &bpdf0);
                             const float sp_cos = fabsf(dot(sdir, sp.gn));
                             RGB nee;
                             if (pick_sun) {
                                 nee = fs * emittance * (vis * sp_cos / area_pdf);
                             } else {
-                                float bpdf = bsdf_pdf(f, q, vin) * nee_lp_cos / nee_dist2;
+                                float bpdf = bpdf0 * nee_lp_cos / nee_dist2;
                                 if (!isfinite(bpdf)) bpdf = 0.0f;
                                 const float light_pdf = area_pdf;
                                 const float mis = (light_pdf * light_pdf) / ((bpdf * bpdf) + (light_pdf * light_pdf));

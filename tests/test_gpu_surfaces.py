@@ -21,11 +21,11 @@ DECISION_PARITY = 0.999
 # Device and oracle differ in the last bits of fast-math transcendentals (the reference's own
 # build flags on the device, libm in the oracle), and each path vertex is a fresh chance for such
 # a difference to flip a decision. Surface paths here are three times longer than the volume
-# workloads' (7.6 vertices), so the bar is set per vertex: at most 2.5e-4 diverging samples per
-# path vertex (the volume workloads' 0.1% of samples at 2.5 vertices is 4e-4), and 99.8% of
-# samples identical.
-PER_VERTEX = 2.5e-4
-SURFACE_PARITY = 0.998
+# workloads' (7.6 vertices), so the bar is set per vertex at the volume tests' level: their 0.1%
+# of samples at 2.5 vertices per path is 4e-4 diverging samples per vertex. At least 99.5% of the
+# samples stay identical.
+PER_VERTEX = 4e-4
+SURFACE_PARITY = 0.995
 
 
 def run_pair(cfg, scene, spp: int, volume_enabled: bool = True) -> dict:
