@@ -31,6 +31,21 @@ __host__ __device__ __forceinline__ uint32_t pack_suffix(uint32_t prev, uint32_t
     return (prev & kInvalidVertex) | ((has_query & 1u) << 22) | ((path_length & 0xFFu) << 23) | ((unbiased & 1u) << 31);
 }
 
+// The arrays one training pass writes: several passes traced in one launch (the frame's
+// training iterations, vpt_nrc_frame) each get their own set; the shuffled batch, the shufflers
+// and the statistics are shared because the sets are post-processed one after the other.
+constexpr uint32_t kMaxTrainSets = 4;
+struct TrainSet {
+    uint32_t* counters;          // as NrcBuffers::counters
+    uint64_t* rng;               // per-pixel PCG32 states of the set's training paths
+    TrainVertexInfo* vertex;     // kTrainBufferSize
+    float* query0;               // kTrainBufferSize * 14 (train_query[0])
+    float* target0;              // kTrainBufferSize * 3 (train_target[0])
+    float* end_query;            // max_train_suffixes * 14
+    float* end_inferred;         // max_train_suffixes * 3
+    uint32_t* suffix;            // max_train_suffixes
+};
+
 // Device pointers and sizes used by the NRC kernels.
 struct NrcBuffers {
     int32_t width = 0, height = 0;   // render image
@@ -65,6 +80,12 @@ struct NrcBuffers {
     uint32_t* counters = nullptr;
     float* stats = nullptr;          // per buffer: min rgb, max rgb, avg rgb (9 floats)
     uint32_t buffer_index = 0;       // nrcBufferIndex of the current training iteration
+    // Training sets of a multi-pass launch: set 0 is the arrays above, sets 1.. are allocated on
+    // first use; `train_sets` is the device table of all of them.
+    TrainSet sets[kMaxTrainSets] = {};
+    uint32_t num_sets = 0;           // sets allocated (0 until the first multi-pass frame)
+    TrainSet* train_sets = nullptr;  // device copy of sets[0 .. num_sets)
+    uint32_t set_buf[kMaxTrainSets] = {1, 1, 1, 1};  // nrcBufferIndex of each set's last pass
 };
 
 // Set-up kernels between the passes (nrc_setup.cu).

@@ -125,12 +125,73 @@ int ensure_render_slots(VptContext* c, uint32_t spp) {
     return VPT_OK;
 }
 
+// Jump of the training states of set k: 2^62 draws past the context's per-pixel states (clear
+// of the render samples' streams, sample s starting s * 2^40 draws in) plus k * 2^58.
+void set_jump(uint32_t k, uint64_t* mult, uint64_t* plus) {
+    vpt::lcg_jump((1ull << 62) + static_cast<uint64_t>(k) * (1ull << 58), mult, plus);
+}
+
+// Training sets 0 .. n-1 of the multi-pass frame (set 0 = the cache's own training arrays) and
+// their device table.
+int ensure_train_sets(VptContext* c, uint32_t n) {
+    vpt::NrcBuffers& b = *c->nrc;
+    if (n <= b.num_sets) return VPT_OK;
+    const size_t npix = static_cast<size_t>(c->width) * c->height;
+    b.sets[0] = vpt::TrainSet{b.counters, b.train_rng, b.train_vertex, b.train_query[0], b.train_target[0],
+                              b.train_end_query, b.train_end_inferred, b.train_suffix};
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    for (uint32_t k = b.num_sets > 1 ? b.num_sets : 1; k < n; ++k) {
+        vpt::TrainSet& t = b.sets[k];
+        chk(alloc_zero(&t.counters, 16));
+        chk(alloc_zero(&t.rng, npix));
+        chk(alloc_zero(&t.vertex, vpt::kTrainBufferSize));
+        chk(alloc_zero(&t.query0, static_cast<size_t>(vpt::kTrainBufferSize) * vpt::kQueryFloats));
+        chk(alloc_zero(&t.target0, static_cast<size_t>(vpt::kTrainBufferSize) * 3));
+        chk(alloc_zero(&t.end_query, npix * vpt::kQueryFloats));
+        chk(alloc_zero(&t.end_inferred, npix * 3));
+        chk(alloc_zero(&t.suffix, npix));
+        if (e == cudaSuccess) {
+            uint64_t mult, plus;
+            set_jump(k, &mult, &plus);
+            const uint32_t np = static_cast<uint32_t>(npix);
+            derive_states_kernel<<<(np + 255) / 256, 256>>>(t.rng, c->d_rng, np, mult, plus);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess && !b.train_sets) e = cudaMalloc(reinterpret_cast<void**>(&b.train_sets), sizeof(b.sets));
+    if (e == cudaSuccess) e = cudaMemcpy(b.train_sets, b.sets, sizeof(b.sets), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        c->release_nrc();
+        return fail(VPT_ERR_OUT_OF_MEMORY, std::string("training sets: ") + cudaGetErrorString(e));
+    }
+    b.num_sets = n;
+    return VPT_OK;
+}
+
+// The cache's buffers as the set-up kernels see them for training set k.
+vpt::NrcBuffers set_view(const vpt::NrcBuffers& b, uint32_t k) {
+    vpt::NrcBuffers v = b;
+    const vpt::TrainSet& t = b.sets[k];
+    v.counters = t.counters;
+    v.train_rng = t.rng;
+    v.train_vertex = t.vertex;
+    v.train_query[0] = t.query0;
+    v.train_target[0] = t.target0;
+    v.train_end_query = t.end_query;
+    v.train_end_inferred = t.end_inferred;
+    v.train_suffix = t.suffix;
+    return v;
+}
+
 // Launch of a radiance-cache pass of the persistent tracker: the training pass or a render pass
 // of one sample per pixel on the per-pixel streams (stream_mode 0), or a render pass of `spp`
 // samples per pixel on sample-parallel streams (stream_mode 1). With `index_queries` the render
 // paths also list the slots of the queries they write (infer_index, counters[8]).
 int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
-                bool index_queries = false) {
+                bool index_queries = false, uint32_t num_sets = 0, uint32_t set_bufs = 0) {
     if (c->surf || !c->has_volume)
         return fail(VPT_ERR_INVALID_ARGUMENT, "the radiance-cache passes need a volume and no surfaces");
     int rc = ensure_nrc(c);
@@ -142,7 +203,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.spp = spp;
     tp.accum_base = 0;
     tp.stream_mode = stream_mode;
-    if (stream_mode == 1) {
+    if (stream_mode == 1 && spp > 0) {  // a combined launch of training sets alone has no samples
         if ((rc = vpt::upload_sample_jumps(c, spp, s))) return rc;
         tp.sample_jumps = c->d_jumps;
     }
@@ -154,6 +215,9 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
         tp.nrc.infer_index = nullptr;
     }
     tp.nrc_buf = buf;
+    tp.train_sets = c->nrc->train_sets;
+    tp.num_train_sets = num_sets;
+    tp.train_bufs = set_bufs;
     tp.nrc_density_query = c->nrc_query_density;
     tp.nrc_termination = c->nrc_termination;
     tp.nrc_train_termination = c->nrc_train_termination;
@@ -168,7 +232,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj), smem);
     vpt::launch_nrc_pass(tp, mode, grid_maj, ctas, threads, smem, s);
     NRCP_CUDA(cudaGetLastError());
-    if (stream_mode == 1) {
+    if (stream_mode == 1 && spp > 0) {
         vpt::launch_frame_update(c->d_frame, spp, false, 0, s);
         c->stream_samples += spp;
     }
@@ -186,6 +250,10 @@ int nrc_reseed_train_rng(VptContextImpl* c) {
     lcg_jump(1ull << 62, &mult, &plus);
     const uint32_t n = static_cast<uint32_t>(c->width) * static_cast<uint32_t>(c->height);
     derive_states_kernel<<<(n + 255) / 256, 256>>>(c->nrc->train_rng, c->d_rng, n, mult, plus);
+    for (uint32_t k = 1; k < c->nrc->num_sets; ++k) {
+        set_jump(k, &mult, &plus);
+        derive_states_kernel<<<(n + 255) / 256, 256>>>(c->nrc->sets[k].rng, c->d_rng, n, mult, plus);
+    }
     NRCP_CUDA(cudaGetLastError());
     NRCP_CUDA(cudaDeviceSynchronize());
     return VPT_OK;
@@ -210,6 +278,18 @@ void VptContextImpl::release_nrc() {
     free_ptr(nrc->shufflers);
     free_ptr(nrc->counters);
     free_ptr(nrc->stats);
+    for (uint32_t k = 1; k < kMaxTrainSets; ++k) {
+        TrainSet& t = nrc->sets[k];
+        free_ptr(t.counters);
+        free_ptr(t.rng);
+        free_ptr(t.vertex);
+        free_ptr(t.query0);
+        free_ptr(t.target0);
+        free_ptr(t.end_query);
+        free_ptr(t.end_inferred);
+        free_ptr(t.suffix);
+    }
+    free_ptr(nrc->train_sets);
     delete nrc;
     nrc = nullptr;
 }
@@ -353,30 +433,58 @@ int vpt_nrc_frame(VptContext* c, void* nrc, void* stream, uint32_t train_iterati
     if (batched && (rc = ensure_render_slots(c, spp))) return rc;
     vpt::NrcBuffers& b = *c->nrc;
     const bool combo = batched && c->nrc_combined_pass;
-    for (uint32_t it = 0; it < train_iterations; ++it) {
-        c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
-        const uint32_t buf = c->nrc_buf_index;
-        const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
-        if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
-        if (combo && it == 0) {
-            // The first training pass and the frame's render samples in one launch: the render
-            // paths need the network only at their inference, after the training steps below.
-            if ((rc = launch_pass(c, s, vpt::kModeComboNrc, buf, spp, 1, true))) return rc;
-        } else if ((rc = vpt_launch_generate_training(c, stream, buf))) {
-            return rc;
-        }
-        // Predictions for the training suffixes' end queries (trainW * trainH of them).
-        if (nrc_infer_device_count(net, stream, b.train_end_query, b.counters + 7, b.max_train_suffixes,
-                                   b.train_end_inferred))
+    constexpr uint32_t kBatch = vpt::kNumTrainingDataPerFrame / 4;  // renderer_main.cpp:1595
+    // Predictions for a training pass's suffix-end queries, propagation, shuffle and the four
+    // training steps of one iteration (renderer_main.cpp:1578-1600) on the buffers `v`.
+    auto post_pass = [&](const vpt::NrcBuffers& v, uint32_t buf) -> int {
+        if (nrc_infer_device_count(net, stream, v.train_end_query, v.counters + 7, v.max_train_suffixes,
+                                   v.train_end_inferred))
             return fail(VPT_ERR_CUDA, std::string("nrc_infer_device_count: ") + nrc_last_error());
-        if ((rc = vpt_propagate(c, stream))) return rc;
-        if ((rc = vpt_shuffle(c, stream, buf))) return rc;
-        constexpr uint32_t kBatch = vpt::kNumTrainingDataPerFrame / 4;  // renderer_main.cpp:1595
+        vpt::nrc_propagate(v, radiance_scale(c), s);
+        vpt::nrc_shuffle(v, buf, radiance_scale(c), s);
+        NRCP_CUDA(cudaGetLastError());
         for (uint32_t step = 0; step < 4; ++step) {
             const size_t first = static_cast<size_t>(step) * kBatch;
-            if (nrc_train(net, stream, b.train_query[1] + first * vpt::kQueryFloats, b.train_target[1] + first * 3, kBatch,
-                          nullptr))
+            if (nrc_train(net, stream, v.train_query[1] + first * vpt::kQueryFloats, v.train_target[1] + first * 3,
+                          kBatch, nullptr))
                 return fail(VPT_ERR_CUDA, std::string("nrc_train: ") + nrc_last_error());
+        }
+        return VPT_OK;
+    };
+    if (combo && train_iterations > 0) {
+        // The frame's training passes are traced in the launch of its render samples (up to
+        // kMaxTrainSets of them per launch, each into its own training set): no pass's path
+        // needs the network, only the predictions of its suffix ends, which are inferred after
+        // the training steps of the iterations before it, in order, as the sequential frame does.
+        // A frame of more iterations (the first one: 8) launches groups of sets, the render
+        // samples with the last group.
+        const uint32_t group_max = train_iterations < vpt::kMaxTrainSets ? train_iterations : vpt::kMaxTrainSets;
+        if ((rc = ensure_train_sets(c, group_max))) return rc;
+        for (uint32_t it = 0; it < train_iterations;) {
+            const uint32_t group = train_iterations - it < group_max ? train_iterations - it : group_max;
+            const bool last = it + group == train_iterations;
+            uint32_t bufs = 0;
+            for (uint32_t k = 0; k < group; ++k) {
+                b.set_buf[k] ^= 1u;
+                bufs |= b.set_buf[k] << k;
+                const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
+                vpt::nrc_prepare(set_view(b, k), b.set_buf[k], offset, new_sequence != 0, s);
+            }
+            NRCP_CUDA(cudaGetLastError());
+            if ((rc = launch_pass(c, s, vpt::kModeComboNrc, 0, last ? spp : 0, 1, last, group, bufs))) return rc;
+            for (uint32_t k = 0; k < group; ++k)
+                if ((rc = post_pass(set_view(b, k), b.set_buf[k]))) return rc;
+            it += group;
+        }
+        c->nrc_buf_index = b.set_buf[0];
+    } else {
+        for (uint32_t it = 0; it < train_iterations; ++it) {
+            c->nrc_buf_index = (c->nrc_buf_index + 1) % 2;
+            const uint32_t buf = c->nrc_buf_index;
+            const uint32_t offset = static_cast<uint32_t>(c->nrc_offset_rng());
+            if ((rc = vpt_prepare_nrc(c, stream, buf, offset, new_sequence))) return rc;
+            if ((rc = vpt_launch_generate_training(c, stream, buf))) return rc;
+            if ((rc = post_pass(b, buf))) return rc;
         }
     }
     if (spp == 0) return VPT_OK;

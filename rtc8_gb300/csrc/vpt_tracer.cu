@@ -324,11 +324,52 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
     // Training image of the pass (the adaptive size prepared on the device). The pass image
     // size, the item counts and the state buffer a sample continues are derived from these and
     // `is_train` where needed rather than held in registers.
-    uint32_t train_w = 0, train_h = 0;
-    if constexpr (kMayTrain) {
+    // A combined launch traces P.num_train_sets training images (the frame's training
+    // iterations), set k from the arrays of P.train_sets[k]; tset is the set of the lane's item.
+    uint32_t train_w = 0, train_h = 0, num_train = 0, tset = 0;
+    auto set_buf = [&](uint32_t k) -> uint32_t { return (P.train_bufs >> k) & 1u; };
+    auto set_w = [&](uint32_t k) -> uint32_t {
+        return min(P.train_sets[k].counters[2 + 2 * set_buf(k)], static_cast<uint32_t>(P.width));
+    };
+    auto set_h = [&](uint32_t k) -> uint32_t {
+        return min(P.train_sets[k].counters[3 + 2 * set_buf(k)], static_cast<uint32_t>(P.height));
+    };
+    if constexpr (kMode == kModeTrainNrc) {
         train_w = min(P.nrc.counters[2 + 2 * P.nrc_buf], static_cast<uint32_t>(P.width));
         train_h = min(P.nrc.counters[3 + 2 * P.nrc_buf], static_cast<uint32_t>(P.height));
+        num_train = min(train_w * train_h, num_pixels);
+    } else if constexpr (kCombo) {
+        for (uint32_t k = 0; k < P.num_train_sets; ++k) num_train += min(set_w(k) * set_h(k), num_pixels);
     }
+    // The arrays a training item writes: its set's in a combined launch, the pass's own otherwise.
+    auto tr_counters = [&]() -> uint32_t* {
+        if constexpr (kCombo) return P.train_sets[tset].counters;
+        else return P.nrc.counters;
+    };
+    auto tr_buf = [&]() -> uint32_t {
+        if constexpr (kCombo) return set_buf(tset);
+        else return P.nrc_buf;
+    };
+    auto tr_vertex = [&]() -> TrainVertexInfo* {
+        if constexpr (kCombo) return P.train_sets[tset].vertex;
+        else return P.nrc.train_vertex;
+    };
+    auto tr_query0 = [&]() -> float* {
+        if constexpr (kCombo) return P.train_sets[tset].query0;
+        else return P.nrc.train_query[0];
+    };
+    auto tr_target0 = [&]() -> float* {
+        if constexpr (kCombo) return P.train_sets[tset].target0;
+        else return P.nrc.train_target[0];
+    };
+    auto tr_end_query = [&]() -> float* {
+        if constexpr (kCombo) return P.train_sets[tset].end_query;
+        else return P.nrc.train_end_query;
+    };
+    auto tr_suffix = [&]() -> uint32_t* {
+        if constexpr (kCombo) return P.train_sets[tset].suffix;
+        else return P.nrc.train_suffix;
+    };
     uint32_t slot = 0;  // record index of the current sample in the pass buffers
     const float term_factor = P.nrc_termination > 0 ? P.nrc_termination : kPathTerminationFactor;
     // Biased training suffixes end at twice the render factor (optix_pathtracing_kernels.cu:
@@ -482,7 +523,6 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                 base = __shfl_sync(need, base, leader);
                 const uint32_t item = base + __popc(need & ((1u << lane) - 1u));
                 if constexpr (kNrc) {
-                    const uint32_t num_train = kMayTrain ? min(train_w * train_h, num_pixels) : 0u;
                     // Sample-parallel streams: P.spp samples per pixel in one render pass, each
                     // its own work item and record slot (sample-major: slot = sample * pixels + pixel).
                     uint32_t num_items = num_pixels;
@@ -499,15 +539,30 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                     if constexpr (kCombo) is_train = item < num_train;
                     sample = 0;
                     if (kMayTrain && is_train) {
-                        uint32_t px, py;
-                        train_item_to_pixel(item, train_w, train_h, P.nrc.counters[6], &px, &py);
-                        pixel = py * train_w + px;  // linear index in the training image
+                        uint32_t px, py, local = item, tw = train_w, th = train_h;
+                        if constexpr (kCombo) {
+                            tset = 0;
+                            while (tset + 1 < P.num_train_sets) {
+                                const uint32_t n = min(set_w(tset) * set_h(tset), num_pixels);
+                                if (local < n) break;
+                                local -= n;
+                                ++tset;
+                            }
+                            tw = set_w(tset);
+                            th = set_h(tset);
+                        }
+                        const uint32_t offset = tr_counters()[6];
+                        train_item_to_pixel(local, tw, th, offset, &px, &py);
+                        pixel = py * tw + px;  // linear index in the training image
                         slot = pixel;
                         rng_index = py * static_cast<uint32_t>(P.width) + px;
-                        rng.state = (kCombo ? P.nrc.train_rng : P.rng)[rng_index];
+                        if constexpr (kCombo)
+                            rng.state = P.train_sets[tset].rng[rng_index];
+                        else
+                            rng.state = P.rng[rng_index];
                         // optix_pathtracing_kernels.cu:60-66: one unbiased suffix per 4x4 tile.
                         const uint32_t tile_index = (py % 4) * 4 + (px % 4);
-                        unbiased = (tile_index + P.nrc.counters[6]) % 16 == 0;
+                        unbiased = (tile_index + offset) % 16 == 0;
                         st = ST_CAMERA;
                         break;
                     }
@@ -559,8 +614,11 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
             }
             case ST_CAMERA: {
                 // optix_pathtracing_kernels.cu:43-55, 76-81.
-                const uint32_t img_w = (kMayTrain && is_train) ? train_w : static_cast<uint32_t>(P.width);
-                const uint32_t img_h = (kMayTrain && is_train) ? train_h : static_cast<uint32_t>(P.height);
+                uint32_t img_w = static_cast<uint32_t>(P.width), img_h = static_cast<uint32_t>(P.height);
+                if (kMayTrain && is_train) {
+                    img_w = kCombo ? set_w(tset) : train_w;
+                    img_h = kCombo ? set_h(tset) : train_h;
+                }
                 uint32_t px = pixel % img_w;
                 uint32_t py = pixel / img_w;
                 float ux = rng.uniform();
@@ -670,8 +728,8 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         // :148-152: the environment hit completes the previous vertex's target.
                         if (prev_vertex != kInvalidVertex) {
                             // The previous vertex's local throughput, as this lane recorded it.
-                            const TrainVertexInfo& pv = P.nrc.train_vertex[prev_vertex];
-                            float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(prev_vertex);
+                            const TrainVertexInfo& pv = tr_vertex()[prev_vertex];
+                            float* tg = tr_target0() + 3 * static_cast<size_t>(prev_vertex);
                             RGB add = rgb(pv.local_tp[0], pv.local_tp[1], pv.local_tp[2]) * implicit;
                             tg[0] += add.r;
                             tg[1] += add.g;
@@ -723,11 +781,11 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                     }
                     if (ends_with_cache) {
                         const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
-                        float* qdst = (kMayTrain && is_train) ? P.nrc.train_end_query : P.nrc.infer_query;
+                        float* qdst = (kMayTrain && is_train) ? tr_end_query() : P.nrc.infer_query;
                         write_query(qdst + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough, P.albedo, wmin,
                                     wmax);
                         if (kMayTrain && is_train) {
-                            P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                            tr_suffix()[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         } else {
                             TerminalInfo ti;
                             ti.tp[0] = throughput.r;
@@ -975,26 +1033,26 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                     // :358-409: record the training vertex (query, local throughput, link to the
                     // previous vertex, target initialised with the NEE estimate); a full buffer
                     // ends the suffix with a cache query.
-                    const uint32_t idx = atomicAdd(P.nrc.counters + P.nrc_buf, 1u);
+                    const uint32_t idx = atomicAdd(tr_counters() + tr_buf(), 1u);
                     const float rough = P.nrc_density_query && P.density_coeff > 0 ? last_density / P.density_coeff : 0.0f;
                     if (idx < kTrainBufferSize) {
-                        write_query(P.nrc.train_query[0] + kQueryFloats * static_cast<size_t>(idx), origin, v_out, rough,
+                        write_query(tr_query0() + kQueryFloats * static_cast<size_t>(idx), origin, v_out, rough,
                                     P.albedo, wmin, wmax);
                         TrainVertexInfo vi;
                         vi.local_tp[0] = local_tp.r;
                         vi.local_tp[1] = local_tp.g;
                         vi.local_tp[2] = local_tp.b;
                         vi.bits = (prev_vertex & kInvalidVertex) | ((path_length & 0xFFu) << 22) | ((unbiased ? 1u : 0u) << 30);
-                        P.nrc.train_vertex[idx] = vi;
-                        float* tg = P.nrc.train_target[0] + 3 * static_cast<size_t>(idx);
+                        tr_vertex()[idx] = vi;
+                        float* tg = tr_target0() + 3 * static_cast<size_t>(idx);
                         tg[0] = nee_value.r;
                         tg[1] = nee_value.g;
                         tg[2] = nee_value.b;
                         prev_vertex = idx;
                     } else {
-                        write_query(P.nrc.train_end_query + kQueryFloats * static_cast<size_t>(slot), origin, v_out,
+                        write_query(tr_end_query() + kQueryFloats * static_cast<size_t>(slot), origin, v_out,
                                     rough, P.albedo, wmin, wmax);
-                        P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                        tr_suffix()[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
                         terminal_written = true;
                         err |= VPT_DEVERR_TRAIN_FULL;
                         end_code = END_TRAIN_FULL;
@@ -1011,7 +1069,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                 if constexpr (kNrc) {
                     if (kMayTrain && is_train) {
                         if (!terminal_written)
-                            P.nrc.train_suffix[slot] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
+                            tr_suffix()[slot] = pack_suffix(prev_vertex, 0, path_length, unbiased ? 1 : 0);
                     } else {
                         if (!terminal_written) {
                             TerminalInfo ti;
@@ -1032,7 +1090,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         fc[2] = c.b;
                     }
                     if ((kMayTrain && is_train) || !sample_parallel)
-                        ((kCombo && is_train) ? P.nrc.train_rng : P.rng)[rng_index] = rng.state;
+                        ((kCombo && is_train) ? P.train_sets[tset].rng : P.rng)[rng_index] = rng.state;
                     st = ST_FETCH;
                     break;
                 }

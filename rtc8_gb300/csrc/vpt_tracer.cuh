@@ -64,6 +64,11 @@ struct TraceParams {
     // Radiance-cache passes only.
     NrcBuffers nrc;
     uint32_t nrc_buf;           // training buffer of this frame (nrcBufferIndex)
+    // kModeComboNrc: the launch traces num_train_sets training images, set k from the arrays of
+    // train_sets[k] with buffer index (train_bufs >> k) & 1, before the render samples.
+    const TrainSet* train_sets;
+    uint32_t num_train_sets;
+    uint32_t train_bufs;
     int32_t nrc_density_query;  // 1: the query's roughness slot carries density / density_coeff
     float nrc_termination;      // path-spread termination factor c (0 = 0.01, renderer_shared.h:11)
     float nrc_train_termination;  // factor of biased training suffixes (0 = 2c)

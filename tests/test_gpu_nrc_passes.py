@@ -289,6 +289,42 @@ def test_nrc_frame_loop_gain_over_truncated_paths(cuda_device):
     p.close()
 
 
+def test_frame_with_training_sets_in_one_launch(cuda_device):
+    """On sample-parallel streams the frame call traces all of its training iterations in the
+    launch of its render samples (one training set per iteration; the first frame's eight in two
+    launches of four). The cache trained that way gives the plain estimate's image, like the
+    sequential frame loop above; every iteration still runs its four training steps."""
+    import torch
+
+    cfg = small_config_mode(size=128, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=1)
+    vox, env = _scene(cfg)
+    r = _setup(cfg, vox, env)
+    cache = nrc.NeuralRadianceCache()
+    cache.initialize(config=nrc.default_config(nrc.NRC_ENCODING_VOLUME))
+    r.nrc_set_query_density(True)
+    r.nrc_frame(cache, 8, 4, True)
+    for _ in range(10):
+        r.nrc_frame(cache, 4, 4, False)
+    torch.cuda.synchronize()
+    assert r.device_errors() == 0 and cache.device_errors() == 0
+    assert cache.lib.nrc_step_count(cache.h) == 4 * (8 + 40)
+    r.reset_accumulation()
+    for _ in range(16):
+        r.nrc_frame(cache, 4, 4, False)
+    img_nrc = r.image()
+    assert np.all(np.isfinite(img_nrc))
+    p = Renderer(cfg.width, cfg.height)
+    setup_scene(p, cfg, volume=vox)
+    p.set_environment_rgb(env)
+    p.launch_plain(256)
+    rel = _rel(_blocks(img_nrc), _blocks(p.image()))
+    assert rel < 0.02, rel
+    assert r.device_errors() == 0
+    cache.finalize()
+    r.close()
+    p.close()
+
+
 def _pcg_jump(states: np.ndarray, delta: int) -> np.ndarray:
     """PCG32 state advanced by `delta` draws (LCG jump-ahead by squaring, Brown 1994)."""
     mult, plus = 6364136223846793005, 1
