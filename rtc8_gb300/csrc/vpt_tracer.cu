@@ -173,7 +173,7 @@ __device__ __forceinline__ int track_pass(const Grid& g, const float* maj_grid, 
 __device__ __forceinline__ void write_query(float* q, V3 pos, V3 vout, float roughness, float albedo, V3 wmin, V3 wmax) {
     V3 d = wmax - wmin, r = pos - wmin;
     float a, b;
-    to_polar_yup(vout, &a, &b);
+    to_polar_yup_sel(vout, &a, &b);
     float2* p = reinterpret_cast<float2*>(q);
     p[0] = make_float2(d.x != 0 ? r.x / d.x : 0.0f, d.y != 0 ? r.y / d.y : 0.0f);
     p[1] = make_float2(d.z != 0 ? r.z / d.z : 0.0f, a);
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                 // optix_pathtracing_kernels.cu:130-174.
                 if (P.env_enabled) {
                     float hyp_pdf;
-                    RGB radiance = env_evaluate(P.env, dir, &hyp_pdf);
+                    RGB radiance = env_evaluate<kNrc>(P.env, dir, &hyp_pdf);
                     float mis = 1.0f;
                     if (path_length > 1) {
                         float sel = P.sun.enabled ? (1.0f - P.sun.select_prob) : 1.0f;
