@@ -291,6 +291,16 @@ def mlp_bench(steps: int, warmup: int) -> dict:
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
     inf_tf = n_inf * flop_fwd / t_inf / 1e12
+    # Ceiling of the network's MMA shapes: cycles per back-to-back M = 128, K = 16 MMA issued by one
+    # thread at N = 16 (output layer), 64 (hidden and input layers) and 256 (the full rate). A
+    # 128-row tile is 9 + 16 MMAs of N = 64 and 4 of N = 16; at the full rate its arithmetic would
+    # take 128 * flop_fwd / 2 MACs / (MACs per cycle at N = 256).
+    cyc = {str(nn): nrc.selftest_mma_rate(nn, 1024) for nn in (16, 64, 128, 256)}
+    full_rate = 128 * 256 * 16 / cyc["256"]
+    tile_floor = 25 * cyc["64"] + 4 * cyc["16"]
+    mma_ceiling = {"cycles_per_mma": cyc, "tile_floor_cycles": tile_floor,
+                   "tile_arith_cycles_at_full_rate": 128 * flop_fwd / 2 / full_rate,
+                   "tensor_pipe_ceiling": 128 * flop_fwd / 2 / full_rate / tile_floor}
     tr_tf = n_tr * 3 * flop_fwd / t_tr / 1e12
     errors = cache.device_errors()
     cache.finalize()
@@ -298,7 +308,8 @@ def mlp_bench(steps: int, warmup: int) -> dict:
             "infer_tflops": inf_tf, "infer_frac_of_peak": inf_tf / peak, "train_step_ms": t_tr * 1e3,
             "train_tflops": tr_tf, "train_frac_of_peak": tr_tf / peak,
             "peak_tflops": peak, "peak_source": "measured bf16_tflops (dense FP16 has the same rate)",
-            "infer_records": n_inf, "train_records": n_tr, "train_larger_batches": big, "device_errors": errors}
+            "infer_records": n_inf, "train_records": n_tr, "train_larger_batches": big,
+            "mma_shape_ceiling": mma_ceiling, "device_errors": errors}
 
 
 def nrc_frame_loop(frames: int, warmup: int, combined: bool = True) -> dict:

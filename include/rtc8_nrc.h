@@ -102,6 +102,12 @@ uint32_t nrc_device_errors(NrcHandle* h);
  * writes D (128 x 64, FP32) to host memory. Checks the shared-memory descriptor layouts the
  * MLP kernels rely on. */
 int nrc_selftest_mma(const float* a, const float* b, int32_t a_mn_major, int32_t b_mn_major, float* d);
+/* Tensor-core issue-rate probe: one thread issues `count` (rounded up to a multiple of 4, at most
+ * 65536) back-to-back tcgen05 MMAs of M = 128, N = `n` (a multiple of 16 in [16, 256]), K = 16,
+ * FP16 operands in shared memory, FP32 accumulators in tensor memory, on one SM; writes the SM
+ * clock cycles per MMA from the first issue to the completion of the last. It measures the rate
+ * the MLP kernels' MMA shapes can reach (their hidden layers are N = 64). */
+int nrc_selftest_mma_rate(int32_t n, uint32_t count, double* cycles_per_mma);
 
 #ifdef __cplusplus
 }

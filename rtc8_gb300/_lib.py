@@ -233,6 +233,7 @@ _NRC = {
     "nrc_step_count": (C.c_uint64, [C.c_void_p]),
     "nrc_device_errors": (C.c_uint32, [C.c_void_p]),
     "nrc_selftest_mma": (C.c_int, [c_float_p, c_float_p, C.c_int32, C.c_int32, c_float_p]),
+    "nrc_selftest_mma_rate": (C.c_int, [C.c_int32, C.c_uint32, c_double_p]),
 }
 
 

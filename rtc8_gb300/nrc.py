@@ -135,6 +135,15 @@ class NeuralRadianceCache:
         return int(self.lib.nrc_device_errors(self.h))
 
 
+def selftest_mma_rate(n: int, count: int = 1024) -> float:
+    """nrc_selftest_mma_rate: SM cycles per back-to-back M = 128 x N = n x K = 16 FP16 MMA issued by
+    one thread (the rate the MLP kernels' layer shapes can reach)."""
+    lib = _lib.load()
+    c = C.c_double(0.0)
+    _check(lib.nrc_selftest_mma_rate(n, count, C.byref(c)), "nrc_selftest_mma_rate")
+    return c.value
+
+
 def selftest_mma(a: np.ndarray, b: np.ndarray, a_mode: int, b_mode: int) -> np.ndarray:
     a = np.ascontiguousarray(a, np.float32)
     b = np.ascontiguousarray(b, np.float32)

@@ -56,6 +56,16 @@ def test_tensor_core_descriptor_layouts(cuda_device, a_mode, b_mode):
     assert err < 1e-3
 
 
+def test_mma_rate_probe(cuda_device):
+    """The issue-rate probe behind the bench's MMA-shape ceiling: it completes, and wider MMAs
+    take at least as long per instruction (an N = 256 MMA is four N = 64 MMAs of work)."""
+    cyc = {n: nrc.selftest_mma_rate(n, 256) for n in (64, 256)}
+    assert all(c > 0 for c in cyc.values())
+    assert cyc[256] >= cyc[64]
+    with pytest.raises(nrc.NrcError):
+        nrc.selftest_mma_rate(72, 256)
+
+
 @pytest.mark.parametrize("encoding", [nrc.NRC_ENCODING_REFERENCE, nrc.NRC_ENCODING_VOLUME])
 def test_encodings_match_oracle(cuda_device, encoding):
     import torch
