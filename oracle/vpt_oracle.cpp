@@ -1154,6 +1154,28 @@ void write_query(const OrcScene& s, float* q, V3 pos, V3 vout, float roughness) 
     q[11] = q[12] = q[13] = 0.0f;
 }
 
+// RadianceQuery of a surface vertex (optix_pathtracing_kernels.cu:14-29 with getSurfaceParameters,
+// common_renderer_types.h:1491-1496 Lambert, 1671-1677 dichromatic): position in the world box,
+// shading normal and vOut as polar angles, roughness, diffuse and specular reflectance.
+void write_query_surf(const OrcScene& s, float* q, V3 pos, V3 normal, V3 vout, const OrcSurfaces::Mat& m) {
+    const float d[3] = {s.world_max[0] - s.world_min[0], s.world_max[1] - s.world_min[1],
+                        s.world_max[2] - s.world_min[2]};
+    const float r[3] = {pos.x - s.world_min[0], pos.y - s.world_min[1], pos.z - s.world_min[2]};
+    for (int a = 0; a < 3; ++a) q[a] = d[a] != 0 ? r[a] / d[a] : 0.0f;
+    float th, ph;
+    to_polar_yup(normal, &th, &ph);
+    q[3] = th;
+    q[4] = ph;
+    to_polar_yup(vout, &th, &ph);
+    q[5] = th;
+    q[6] = ph;
+    q[7] = m.roughness;
+    for (int a = 0; a < 3; ++a) {
+        q[8 + a] = m.diffuse[a];
+        q[11 + a] = m.specular[a];
+    }
+}
+
 inline uint32_t suffix_bits(uint32_t prev, uint32_t has_query, uint32_t path_length, uint32_t unbiased) {
     return (prev & ORC_NRC_INVALID_VERTEX) | ((has_query & 1u) << 22) | ((path_length & 0xFFu) << 23) |
            ((unbiased & 1u) << 31);
@@ -1227,13 +1249,24 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
             }
         }
         if (!collided && hit_tri >= 0) {
-            // A triangle hit: surface point, emission against area-light sampling (:216-239),
-            // Russian roulette, NEE, BSDF sampling and the offset origin (:254-356).
+            // A triangle hit: surface point, path spread, emission against area-light sampling
+            // (:176-239), Russian roulette and the radiance-cache end (:254-330), NEE, BSDF
+            // sampling, the offset origin and the training vertex (:332-409).
             const OrcSurfaces& S = *s.surfaces;
             const SurfPt sp = surface_point(S, static_cast<uint32_t>(hit_tri), hb1, hb2, s.env_enabled != 0);
             const V3 ray_origin = origin;
             const V3 q = to_local(sp.sf, -dir);
             const OrcSurfaces::Mat& mt = S.mats[sp.material];
+            if (with_nrc) {
+                // :200-210, |cos| against the geometric normal.
+                const V3 dv = ray_origin - sp.pos;
+                const float dist2 = dv.x * dv.x + dv.y * dv.y + dv.z * dv.z;
+                const float abs_dot = std::fabs(dot(dir, sp.gn));
+                if (path_length == 1)
+                    primary_spread = dist2 / (4 * kPi * abs_dot);
+                else
+                    sqrt_spread += std::sqrt(dist2 / (dir_pdf * abs_dot));
+            }
             if (q.z > 0 && mt.emissive) {
                 float mis = 1.0f;
                 if (path_length > 1) {
@@ -1243,25 +1276,63 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                     const float bsdf_pdf = dir_pdf;
                     mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                 }
-                contribution = contribution + throughput * (rgb(mt.emit[0], mt.emit[1], mt.emit[2]) * (mis / kPi));
+                const RGB implicit = rgb(mt.emit[0], mt.emit[1], mt.emit[2]) * (mis / kPi);
+                if (!train) contribution = contribution + throughput * implicit;
+                if (train && prev_vertex != ORC_NRC_INVALID_VERTEX) {
+                    float* tg = nrc->train_target + 3 * static_cast<size_t>(prev_vertex);
+                    const RGB add = prev_local_tp * implicit;
+                    tg[0] += add.r;
+                    tg[1] += add.g;
+                    tg[2] += add.b;
+                }
             }
             float continue_prob = 1.0f;
-            if (static_cast<int32_t>(path_length) >= s.rr_start) {
+            bool rr_kill = false;
+            const int32_t rr_from = train ? std::max(s.rr_start, 3) : s.rr_start;
+            if (static_cast<int32_t>(path_length) >= rr_from) {
                 continue_prob = std::fmin(luminance(throughput) / init_importance, 1.0f);
-                if (rng.uniform() >= continue_prob) {
-                    end_code = ORC_END_RR;
+                if (rng.uniform() >= continue_prob) rr_kill = true;
+            }
+            if (!with_nrc && rr_kill) {
+                end_code = ORC_END_RR;
+                break;
+            }
+            if (with_nrc) {
+                bool ends_with_cache = rr_kill;
+                const float spread2 = sqrt_spread * sqrt_spread;
+                if (train) {
+                    if (!unbiased) ends_with_cache |= spread2 > train_term_factor * primary_spread;
+                } else {
+                    ends_with_cache |= spread2 > term_factor * primary_spread;
+                }
+                if (ends_with_cache) {
+                    write_query_surf(s, nrc->infer_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(item), sp.pos,
+                                     sp.sf.n, -dir, mt);
+                    if (train) {
+                        nrc->train_suffix[item] = suffix_bits(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                    } else {
+                        float* tp = nrc->terminal_tp + 3 * static_cast<size_t>(item);
+                        tp[0] = throughput.r;
+                        tp[1] = throughput.g;
+                        tp[2] = throughput.b;
+                        nrc->terminal_bits[item] = 1u | ((path_length & 0xFFu) << 1);
+                    }
+                    terminal_written = true;
+                    end_code = ORC_END_CACHE;
                     break;
                 }
             }
             throughput = div(throughput, continue_prob);
             const Brdf f = brdf_of(mt);
             bool capped = false;
-            const RGB nee = next_event_surf(s, rng, sp.pos, sp.sf, &sp, &f, q, &rec[2], lookups, &capped);
+            OrcScene s_nee = s;
+            if (train) s_nee.shadow_rr = 0.0f;
+            const RGB nee = next_event_surf(s_nee, rng, sp.pos, sp.sf, &sp, &f, q, &rec[2], lookups, &capped);
             if (capped) {
                 end_code = ORC_END_STEP_CAP;
                 break;
             }
-            contribution = contribution + throughput * nee;
+            if (!train) contribution = contribution + throughput * nee;
             if (s.max_bounces > 0 && static_cast<int32_t>(path_length) >= s.max_bounces) {
                 end_code = ORC_END_MAX_BOUNCES;
                 break;
@@ -1275,11 +1346,39 @@ RGB trace_path(const OrcScene& s, Pcg32& rng, int px, int py, uint32_t rec[4], i
                 end_code = ORC_END_PDF_ZERO;
                 break;
             }
+            const V3 v_out = -dir;
             dir = from_local(sp.sf, local);
             const float dot_sgn = dot(dir, sp.gn);
-            throughput = throughput * (fs * (std::fabs(dot_sgn) / pdf));
+            const RGB local_tp = fs * (std::fabs(dot_sgn) / pdf);
+            throughput = throughput * local_tp;
             origin = offset_origin(sp.pos, (dot_sgn > 0.0f ? 1.0f : -1.0f) * sp.gn);
             dir_pdf = pdf;
+            if (train) {
+                const uint32_t idx = (*nrc->num_train)++;
+                if (idx < ORC_NRC_TRAIN_BUFFER_SIZE) {
+                    write_query_surf(s, nrc->train_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(idx), sp.pos,
+                                     sp.sf.n, v_out, mt);
+                    float* lt = nrc->train_local_tp + 3 * static_cast<size_t>(idx);
+                    lt[0] = local_tp.r;
+                    lt[1] = local_tp.g;
+                    lt[2] = local_tp.b;
+                    nrc->train_bits[idx] = (prev_vertex & ORC_NRC_INVALID_VERTEX) | ((path_length & 0xFFu) << 22) |
+                                           ((unbiased ? 1u : 0u) << 30);
+                    float* tg = nrc->train_target + 3 * static_cast<size_t>(idx);
+                    tg[0] = nee.r;
+                    tg[1] = nee.g;
+                    tg[2] = nee.b;
+                    prev_local_tp = local_tp;
+                    prev_vertex = idx;
+                } else {
+                    write_query_surf(s, nrc->infer_query + ORC_NRC_QUERY_FLOATS * static_cast<size_t>(item), sp.pos,
+                                     sp.sf.n, v_out, mt);
+                    nrc->train_suffix[item] = suffix_bits(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                    terminal_written = true;
+                    end_code = ORC_END_TRAIN_FULL;
+                    break;
+                }
+            }
             continue;
         }
         if (!collided) {

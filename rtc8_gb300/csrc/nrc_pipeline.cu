@@ -192,8 +192,8 @@ vpt::NrcBuffers set_view(const vpt::NrcBuffers& b, uint32_t k) {
 // paths also list the slots of the queries they write (infer_index, counters[8]).
 int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t spp = 1, int32_t stream_mode = 0,
                 bool index_queries = false, uint32_t num_sets = 0, uint32_t set_bufs = 0) {
-    if (c->surf || !c->has_volume)
-        return fail(VPT_ERR_INVALID_ARGUMENT, "the radiance-cache passes need a volume and no surfaces");
+    if (!c->surf && !c->has_volume)
+        return fail(VPT_ERR_INVALID_ARGUMENT, "the radiance-cache passes need a volume or surfaces");
     int rc = ensure_nrc(c);
     if (rc) return rc;
     vpt::TraceParams tp;
@@ -223,14 +223,15 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc_train_termination = c->nrc_train_termination;
     NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
     const int threads = c->threads > 0 ? c->threads : 128;
-    const bool grid_maj = c->frame.majorant_mode == 1;
+    const bool grid_maj = c->has_volume && c->frame.majorant_mode == 1;
+    const bool surfaces = c->surf != nullptr;
     size_t smem = 0;
     if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {
         tp.maj_in_smem = 1;
         smem = static_cast<size_t>(c->mx) * c->my * c->mz * sizeof(float);
     }
-    const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj), smem);
-    vpt::launch_nrc_pass(tp, mode, grid_maj, ctas, threads, smem, s);
+    const int ctas = vpt::persistent_grid(c, threads, vpt::nrc_kernel_ptr(mode, grid_maj, surfaces), smem);
+    vpt::launch_nrc_pass(tp, mode, grid_maj, surfaces, ctas, threads, smem, s);
     NRCP_CUDA(cudaGetLastError());
     if (stream_mode == 1 && spp > 0) {
         vpt::launch_frame_update(c->d_frame, spp, false, 0, s);

@@ -524,6 +524,10 @@ int fill_trace_params(VptContextImpl* c, TraceParams* tp) {
     tp->phase_kind = f.phase_kind;
     tp->phase_param = f.phase_param;
     tp->world_radius = c->world_radius;
+    for (int a = 0; a < 3; ++a) {
+        tp->world_min[a] = c->world_min[a];
+        tp->world_max[a] = c->world_max[a];
+    }
     tp->max_bounces = f.max_bounces;
     tp->rr_start = f.rr_start_vertex;
     tp->max_steps = f.max_steps_per_segment;

@@ -184,6 +184,26 @@ __device__ __forceinline__ void write_query(float* q, V3 pos, V3 vout, float rou
     p[6] = make_float2(0.0f, 0.0f);
 }
 
+// RadianceQuery of a surface vertex (optix_pathtracing_kernels.cu:14-29 with the BSDF's
+// getSurfaceParameters, common_renderer_types.h:1491-1496 Lambert, 1671-1677 dichromatic):
+// position in the world box, the shading normal and vOut as toPolarYUp outputs, roughness,
+// diffuse and specular reflectance of the material.
+__device__ __forceinline__ void write_query_surface(float* q, V3 pos, V3 normal, V3 vout, const SurfMaterial& m, V3 wmin,
+                                                    V3 wmax) {
+    V3 d = wmax - wmin, r = pos - wmin;
+    float na, nb, va, vb;
+    to_polar_yup_sel(normal, &na, &nb);
+    to_polar_yup_sel(vout, &va, &vb);
+    float2* p = reinterpret_cast<float2*>(q);
+    p[0] = make_float2(d.x != 0 ? r.x / d.x : 0.0f, d.y != 0 ? r.y / d.y : 0.0f);
+    p[1] = make_float2(d.z != 0 ? r.z / d.z : 0.0f, na);
+    p[2] = make_float2(nb, va);
+    p[3] = make_float2(vb, m.roughness);
+    p[4] = make_float2(m.diffuse[0], m.diffuse[1]);
+    p[5] = make_float2(m.diffuse[2], m.specular[0]);
+    p[6] = make_float2(m.specular[1], m.specular[2]);
+}
+
 // Work order of the training pass: item -> pixel of the training image, class by class, where
 // the class of a pixel is (its position in the 4x4 tile + offset) % 16 and class 0 holds the
 // unbiased suffixes (optix_pathtracing_kernels.cu:60-66). The long unbiased paths thus gather in
@@ -231,7 +251,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                                        : kStreams == kStreamsSampleParallel ? kPlainCtasPerSm
                                                                             : kPlainPerPixelCtasPerSm)
     plain_trace_kernel(const TraceParams P) {
-    static_assert(!kSurfaces || (kMode == kModePlain && !kStage), "surfaces: plain mode without leaf staging");
+    static_assert(!kSurfaces || !kStage, "surfaces: no leaf staging");
     const bool sample_parallel = kStreams == kStreamsRuntime ? P.stream_mode == 1 : kStreams == kStreamsSampleParallel;
     extern __shared__ __align__(128) float s_maj[];
     const Grid& g = P.grid;
@@ -375,7 +395,10 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
     // Biased training suffixes end at twice the render factor (optix_pathtracing_kernels.cu:
     // 284-285) unless a separate training factor is set.
     const float train_term_factor = P.nrc_train_termination > 0 ? P.nrc_train_termination : 2 * term_factor;
-    const V3 wmin = bmin, wmax = bmax;
+    // Radiance queries locate positions in the world box (worldDimInfo.aabb,
+    // optix_pathtracing_kernels.cu:19), which is the volume's box unless the scene has meshes.
+    const V3 wmin = kSurfaces ? v3(P.world_min[0], P.world_min[1], P.world_min[2]) : bmin;
+    const V3 wmax = kSurfaces ? v3(P.world_max[0], P.world_max[1], P.world_max[2]) : bmax;
     uint32_t rng_index = 0;
     float primary_spread = 0.0f, sqrt_spread = 0.0f, last_density = 0.0f;
     uint32_t prev_vertex = kInvalidVertex;
@@ -497,6 +520,35 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
         } else {
             st = ST_NEE_DONE;
         }
+    };
+
+    // The path ends at a vertex whose cache query was just written (optix_pathtracing_kernels.cu
+    // :307-330): the training suffix's terminal record, or the render path's terminal info and,
+    // when the render queries are listed, its slot in the inference list.
+    auto end_with_query = [&]() {
+        if (kMayTrain && is_train) {
+            tr_suffix()[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+        } else {
+            TerminalInfo ti;
+            ti.tp[0] = throughput.r;
+            ti.tp[1] = throughput.g;
+            ti.tp[2] = throughput.b;
+            ti.bits = 1u | ((path_length & 0xFFu) << 1);
+            P.nrc.infer_terminal[slot] = ti;
+            if (P.nrc.infer_index) {
+                // List the slot for the inference (one atomic per converged group).
+                const uint32_t m = __activemask();
+                const int leader = __ffs(m) - 1;
+                const uint32_t lane = threadIdx.x & 31;
+                uint32_t base = 0;
+                if (static_cast<int>(lane) == leader) base = atomicAdd(P.nrc.counters + 8, __popc(m));
+                base = __shfl_sync(m, base, leader);
+                P.nrc.infer_index[base + __popc(m & ((1u << lane) - 1u))] = slot;
+            }
+        }
+        terminal_written = true;
+        end_code = END_CACHE;
+        st = ST_END_SAMPLE;
     };
 
     while (true) {
@@ -784,29 +836,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         float* qdst = (kMayTrain && is_train) ? tr_end_query() : P.nrc.infer_query;
                         write_query(qdst + kQueryFloats * static_cast<size_t>(slot), origin, -dir, rough, P.albedo, wmin,
                                     wmax);
-                        if (kMayTrain && is_train) {
-                            tr_suffix()[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
-                        } else {
-                            TerminalInfo ti;
-                            ti.tp[0] = throughput.r;
-                            ti.tp[1] = throughput.g;
-                            ti.tp[2] = throughput.b;
-                            ti.bits = 1u | ((path_length & 0xFFu) << 1);
-                            P.nrc.infer_terminal[slot] = ti;
-                            if (P.nrc.infer_index) {
-                                // List the slot for the inference (one atomic per converged group).
-                                const uint32_t m = __activemask();
-                                const int leader = __ffs(m) - 1;
-                                const uint32_t lane = threadIdx.x & 31;
-                                uint32_t base = 0;
-                                if (static_cast<int>(lane) == leader) base = atomicAdd(P.nrc.counters + 8, __popc(m));
-                                base = __shfl_sync(m, base, leader);
-                                P.nrc.infer_index[base + __popc(m & ((1u << lane) - 1u))] = slot;
-                            }
-                        }
-                        terminal_written = true;
-                        end_code = END_CACHE;
-                        st = ST_END_SAMPLE;
+                        end_with_query();
                         break;
                     }
                 }
@@ -891,6 +921,16 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                     origin = sp.pos;
                     const V3 vout_local = to_local(sp.sf, -dir);
                     const SurfMaterial& mt = P.surf.mats[sp.material];
+                    if constexpr (kNrc) {
+                        // :200-210: path spread, |cos| against the geometric normal.
+                        const V3 dv = ray_origin - origin;
+                        const float dist2 = dv.x * dv.x + dv.y * dv.y + dv.z * dv.z;
+                        const float abs_dot = fabsf(dot(dir, sp.gn));
+                        if (path_length == 1)
+                            primary_spread = dist2 / (4 * kPi * abs_dot);
+                        else
+                            sqrt_spread += sqrtf(dist2 / (dir_pdf * abs_dot));
+                    }
                     if (vout_local.z > 0 && mt.emissive) {
                         const RGB em = rgb(mt.emittance[0], mt.emittance[1], mt.emittance[2]);
                         float mis = 1.0f;
@@ -901,14 +941,46 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                             const float bsdf_pdf = dir_pdf;
                             mis = (bsdf_pdf * bsdf_pdf) / ((bsdf_pdf * bsdf_pdf) + (light_pdf * light_pdf));
                         }
-                        contribution = contribution + throughput * (em * (mis / kPi));
+                        const RGB implicit = em * (mis / kPi);
+                        if (!(kMayTrain && is_train)) contribution = contribution + throughput * implicit;
+                        if (kMayTrain && is_train && prev_vertex != kInvalidVertex) {
+                            // :231-237: the emission completes the previous vertex's target.
+                            const TrainVertexInfo& pv = tr_vertex()[prev_vertex];
+                            float* tg = tr_target0() + 3 * static_cast<size_t>(prev_vertex);
+                            const RGB add = rgb(pv.local_tp[0], pv.local_tp[1], pv.local_tp[2]) * implicit;
+                            tg[0] += add.r;
+                            tg[1] += add.g;
+                            tg[2] += add.b;
+                        }
                     }
                     float continue_prob = 1.0f;
-                    if (static_cast<int32_t>(path_length) >= P.rr_start) {
+                    bool rr_kill = false;
+                    const int32_t rr_from = (kMayTrain && is_train) ? max(P.rr_start, 3) : P.rr_start;
+                    if (static_cast<int32_t>(path_length) >= rr_from) {
                         continue_prob = fminf(luminance(throughput) / init_importance, 1.0f);
-                        if (rng.uniform() >= continue_prob) {
+                        if (rng.uniform() >= continue_prob) rr_kill = true;
+                    }
+                    if constexpr (!kNrc) {
+                        if (rr_kill) {
                             end_code = END_RR;
                             st = ST_END_SAMPLE;
+                            break;
+                        }
+                    } else {
+                        // :282-330 at a surface: the query holds the shading normal and the
+                        // material's reflectances and roughness.
+                        bool ends_with_cache = rr_kill;
+                        const float spread2 = sqrt_spread * sqrt_spread;
+                        if (kMayTrain && is_train) {
+                            if (!unbiased) ends_with_cache |= spread2 > train_term_factor * primary_spread;
+                        } else {
+                            ends_with_cache |= spread2 > term_factor * primary_spread;
+                        }
+                        if (ends_with_cache) {
+                            float* qdst = (kMayTrain && is_train) ? tr_end_query() : P.nrc.infer_query;
+                            write_query_surface(qdst + kQueryFloats * static_cast<size_t>(slot), origin, sp.sf.n, -dir,
+                                                mt, wmin, wmax);
+                            end_with_query();
                             break;
                         }
                     }
@@ -933,8 +1005,10 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         // sampling and the offset origin of the next ray
                         // (optix_pathtracing_kernels.cu:340-356).
                         const SurfPoint sp = surface_point(P.surf, hit_tri, hit_b1, hit_b2, P.env_enabled != 0);
-                        const Bsdf f = make_bsdf(P.surf.mats[sp.material]);
+                        const SurfMaterial& mt = P.surf.mats[sp.material];
+                        const Bsdf f = make_bsdf(mt);
                         const V3 q = to_local(sp.sf, -dir);
+                        RGB nee_s = rgb(0, 0, 0);
                         if (vis > 0.0f) {
                             const V3 sdir = -light_dir;
                             const V3 vin = to_local(sp.sf, -sdir);
@@ -953,7 +1027,8 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                                 const float gterm = nee_lp_cos * sp_cos / nee_dist2;
                                 nee = fs * le * (vis * mis * gterm / area_pdf);
                             }
-                            contribution = contribution + throughput * nee;
+                            if (!(kMayTrain && is_train)) contribution = contribution + throughput * nee;
+                            nee_s = nee;
                         }
                         if (P.max_bounces > 0 && static_cast<int32_t>(path_length) >= P.max_bounces) {
                             end_code = END_MAX_BOUNCES;
@@ -970,6 +1045,7 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                             st = ST_END_SAMPLE;
                             break;
                         }
+                        const V3 v_out = -dir;
                         dir = from_local(sp.sf, local);
                         const float dot_sgn = dot(dir, sp.gn);
                         const RGB local_tp = fs * (fabsf(dot_sgn) / pdf);
@@ -978,6 +1054,35 @@ __global__ void __launch_bounds__(128, kSurfaces                              ? 
                         dir_pdf = pdf;
                         at_surface = false;
                         st = ST_SEGMENT;
+                        if (kMayTrain && is_train) {
+                            // :358-409 at a surface vertex: the query at the surface point (not the
+                            // offset origin), the BSDF's local throughput, the NEE target.
+                            const uint32_t idx = atomicAdd(tr_counters() + tr_buf(), 1u);
+                            if (idx < kTrainBufferSize) {
+                                write_query_surface(tr_query0() + kQueryFloats * static_cast<size_t>(idx), sp.pos, sp.sf.n,
+                                                    v_out, mt, wmin, wmax);
+                                TrainVertexInfo vi;
+                                vi.local_tp[0] = local_tp.r;
+                                vi.local_tp[1] = local_tp.g;
+                                vi.local_tp[2] = local_tp.b;
+                                vi.bits = (prev_vertex & kInvalidVertex) | ((path_length & 0xFFu) << 22) |
+                                          ((unbiased ? 1u : 0u) << 30);
+                                tr_vertex()[idx] = vi;
+                                float* tg = tr_target0() + 3 * static_cast<size_t>(idx);
+                                tg[0] = nee_s.r;
+                                tg[1] = nee_s.g;
+                                tg[2] = nee_s.b;
+                                prev_vertex = idx;
+                            } else {
+                                write_query_surface(tr_end_query() + kQueryFloats * static_cast<size_t>(slot), sp.pos,
+                                                    sp.sf.n, v_out, mt, wmin, wmax);
+                                tr_suffix()[slot] = pack_suffix(prev_vertex, 1, path_length, unbiased ? 1 : 0);
+                                terminal_written = true;
+                                err |= VPT_DEVERR_TRAIN_FULL;
+                                end_code = END_TRAIN_FULL;
+                                st = ST_END_SAMPLE;
+                            }
+                        }
                         break;
                     }
                 }
@@ -1383,37 +1488,29 @@ void launch_surface(const TraceParams& p, bool grid_majorant, int grid_ctas, int
     cudaLaunchKernel(surface_kernel_ptr(grid_majorant, p.dlog != nullptr), dim3(grid_ctas), dim3(threads), args, sm, s);
 }
 
-const void* nrc_kernel_ptr(int mode, bool grid_majorant) {
-    if (mode == kModeTrainNrc)
-        return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeTrainNrc>)
-                             : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeTrainNrc>);
-    if (mode == kModeComboNrc)
-        return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeComboNrc>)
-                             : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeComboNrc>);
-    return grid_majorant ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kModeRenderNrc>)
-                         : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kModeRenderNrc>);
+template <int kMode, bool kSurfaces>
+static const void* nrc_kernel_for(bool grid_majorant) {
+    return grid_majorant
+               ? reinterpret_cast<const void*>(plain_trace_kernel<true, false, kMode, kStreamsRuntime, false, kSurfaces>)
+               : reinterpret_cast<const void*>(plain_trace_kernel<false, false, kMode, kStreamsRuntime, false, kSurfaces>);
 }
 
-void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
-                     cudaStream_t s) {
-    dim3 grid(grid_ctas), block(threads);
-    const size_t sm = grid_majorant ? smem : 0;
-    if (mode == kModeTrainNrc) {
-        if (grid_majorant)
-            plain_trace_kernel<true, false, kModeTrainNrc><<<grid, block, sm, s>>>(p);
-        else
-            plain_trace_kernel<false, false, kModeTrainNrc><<<grid, block, sm, s>>>(p);
-    } else if (mode == kModeComboNrc) {
-        if (grid_majorant)
-            plain_trace_kernel<true, false, kModeComboNrc><<<grid, block, sm, s>>>(p);
-        else
-            plain_trace_kernel<false, false, kModeComboNrc><<<grid, block, sm, s>>>(p);
-    } else {
-        if (grid_majorant)
-            plain_trace_kernel<true, false, kModeRenderNrc><<<grid, block, sm, s>>>(p);
-        else
-            plain_trace_kernel<false, false, kModeRenderNrc><<<grid, block, sm, s>>>(p);
+const void* nrc_kernel_ptr(int mode, bool grid_majorant, bool surfaces) {
+    if (surfaces) {
+        if (mode == kModeTrainNrc) return nrc_kernel_for<kModeTrainNrc, true>(grid_majorant);
+        if (mode == kModeComboNrc) return nrc_kernel_for<kModeComboNrc, true>(grid_majorant);
+        return nrc_kernel_for<kModeRenderNrc, true>(grid_majorant);
     }
+    if (mode == kModeTrainNrc) return nrc_kernel_for<kModeTrainNrc, false>(grid_majorant);
+    if (mode == kModeComboNrc) return nrc_kernel_for<kModeComboNrc, false>(grid_majorant);
+    return nrc_kernel_for<kModeRenderNrc, false>(grid_majorant);
+}
+
+void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, bool surfaces, int grid_ctas, int threads,
+                     size_t smem, cudaStream_t s) {
+    const size_t sm = grid_majorant ? smem : 0;
+    void* args[] = {const_cast<TraceParams*>(&p)};
+    cudaLaunchKernel(nrc_kernel_ptr(mode, grid_majorant, surfaces), dim3(grid_ctas), dim3(threads), args, sm, s);
 }
 
 }  // namespace vpt

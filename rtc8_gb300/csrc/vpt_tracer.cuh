@@ -37,6 +37,7 @@ struct TraceParams {
     int32_t phase_kind;
     float phase_param;
     float world_radius;
+    float world_min[3], world_max[3];  // the world box (volume and instances); the queries' frame
 
     int32_t max_bounces, rr_start, max_steps;
 
@@ -86,10 +87,11 @@ const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parall
 // Plain tracer of scenes with surfaces (either stream layout, logged or not).
 const void* surface_kernel_ptr(bool grid_majorant, bool logged);
 void launch_surface(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
-// Radiance-cache render (kModeRenderNrc) or training (kModeTrainNrc) pass.
-void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, int grid_ctas, int threads, size_t smem,
-                     cudaStream_t s);
-const void* nrc_kernel_ptr(int mode, bool grid_majorant);
+// Radiance-cache render (kModeRenderNrc), training (kModeTrainNrc) or combined (kModeComboNrc)
+// pass; `surfaces`: the instance that also traces the context's triangle meshes.
+void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, bool surfaces, int grid_ctas, int threads,
+                     size_t smem, cudaStream_t s);
+const void* nrc_kernel_ptr(int mode, bool grid_majorant, bool surfaces);
 // Jump table of sample-parallel streams first .. first + count - 1, computed on the device.
 void launch_sample_jump_table(ulonglong2* out, uint32_t first, uint32_t count, cudaStream_t s);
 void launch_finalize_mean(const double* sum, float* mean, uint32_t n_values, uint32_t samples, cudaStream_t s);
