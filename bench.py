@@ -371,6 +371,28 @@ def nrc_equal_error_large(name: str) -> dict:
     return out
 
 
+def nrc_equal_error_room() -> dict:
+    """The radiance cache against the plain tracer to relMSE 1e-3 (held for 3 evaluations) on the
+    mixed scene (the room's meshes around the 64^3 cloud) at 256^2, one seed: 16384-spp FP64 oracle
+    image, plain in chunks of 16 spp, the cache with the reference's query encoding of surface
+    vertices (the hash grid of its `initialize(HashGrid, 2, 0.01f)` call: 2 hidden layers) and
+    the comparison's frame settings; repeated with the reference's own training settings (Adam lr
+    1e-2, weight EMA 0.99) and with its path-termination factor (0.01)."""
+    from rtc8_gb300 import convergence, nrc
+
+    cfg = _cfg("room").replace(name="room_cloud64_256px", width=256, height=256)
+    hg = {"encoding": nrc.NRC_ENCODING_HASHGRID}
+    t0 = time.perf_counter()
+    res = convergence.compare(cfg, target=1e-3, oracle_spp=16384, time_budget=120.0, seeds=1, settings=hg,
+                              extra_settings={"reference_training": dict(hg, ema_decay=0.99, learning_rate=1e-2),
+                                              "reference_termination": dict(hg, termination=0.01,
+                                                                            train_termination=0.02)})
+    out = {k: v for k, v in res.items() if k != "curves"}
+    out["workload"] = f"{cfg.name}: room of 36 triangles (Lambert walls, two SimplePBR blocks, a rectangle light) around the 64^3 cloud, 256x256"
+    out["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def stress_plain(steps: int = 3, warmup: int = 2) -> dict:
     """The plain tracer on the 2048^2 stress scene (1024^3, two unioned fBm clouds, sigma_t max 400,
     albedo 0.9995, g 0.9, <= 1024 bounces), STEP_SPP per launch, device-timed."""
@@ -522,9 +544,9 @@ def main():
                     help="profiling run: only the cache's MLP kernels (inference and training steps)")
     ap.add_argument("--nrc-frames", type=int, default=0,
                     help="profiling run: only the radiance-cache frame loop on the 256x256 scene, N timed frames")
-    ap.add_argument("--nrc-equal-error", default="", choices=["", "c5", "c2"],
-                    help="only the radiance-cache vs plain equal-error comparison on the 2048^2 stress scene (c5) "
-                         "or the 1024^2 sparse scene (c2), one seed")
+    ap.add_argument("--nrc-equal-error", default="", choices=["", "c5", "c2", "room"],
+                    help="only the radiance-cache vs plain equal-error comparison on the 2048^2 stress scene (c5), "
+                         "the 1024^2 sparse scene (c2) or the mixed surface scene at 256^2 (room), one seed")
     ap.add_argument("--nrc-separate-passes", action="store_true",
                     help="with --nrc-frames: first training pass and render samples as two launches")
     ap.add_argument("--leaf-stage", type=int, default=0,
@@ -570,7 +592,8 @@ def main():
         return
     if args.nrc_equal_error:
         torch.cuda.set_device(local)
-        print(json.dumps(nrc_equal_error_large(args.nrc_equal_error)), flush=True)
+        res = nrc_equal_error_room() if args.nrc_equal_error == "room" else nrc_equal_error_large(args.nrc_equal_error)
+        print(json.dumps(res), flush=True)
         return
 
     torch.cuda.set_device(local)

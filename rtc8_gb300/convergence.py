@@ -182,7 +182,9 @@ def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, tim
     """One equal-error comparison on `cfg` (its RNG seed) against the oracle image `ref`."""
     from . import nrc
 
-    net = nrc.default_config(nrc.NRC_ENCODING_VOLUME)
+    # The volume encoding by default; scenes with meshes take the reference's query encodings
+    # (settings "encoding"), whose inputs hold the surface normal, roughness and reflectances.
+    net = nrc.default_config(st.get("encoding", nrc.NRC_ENCODING_VOLUME))
     net.ema_decay = st["ema_decay"]
     net.learning_rate = st["learning_rate"]
     plain = plain_curve(cfg, ref, target, chunk_spp=plain_chunk, time_budget=time_budget)
