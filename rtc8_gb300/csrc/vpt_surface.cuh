@@ -188,6 +188,10 @@ __device__ __forceinline__ float box_entry(const BvhNode& nd, V3 o, V3 inv, floa
 }
 
 constexpr int kBvhStack = 64;
+// Scenes of at most this many world triangles are not traversed: every lane of a warp tests the
+// same triangle in the same step (one broadcast load, no stack, no divergence), which beats a
+// tree whose boxes a small scene's large triangles overlap. Hits and ties are the tree's.
+constexpr uint32_t kFlatTriangles = 64;
 
 struct SurfHit {
     uint32_t tri;   // world triangle, ~0u = none
@@ -199,6 +203,21 @@ struct SurfHit {
 // (the builder bounds the depth below the stack size, so trees it built never do).
 static __device__ __noinline__ SurfHit bvh_closest(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
     SurfHit h{~0u, tmax, 0.0f, 0.0f};
+    if (S.num_tris <= kFlatTriangles) {
+        // Ascending index order: a later triangle replaces the best only when strictly closer.
+        for (uint32_t tri = 0; tri < S.num_tris; ++tri) {
+            float t, b1, b2;
+            if (tri_hit(o, d, ld3(S.tri_pos[3 * tri]), ld3(S.tri_pos[3 * tri + 1]), ld3(S.tri_pos[3 * tri + 2]), tmin,
+                        h.t, &t, &b1, &b2) &&
+                (t < h.t || tri < h.tri)) {
+                h.tri = tri;
+                h.t = t;
+                h.b1 = b1;
+                h.b2 = b2;
+            }
+        }
+        return h;
+    }
     const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     uint32_t stack[kBvhStack];
     int sp = 0;
@@ -256,6 +275,15 @@ static __device__ __noinline__ SurfHit bvh_closest(const Surfaces& S, V3 o, V3 d
 
 // Any hit in [tmin, tmax] (the visibility ray's any-hit program, optix_pathtracing_kernels.cu:7-10).
 static __device__ __noinline__ bool bvh_any(const Surfaces& S, V3 o, V3 d, float tmin, float tmax, bool* overflow) {
+    if (S.num_tris <= kFlatTriangles) {
+        for (uint32_t tri = 0; tri < S.num_tris; ++tri) {
+            float t, b1, b2;
+            if (tri_hit(o, d, ld3(S.tri_pos[3 * tri]), ld3(S.tri_pos[3 * tri + 1]), ld3(S.tri_pos[3 * tri + 2]), tmin,
+                        tmax, &t, &b1, &b2))
+                return true;
+        }
+        return false;
+    }
     const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     uint32_t stack[kBvhStack];
     int sp = 0;

@@ -146,3 +146,35 @@ def room_scene(light_emittance: float = 40.0, light_size: float = 0.5) -> Surfac
     sc.add(box((0.17, 0.25, 0.17), 4), rotation_y(20.0, -0.42, -0.35, -0.35))
     sc.add(box((0.14, 0.14, 0.14), 5), rotation_y(-30.0, 0.45, -0.46, 0.3))
     return sc
+
+
+def sphere(radius: float, material: int, segments: int = 16, rings: int = 8) -> Mesh:
+    """A UV sphere centred at the origin (y up): `rings` bands of `segments` quads, triangles at the
+    poles, smooth shading normals, tangents along the azimuth, every triangle wound so that its
+    geometric normal points outwards."""
+    verts = []
+    for r in range(rings + 1):
+        th = math.pi * r / rings
+        for s in range(segments + 1):
+            ph = 2 * math.pi * s / segments
+            n = (math.sin(th) * math.cos(ph), math.cos(th), math.sin(th) * math.sin(ph))
+            verts.append((*[radius * c for c in n], *n, -math.sin(ph), 0.0, math.cos(ph)))
+    v = np.array(verts, dtype=np.float32)
+
+    def idx(r, s):
+        return r * (segments + 1) + s
+
+    tris = []
+    for r in range(rings):
+        for s in range(segments):
+            a, b, c, d = idx(r, s), idx(r + 1, s), idx(r + 1, s + 1), idx(r, s + 1)
+            if r > 0:
+                tris.append((a, b, d))
+            if r < rings - 1:
+                tris.append((b, c, d))
+    t = np.array(tris, dtype=np.uint32)
+    p = v[:, 0:3]
+    gn = np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]])
+    inward = np.einsum("ij,ij->i", gn, p[t].mean(axis=1)) < 0
+    t[inward] = t[inward][:, ::-1]
+    return Mesh(v, t, material)

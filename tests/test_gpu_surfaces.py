@@ -94,6 +94,21 @@ def test_surfaces_without_volume(cuda_device):
     assert res["gpu"]["counters"]["lookups"] == 0 and res["oracle"]["log"][..., 1:3].sum() == 0
 
 
+def test_tessellated_mesh_through_the_bvh(cuda_device):
+    """Scenes above the flat-list size (64 triangles) are traversed through the BVH: the room
+    with a 224-triangle sphere (smooth shading normals) and two copies of the room's blocks inside
+    the cloud, against the oracle's exhaustive search; both reference and configuration mode."""
+    sc = S.room_scene()
+    sc.add(S.sphere(0.22, 5, 16, 8), S.translation(0.05, 0.05, 0.4))
+    sc.add(S.sphere(0.12, 4, 12, 6), S.translation(-0.35, 0.3, -0.2))
+    assert sc.num_triangles > 64
+    for cfg in (C_ROOM.replace(width=48, height=48), C_ROOM_REFERENCE_MODE.replace(width=40, height=40)):
+        res = run_pair(cfg, sc, 8)
+        check(cfg, res, 8)
+        info = res["gpu"]["info"]
+        assert info["triangles"] == sc.num_triangles and info["bvh_nodes"] > 31
+
+
 def test_instanced_groups_and_transforms(cuda_device):
     """A geometry group (two meshes) placed twice with rotation, scale and translation, and an
     instance whose uniform scale differs from its transform's (the reference's two scales)."""
