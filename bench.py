@@ -304,12 +304,25 @@ def mlp_bench(steps: int, warmup: int) -> dict:
     tr_tf = n_tr * 3 * flop_fwd / t_tr / 1e12
     errors = cache.device_errors()
     cache.finalize()
+    # The reference's own network (its initialize(HashGrid, 2, 0.01f) call): 16 hash-grid levels
+    # of 2 features gathered and interpolated into the first layer's tile, OneBlob(4) angles and
+    # identity reflectances (64 inputs), 2 hidden layers, output None; 2^23 queries and
+    # 16384-record training steps (the tables' scatter-add and their Adam step included).
+    hg = nrc.NeuralRadianceCache()
+    hg.initialize(config=nrc.default_config(nrc.NRC_ENCODING_HASHGRID))
+    flop_hg = 2 * (64 * 64 + 64 * 64 + 64 * 16)
+    t_hi = timed(lambda: hg.infer(s.cuda_stream, q, n_inf, out), max(steps, 10))
+    t_ht = timed(lambda: hg.train(s.cuda_stream, q, tgt, n_tr), max(steps, 10))
+    hashgrid = {"infer_ms": t_hi * 1e3, "infer_queries_per_s": n_inf / t_hi,
+                "infer_mlp_tflops": n_inf * flop_hg / t_hi / 1e12, "train_step_ms": t_ht * 1e3,
+                "train_records_per_s": n_tr / t_ht, "device_errors": hg.device_errors()}
+    hg.finalize()
     return {"metric": "MLP TFLOP/s (padded FP16 network, FP32 accumulation)", "infer_ms": t_inf * 1e3,
             "infer_tflops": inf_tf, "infer_frac_of_peak": inf_tf / peak, "train_step_ms": t_tr * 1e3,
             "train_tflops": tr_tf, "train_frac_of_peak": tr_tf / peak,
             "peak_tflops": peak, "peak_source": "measured bf16_tflops (dense FP16 has the same rate)",
             "infer_records": n_inf, "train_records": n_tr, "train_larger_batches": big,
-            "mma_shape_ceiling": mma_ceiling, "device_errors": errors}
+            "mma_shape_ceiling": mma_ceiling, "hashgrid_reference_network": hashgrid, "device_errors": errors}
 
 
 def nrc_frame_loop(frames: int, warmup: int, combined: bool = True) -> dict:
