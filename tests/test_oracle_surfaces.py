@@ -94,3 +94,41 @@ def test_emitting_closed_room_furnace():
                                 constant_environment(radiance))
     ref = orc.render_plain(env, orc.seed_states(8, 8, cfg.rng_seed), 512)["sum"]
     np.testing.assert_allclose(out.sum(axis=(0, 1)), ref.sum(axis=(0, 1)), rtol=0.02)
+
+
+def test_sphere_mesh_is_closed_and_outward():
+    m = S.sphere(0.5, 0, 12, 6)
+    p = m.vertices[:, 0:3]
+    assert len(m.triangles) == 2 * 12 * (6 - 1)
+    np.testing.assert_allclose(np.linalg.norm(m.vertices[:, 3:6], axis=1), 1.0, rtol=1e-6)
+    np.testing.assert_allclose(np.linalg.norm(p, axis=1), 0.5, rtol=1e-6)
+    t = m.triangles
+    gn = np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]])
+    assert (np.einsum("ij,ij->i", gn, p[t].mean(axis=1)) > 0).all()
+    # closed: the triangles' area approaches the sphere's
+    area = 0.5 * np.linalg.norm(gn, axis=1).sum()
+    assert 0.85 * 4 * math.pi * 0.25 < area < 4 * math.pi * 0.25
+
+
+def test_radiance_cache_queries_at_surfaces():
+    """The oracle's render pass over the room writes surface queries with the shading normal,
+    roughness and the materials' reflectances (Lambert: roughness 1, no specular; SimplePBR:
+    specular F0 > 0), and its training pass records surface vertices."""
+    from rtc8_gb300.configs import C_ROOM_REFERENCE_MODE
+
+    cfg = C_ROOM_REFERENCE_MODE.replace(width=24, height=24)
+    vox = orc.fbm_volume(cfg.volume)
+    sc = orc.scene_from_config(cfg, vox, constant_environment(cfg.env_constant))
+    orc.attach_surfaces(sc, S.room_scene(), True)
+    rng = orc.seed_states(cfg.width, cfg.height, cfg.rng_seed)
+    o = orc.nrc_pass(sc, rng.copy(), 1, cfg.width, cfg.height, termination=0.02)
+    q = o["infer_query"][(o["terminal_bits"] & 1) == 1]
+    assert len(q) > 0.25 * cfg.width * cfg.height
+    assert (q[:, 0:3] >= -1e-5).all() and (q[:, 0:3] <= 1 + 1e-5).all()   # in the world box (walls on its faces)
+    lam = q[:, 7] == 1.0
+    assert lam.any() and (q[lam, 11:14] == 0).all()
+    assert (q[:, 11:14].max(axis=1) > 0).any()
+    t = orc.nrc_pass(sc, rng.copy(), 2, cfg.width // 4, cfg.height // 4, unbiased_offset=7, termination=0.02)
+    n = int(t["num_train"][0])
+    tq = t["train_query"][:n]
+    assert n > 0 and ((tq[:, 7] == 1.0) | (tq[:, 11:14].max(axis=1) > 0)).any()
