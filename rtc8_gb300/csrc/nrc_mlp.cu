@@ -255,7 +255,9 @@ __device__ __forceinline__ void grid_corners(const NetLayout& ly, int lv, const 
         const float wz = (c & 4) ? fr[2] : 1.0f - fr[2];
         w[c] = (wx * wy) * wz;
         const uint32_t i = hashed ? (x ^ (y * 2654435761u) ^ (z * 805459861u)) : (x + (y + z * res) * res);
-        e[c] = off + i % size;
+        // i modulo the level's size without a division: a hashed level has 2^15 entries (a mask);
+        // a dense level's corner indices stay below res^3 + res^2 + res < 2 size (one subtraction).
+        e[c] = off + (hashed ? (i & (size - 1u)) : (i >= size ? i - size : i));
     }
 }
 
