@@ -21,8 +21,12 @@ import numpy as np
 from .configs import C1, SceneConfig, VolumeSpec
 from .renderer import Renderer, setup_scene
 
-# Launch shapes the autotuner tries: (CTAs per SM, park threshold); 0 = the defaults.
+# Launch shapes the autotuner tries: (CTAs per SM, park threshold); 0 = the defaults. The batch's
+# launches run CTAs of 128 threads (BATCH_THREADS): alone, a scene's plain launch is fastest as one
+# 896-thread CTA per SM, but the batch's concurrent launches then cannot share an SM (16 scenes:
+# 606 M paths/s against 647 M with 128-thread CTAs).
 LAUNCH_CANDIDATES = [(0, 0), (0, 16), (0, 28), (6, 24), (5, 24)]
+BATCH_THREADS = 128
 
 
 def make_c4_scenes(count: int = 16, seed: int = 4) -> list[SceneConfig]:
@@ -57,6 +61,7 @@ class SceneBatch:
             # The batch step is one CUDA graph: its launches are the persistent megakernel (the
             # wavefront tracer issues its passes from the host and cannot be captured).
             r.set_tracker(0)
+            r.set_launch_shape(0, BATCH_THREADS, 0)
             self.renderers.append(r)
         self.streams = [torch.cuda.Stream() for _ in self.renderers]
         self.graph = None
@@ -87,7 +92,7 @@ class SceneBatch:
             s = self.streams[i]
             best = None
             for ctas, park in candidates:
-                r.set_launch_shape(ctas, 0, park)
+                r.set_launch_shape(ctas, BATCH_THREADS, park)
                 r.launch_plain(spp, s.cuda_stream)  # warm
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a.record(s)
@@ -97,7 +102,7 @@ class SceneBatch:
                 ms = a.elapsed_time(b)
                 if best is None or ms < best[0]:
                     best = (ms, ctas, park)
-            r.set_launch_shape(best[1], 0, best[2])
+            r.set_launch_shape(best[1], BATCH_THREADS, best[2])
             r.reset_accumulation()
             self.shapes[i] = (best[1], best[2])
             report.append({"scene": self.configs[i].name, "ctas_per_sm": best[1], "park_threshold": best[2],

@@ -222,7 +222,7 @@ int launch_pass(VptContext* c, cudaStream_t s, int mode, uint32_t buf, uint32_t 
     tp.nrc_termination = c->nrc_termination;
     tp.nrc_train_termination = c->nrc_train_termination;
     NRCP_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
-    const int threads = c->threads > 0 ? c->threads : 128;
+    const int threads = c->threads > 0 ? c->threads : (c->surf ? 128 : vpt::kPlainSampleParallelThreads);
     const bool grid_maj = c->has_volume && c->frame.majorant_mode == 1;
     const bool surfaces = c->surf != nullptr;
     size_t smem = 0;

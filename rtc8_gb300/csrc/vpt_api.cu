@@ -574,7 +574,8 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         tp.sample_jumps = c->d_jumps;
     }
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
-    int threads = c->threads > 0 ? c->threads : 128;
+    const bool sp_plain = dlog == nullptr && tp.stream_mode == 1 && !c->surf && c->tracker != 1;
+    int threads = c->threads > 0 ? c->threads : (sp_plain ? vpt::kPlainSampleParallelThreads : 128);
     bool grid_maj = c->frame.majorant_mode == 1 && c->has_volume;
     size_t smem = 0;
     if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {

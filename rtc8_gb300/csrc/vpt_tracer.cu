@@ -58,14 +58,20 @@ constexpr int kNrcCellStepsPerPass = 4;
 // 4.56 ms against 4.75 ms at 20).
 constexpr int kParkThreshold = 20;
 constexpr int kNrcParkThreshold = 24;
-// Resident CTAs of 128 threads per SM the register allocation is bounded for. The plain tracer
-// on sample-parallel streams holds its state in 72 registers at 7 CTAs/SM (1024^2 sparse 512^3:
-// 261 / 284 / 295 / 283 M paths/s at 5 / 6 / 7 / 8); per-pixel streams (and the logged parity
-// kernels) carry per-lane FP64 sums and stay at 5, where they need no spills; the radiance-cache
-// passes measured best at 7 (8 equal).
-constexpr int kPlainCtasPerSm = 7;
+// Resident CTAs per SM the register allocation is bounded for (CTAs of 128 threads unless noted).
+// The plain tracer on sample-parallel streams holds its state in 72 registers at 28 warps per SM
+// (1024^2 sparse 512^3 with 128-thread CTAs: 261 / 284 / 295 / 283 M paths/s at 5 / 6 / 7 / 8 per
+// SM). It runs them as ONE CTA of kPlainSampleParallelThreads = 896 threads per SM: one copy of
+// the staged majorant grid per SM instead of seven leaves more of the SM's L1 to the density
+// gathers (C2 / C5 / C1 per 16-spp launch: 35.0 / 68.4 / 1.17 ms as 7 x 128, 34.5 / 67.8 / 1.14
+// as 2 x 448, 34.0 / 67.0 / 1.13 as 1 x 896; 3 x 256 and 2 x 384, with more registers, slower).
+// Per-pixel streams (and the logged parity kernels) carry per-lane FP64 sums and stay at 5 CTAs
+// of 128, where they need no spills. The radiance-cache passes measured best at 7 x 128 (8 equal)
+// and better still as one 896-thread CTA per SM (256^2 frame: render pass 4.53 -> 4.44 ms, frame
+// 6.28 -> 6.13 ms); over meshes they keep CTAs of 128 (kSurfCtasPerSm).
+constexpr int kPlainCtasPerSm = 1;
 constexpr int kPlainPerPixelCtasPerSm = 5;
-constexpr int kNrcCtasPerSm = 7;
+constexpr int kNrcCtasPerSm = 1;
 // The surface tracer carries the hit, the light sample's geometry and a BVH stack per lane; it
 // is latency-bound (every vertex traverses the BVH twice with divergent loops), and occupancy wins
 // over register spills: room scene 512^2 x 16 spp, 4 / 6 / 8 / 10 / 12 / 16 CTAs per SM ->
@@ -243,10 +249,13 @@ constexpr int kStreamsPerPixel = 0, kStreamsSampleParallel = 1, kStreamsRuntime 
 // finds its closest triangle, volume tracking stops there, surface vertices scatter by their
 // BSDF, NEE also samples the emitting triangles and shadow rays test the triangles for
 // visibility (optix_pathtracing_kernels.cu:84-96, 176-195, 216-239, 268-275, 340-356;
-// renderer_kernel_common.h:72-124, 146-403). Plain mode only.
+// renderer_kernel_common.h:72-124, 146-403), in the plain and the radiance-cache modes.
 template <bool kGridMajorant, bool kLog, int kMode, int kStreams = kStreamsRuntime, bool kStage = false,
           bool kSurfaces = false>
-__global__ void __launch_bounds__(128, kSurfaces                              ? kSurfCtasPerSm
+__global__ void __launch_bounds__(((kMode == kModePlain && kStreams == kStreamsSampleParallel) || kMode != kModePlain) && !kSurfaces
+                                      ? kPlainSampleParallelThreads
+                                      : 128,
+                                  kSurfaces                              ? kSurfCtasPerSm
                                        : kMode != kModePlain                  ? kNrcCtasPerSm
                                        : kStreams == kStreamsSampleParallel ? kPlainCtasPerSm
                                                                             : kPlainPerPixelCtasPerSm)

@@ -87,6 +87,9 @@ const void* plain_kernel_ptr(bool grid_majorant, bool logged, bool sample_parall
 // Plain tracer of scenes with surfaces (either stream layout, logged or not).
 const void* surface_kernel_ptr(bool grid_majorant, bool logged);
 void launch_surface(const TraceParams& p, bool grid_majorant, int grid_ctas, int threads, size_t smem, cudaStream_t s);
+// Threads per CTA of the plain tracer on sample-parallel streams and of the radiance-cache
+// passes without meshes (one CTA per SM); the other forms of the tracer run CTAs of 128 threads.
+constexpr int kPlainSampleParallelThreads = 896;
 // Radiance-cache render (kModeRenderNrc), training (kModeTrainNrc) or combined (kModeComboNrc)
 // pass; `surfaces`: the instance that also traces the context's triangle meshes.
 void launch_nrc_pass(const TraceParams& p, int mode, bool grid_majorant, bool surfaces, int grid_ctas, int threads,
