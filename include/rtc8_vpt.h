@@ -390,10 +390,13 @@ int vpt_set_tracker(VptContext* ctx, int32_t kind, int32_t slots_per_sm, int32_t
  * the same leaf in one tracking step; those lanes read their stencils from it. 0 = off (the
  * default). Decisions and values are those of the unstaged tracker. */
 int vpt_set_leaf_staging(VptContext* ctx, int32_t min_lanes);
-/* Launch shape of the persistent tracker (CTAs per SM, threads per CTA) and the number of
- * parked lanes of a warp that triggers its joint event phase; 0 = defaults (as many 128-thread
- * CTAs as fit: 7 per SM for the plain tracer on sample-parallel streams; park threshold 20 for
- * the plain tracer, 24 for the radiance-cache passes). */
+/* Launch shape of the persistent tracker (CTAs per SM, threads per CTA, a multiple of 32 up to
+ * 128) and the number of parked lanes of a warp that triggers its joint event phase; 0 = defaults:
+ * one CTA of 896 threads per SM for the plain tracer on sample-parallel streams and for the
+ * radiance-cache passes without meshes, as many 128-thread CTAs as fit for the other forms; park
+ * threshold 20 for the plain tracer, 24 for the radiance-cache passes. Contexts whose launches run
+ * concurrently on one GPU (several scenes at once) do better with 128-thread CTAs, which can share
+ * an SM. */
 int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,
                          int32_t park_threshold);
 
