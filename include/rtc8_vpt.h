@@ -394,7 +394,7 @@ int vpt_set_leaf_staging(VptContext* ctx, int32_t min_lanes);
  * 128) and the number of parked lanes of a warp that triggers its joint event phase; 0 = defaults:
  * one CTA of 896 threads per SM for the plain tracer on sample-parallel streams and for the
  * radiance-cache passes without meshes, as many 128-thread CTAs as fit for the other forms; park
- * threshold 20 for the plain tracer, 24 for the radiance-cache passes. Contexts whose launches run
+ * threshold 16 for the plain tracer, 24 for the radiance-cache passes. Contexts whose launches run
  * concurrently on one GPU (several scenes at once) do better with 128-thread CTAs, which can share
  * an SM. */
 int vpt_set_launch_shape(VptContext* ctx, int32_t ctas_per_sm, int32_t threads_per_cta,

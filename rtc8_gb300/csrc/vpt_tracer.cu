@@ -52,11 +52,12 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 // 4.55 ms against 4.68 ms at 16).
 constexpr int kCellStepsPerPass = 16;
 constexpr int kNrcCellStepsPerPass = 4;
-// Parked lanes of a warp that trigger a joint event phase. Plain tracer (C2 / C5 at 7 CTAs/SM):
-// 12 -> 432 / 913, 16 -> 450 / 939, 20 -> 452 / 932, 24 -> 442 / 916, 28 -> 419 / 862 M paths/s;
-// the radiance-cache passes (shorter paths, more event work per path) are faster at 24 (frame
-// 4.56 ms against 4.75 ms at 20).
-constexpr int kParkThreshold = 20;
+// Parked lanes of a warp that trigger a joint event phase. Plain tracer, C2 / C5 / C1 ms per
+// 16-spp launch with a pixel's samples consecutive: 12 -> 30.6 / 55.4 / 1.13, 16 -> 29.6 / 54.6 /
+// 1.15, 20 -> 29.8 / 55.4 / 1.17, 24 -> 31.2 / 58.2 / 1.17, 28 -> 33.6 / 62.1 / 1.15 (with the samples
+// of all pixels interleaved 20 was best); the radiance-cache passes (shorter paths, more event
+// work per path) are fastest at 24 (frame 5.05 ms; 16 / 20 / 28 / 32: 5.31 / 5.09 / 5.06 / 5.23).
+constexpr int kParkThreshold = 16;
 constexpr int kNrcParkThreshold = 24;
 // Resident CTAs per SM the register allocation is bounded for (CTAs of 128 threads unless noted).
 // The plain tracer on sample-parallel streams holds its state in 72 registers at 28 warps per SM
