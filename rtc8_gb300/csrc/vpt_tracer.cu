@@ -46,12 +46,13 @@ enum : uint32_t {
 constexpr uint32_t kHardStepCap = 1u << 24;
 constexpr uint32_t kHardVertexCap = 1u << 16;
 // Majorant-grid cells a lane crosses per tracking iteration before yielding to the warp. With
-// the current arithmetic (C2 / C5 / C1 M paths/s): 2 -> - / 925 / 861, 4 -> 454 / 927 / 852,
-// 8 -> 471 / 979 / 888, 16 -> 480 / 977 / 898, 32 -> 481 / 974 / 870 (1 -> 4 had raised C2 by 12%
-// with IEEE division and libm-accurate functions). The radiance-cache passes keep 4 (frame
-// 4.55 ms against 4.68 ms at 16).
-constexpr int kCellStepsPerPass = 16;
-constexpr int kNrcCellStepsPerPass = 4;
+// a pixel's samples traced consecutively (C2 / C5 ms per 16-spp launch, radiance-cache frame ms):
+// 8 -> 29.3 / 53.7 / 5.02, 16 -> 29.9 / 54.5 / -, 32 -> 29.5 / 54.6 / -; the radiance-cache passes
+// at 4 / 8 / 16: 5.08 / 5.02 / 5.01. Earlier, with the samples of all pixels interleaved (M paths/s):
+// 4 -> 454 / 927, 8 -> 471 / 979, 16 -> 480 / 977, 32 -> 481 / 974 (1 -> 4 had raised C2 by 12% with
+// IEEE division and libm-accurate functions).
+constexpr int kCellStepsPerPass = 8;
+constexpr int kNrcCellStepsPerPass = 8;
 // Parked lanes of a warp that trigger a joint event phase. Plain tracer, C2 / C5 / C1 ms per
 // 16-spp launch with a pixel's samples consecutive: 12 -> 30.6 / 55.4 / 1.13, 16 -> 29.6 / 54.6 /
 // 1.15, 20 -> 29.8 / 55.4 / 1.17, 24 -> 31.2 / 58.2 / 1.17, 28 -> 33.6 / 62.1 / 1.15 (with the samples
