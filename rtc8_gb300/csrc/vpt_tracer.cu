@@ -53,12 +53,15 @@ constexpr uint32_t kHardVertexCap = 1u << 16;
 // IEEE division and libm-accurate functions).
 constexpr int kCellStepsPerPass = 8;
 constexpr int kNrcCellStepsPerPass = 8;
+constexpr int kSurfCellStepsPerPass = 16;
 // Parked lanes of a warp that trigger a joint event phase. Plain tracer, C2 / C5 / C1 ms per
 // 16-spp launch with a pixel's samples consecutive: 12 -> 30.6 / 55.4 / 1.13, 16 -> 29.6 / 54.6 /
 // 1.15, 20 -> 29.8 / 55.4 / 1.17, 24 -> 31.2 / 58.2 / 1.17, 28 -> 33.6 / 62.1 / 1.15 (with the samples
 // of all pixels interleaved 20 was best); the radiance-cache passes (shorter paths, more event
 // work per path) are fastest at 24 (frame 5.05 ms; 16 / 20 / 28 / 32: 5.31 / 5.09 / 5.06 / 5.23).
 constexpr int kParkThreshold = 16;
+// The surface tracer keeps the values it was tuned with (park threshold 20, 16 cells per step).
+constexpr int kSurfParkThreshold = 20;
 constexpr int kNrcParkThreshold = 24;
 // Resident CTAs per SM the register allocation is bounded for (CTAs of 128 threads unless noted).
 // The plain tracer on sample-parallel streams holds its state in 72 registers at 28 warps per SM
@@ -291,7 +294,8 @@ __global__ void __launch_bounds__(((kMode == kModePlain && kStreams == kStreamsS
     const float global_maj = P.density_coeff * g.global_majorant;
     const uint32_t step_cap = P.max_steps > 0 ? static_cast<uint32_t>(P.max_steps) : kHardStepCap;
     const int park_threshold =
-        P.park_threshold > 0 ? P.park_threshold : (kMode == kModePlain ? kParkThreshold : kNrcParkThreshold);
+        P.park_threshold > 0 ? P.park_threshold
+                             : (kMode == kModePlain ? (kSurfaces ? kSurfParkThreshold : kParkThreshold) : kNrcParkThreshold);
     const V3 bmin = v3(g.bbox_min[0], g.bbox_min[1], g.bbox_min[2]);
     const V3 bmax = v3(g.bbox_max[0], g.bbox_max[1], g.bbox_max[2]);
     // Sensor height of the launch's camera (optix_pathtracing_kernels.cu:43-55); the rest of the
@@ -757,7 +761,8 @@ __global__ void __launch_bounds__(((kMode == kModePlain && kStreams == kStreamsS
             }
             case ST_STEP: {
                 const V3 seg_dir = shadow ? -light_dir : dir;
-                constexpr int kCells = kMode == kModePlain ? kCellStepsPerPass : kNrcCellStepsPerPass;
+                constexpr int kCells = kMode == kModePlain ? (kSurfaces ? kSurfCellStepsPerPass : kCellStepsPerPass)
+                                                           : kNrcCellStepsPerPass;
                 const int r = track_pass<kGridMajorant, kCells>(g, maj_grid, P.density_coeff, t1, seg_dir, rng, t, texit,
                                                                 maj, dda, n_cells);
                 if (r == PASS_LOOKUP) {
