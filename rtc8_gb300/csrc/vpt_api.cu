@@ -574,8 +574,6 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
         tp.sample_jumps = c->d_jumps;
     }
     VPT_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned int), s));
-    const bool sp_plain = dlog == nullptr && tp.stream_mode == 1 && !c->surf && c->tracker != 1;
-    int threads = c->threads > 0 ? c->threads : (sp_plain ? vpt::kPlainSampleParallelThreads : 128);
     bool grid_maj = c->frame.majorant_mode == 1 && c->has_volume;
     size_t smem = 0;
     if (grid_maj && c->mx * c->my * c->mz <= vpt::kMajSmemCells) {
@@ -585,6 +583,11 @@ static int launch_plain_impl(VptContext* c, void* stream, uint32_t spp, uint32_t
     // Leaf staging: majorant-grid tracker on sample-parallel streams (and its logged form).
     const bool stage = c->leaf_stage_min > 0 && grid_maj && (dlog != nullptr || tp.stream_mode == 1) && !c->surf;
     tp.leaf_stage_min = stage ? c->leaf_stage_min : 0;
+    // One 896-thread CTA per SM for the production plain tracer on sample-parallel streams; the
+    // other forms (and leaf staging, whose per-warp buffers would exceed the default dynamic
+    // shared-memory limit at 28 warps) run CTAs of 128.
+    const bool sp_plain = dlog == nullptr && tp.stream_mode == 1 && !c->surf && c->tracker != 1 && !stage;
+    const int threads = c->threads > 0 ? c->threads : (sp_plain ? vpt::kPlainSampleParallelThreads : 128);
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
     if (c->surf) {

@@ -227,3 +227,28 @@ def test_leaf_staging_keeps_every_decision(cuda_device, min_lanes):
     np.testing.assert_array_equal(a["log"], b["log"])
     np.testing.assert_allclose(a["sum"], b["sum"], rtol=1e-12, atol=1e-15)   # FP64 atomics in launch order
     assert a["counters"] == b["counters"] and a["errors"] == b["errors"] == 0
+
+
+@pytest.mark.parametrize("stage", [0, 4])
+def test_production_launch_shapes_agree(cuda_device, stage):
+    """The production launch (no decision log, sample-parallel streams: one 896-thread CTA per SM,
+    a pixel's samples consecutive; CTAs of 128 with leaf staging) against the same launch forced to
+    CTAs of 128 threads: each sample's path is the same, so the FP64 sums agree up to the order of
+    the atomic additions, and the RNG seeds are untouched in both."""
+    cfg = small_config_mode(size=48, n=32, g=0.6, majorant_mode=1).replace(rng_stream_mode=1)
+    vox = volume_for(cfg)
+    sums = []
+    for threads in (0, 128):
+        r = Renderer(cfg.width, cfg.height)
+        setup_scene(r, cfg, volume=vox)
+        r.set_leaf_staging(stage)
+        r.set_launch_shape(0, threads, 0)
+        r.launch_plain(8)
+        r.launch_plain(8)
+        r.synchronize()
+        s, n = r.download_sum()
+        assert n == 16 and r.device_errors() == 0
+        sums.append(s)
+        r.close()
+    assert sums[0].sum() > 0
+    np.testing.assert_allclose(sums[0], sums[1], rtol=1e-12, atol=1e-15)
