@@ -60,7 +60,8 @@ constexpr int kSurfCellStepsPerPass = 16;
 // of all pixels interleaved 20 was best); the radiance-cache passes (shorter paths, more event
 // work per path) are fastest at 24 (frame 5.05 ms; 16 / 20 / 28 / 32: 5.31 / 5.09 / 5.06 / 5.23).
 constexpr int kParkThreshold = 16;
-// The surface tracer keeps the values it was tuned with (park threshold 20, 16 cells per step).
+// The surface tracer keeps the values it was tuned with (park threshold 20, 16 cells per step:
+// room scene 512^2 x 16 spp 92.8 ms per launch against 96.7 ms with the volume tracer's 16 and 8).
 constexpr int kSurfParkThreshold = 20;
 constexpr int kNrcParkThreshold = 24;
 // Resident CTAs per SM the register allocation is bounded for (CTAs of 128 threads unless noted).
@@ -80,7 +81,9 @@ constexpr int kNrcCtasPerSm = 1;
 // The surface tracer carries the hit, the light sample's geometry and a BVH stack per lane; it
 // is latency-bound (every vertex traverses the BVH twice with divergent loops), and occupancy wins
 // over register spills: room scene 512^2 x 16 spp, 4 / 6 / 8 / 10 / 12 / 16 CTAs per SM ->
-// 176 / 151 / 137 / 132 / 128 / 121 ms per launch.
+// 176 / 151 / 137 / 132 / 128 / 121 ms per launch through the BVH (with the flat triangle loop:
+// 8 / 12 / 16 -> 110.7 / 102.4 / 96.7 ms; the same 2048 threads as 2 x 1024, 4 x 512 or 8 x 256
+// threads within 1%).
 constexpr int kSurfCtasPerSm = 16;
 
 struct DdaState {
