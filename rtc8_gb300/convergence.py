@@ -168,15 +168,17 @@ def nrc_curve(cfg: SceneConfig, ref: np.ndarray, target: float, net_config=None,
 # Radiance-cache settings of the equal-error comparison, from sweeps on the 64^3 cloud with RNG
 # seeds that the comparison itself does not use, judged by the sustained criterion: the volume
 # cache of rtc8_nrc.h with Adam lr 5e-3; 128 samples per pixel per frame with four training
-# iterations (generate, propagate, shuffle, 4 x 16384-record steps) per frame and five in the
+# iterations (generate, propagate, shuffle, 4 x 16384-record steps) per frame and three in the
 # first frame; render paths end at path-spread factor 0.9 and biased training suffixes at 0.08;
-# inference with an EMA of the weights at decay 0.8. Last sweep (ten held-out seeds, pixel-major
-# sample order): first-frame iterations {5, 6, 7, 8} x render factor {0.9, 1.0, 1.1, 1.28} x decay
-# {0.7, 0.8}: mean speed-up 2.90 at (5, 0.9, 0.8) against 2.75 at the earlier (8, 1.28, 0.8);
-# 96 / 112 / 160 spp per frame, 3 or 5 iterations per frame and decay 0.9 were slower. Render
+# inference with an EMA of the weights at decay 0.8. Sweeps on ten held-out seeds with the
+# pixel-major sample order: first-frame iterations {5, 6, 7, 8} x render factor {0.9, 1.0, 1.1,
+# 1.28} x decay {0.7, 0.8} gave a mean speed-up of 2.90 at (5, 0.9, 0.8) against 2.75 at the
+# earlier (8, 1.28, 0.8); then, with 8 cells per tracking step, first-frame iterations 1 / 2 / 3 /
+# 4 / 5 gave means 2.97 / 3.14 / 3.14 / 3.05 / 2.99 at factor 0.9 (factor 0.8: 3.18 at 2, 3.08 at
+# 3); 96 / 112 / 160 spp per frame, 3 or 5 iterations per frame and decay 0.9 were slower. Render
 # paths use the configuration's shadow-ray roulette; the training suffixes do not.
 NRC_SETTINGS = {"termination": 0.9, "train_termination": 0.08, "ema_decay": 0.8, "learning_rate": 5e-3,
-                "spp_per_frame": 128, "train_iterations": 4, "first_train_iterations": 5}
+                "spp_per_frame": 128, "train_iterations": 4, "first_train_iterations": 3}
 
 
 def compare_once(cfg: SceneConfig, ref: np.ndarray, target: float, st: dict, time_budget: float,
